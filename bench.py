@@ -1,0 +1,383 @@
+"""Benchmark: particle-updates/s of full P3M steps on one GB300.
+
+Workload (the plain method at mid size): 128^3 particles in a periodic
+256 Mpc/h box, Zel'dovich ICs at z = 49 (P(k) ~ k^0.96 T_BBKS^2, sigma_8 = 0.8,
+Omega_m = 0.3, h = 0.7, seeded Philox noise), 256^3 PM mesh, ASMTH = 1.25 mesh
+cells, RCUT = 4.5 r_s, spline softening 2.8 * 0.025 of the mean spacing, short
+range on a 64^3 cell grid, a z = 49 -> 0 run in 200 equal log-a steps.  A step
+is drift + wrap + cell keys + stable radix sort + reorder + PM (deposit, FFT,
+Green's function, FD4 gradient, interpolation) + short range + kick.
+
+`value` = N * K / (device time of K consecutive steps), inputs resident in HBM.
+The W warm-up steps run from the ICs and the state is then reset to the ICs,
+so the timed steps are steps 0..K-1 of the run (K = 200 times the whole run to
+z = 0, late steps are the most clustered).  The working set (positions,
+velocities, forces, keys, sorted copies, 2 x 64 MB mesh) is ~0.3 GB, above the
+129 MB L2, so nothing stays L2-resident from one step to the next.
+
+`e2e` is the same metric through the reference-facing C ABI with host buffers:
+the reference's run loop (run.c:11-20) calling the drop-in move_particles,
+compute_accelerations and advance_and_find_timesteps on a host P[] array, with
+every P[] copy between host and device inside the timed region.
+
+`--impl reference` times the reference's own CPU force path (oracle/_ref, where
+it was compiled) or the oracle's C restatement of it, with all host threads, on
+a bounded sample of each step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SIDE = 128
+BOX_MPC = 256.0
+PM_GRID = 256
+CELL_GRID = 64
+Z_INIT = 49.0
+NSTEPS_RUN = 200
+SEED = 12345
+SOFT_FRAC = 0.025
+WORKLOAD = "plain-128^3-L256-M256-G64-z49to0-200steps"
+
+
+def workload_config():
+    return {"workload": WORKLOAD, "particles": N_SIDE ** 3, "box_mpc_h": BOX_MPC, "pm_grid": PM_GRID,
+            "cell_grid": CELL_GRID, "z_init": Z_INIT, "log_a_steps": NSTEPS_RUN, "seed": SEED,
+            "softening": f"{SOFT_FRAC} mean spacing", "l2": "working set > L2 (no flush)"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_ic():
+    from cuco_gb300 import ics
+    return ics.zeldovich(N_SIDE, BOX_MPC, Z_INIT, SEED)
+
+
+def softening_h(ic):
+    return float(np.float32(2.8 * np.float32(SOFT_FRAC * ic.boxsize / N_SIDE)))
+
+
+def schedule(ic):
+    from cuco_gb300 import fixed_step_schedule
+    return fixed_step_schedule(ic.a, 1.0, NSTEPS_RUN)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ----------------------------------------------------------------- CPU arm
+
+class CpuStep:
+    """The CPU force path on a bounded sample of one step of the workload: the
+    short range for a seeded 1/64 of the targets (scaled to all N; the
+    reference's per-target cost does not depend on which targets are taken),
+    the full PM on the whole mesh, and the drift/kick of all particles."""
+
+    FRAC = 64
+
+    def __init__(self, nthreads: int):
+        import oracle
+        from cuco_gb300 import ics
+        self.ic = make_ic()
+        soft = softening_h(self.ic)
+        self.p = oracle.reference_params(self.ic.boxsize, self.ic.mass, ics.G_INTERNAL, PM_GRID, soft)
+        n = self.ic.n
+        rng = np.random.default_rng(7)
+        self.sub = np.sort(rng.choice(n, n // self.FRAC, replace=False))
+        self.port = oracle.Port()
+        self.kind = "port"
+        self.nthreads = nthreads
+        self.vel = self.ic.canonical_velocity()
+        self.sample = (f"one z=49 step: short range for {len(self.sub)} of {n} targets (x{self.FRAC}), "
+                       f"on the reference's PMGRID^3 = {PM_GRID}^3 cell grid (gravlist.cpp:117-146), "
+                       f"full {PM_GRID}^3 PM (pm_periodic.c:67-314, FP64 FFT), drift+kick of all; "
+                       f"{nthreads} threads")
+
+    def rate(self):
+        ic, p = self.ic, self.p
+        t0 = time.perf_counter()
+        acc = self.port.pp_targets(ic.pos, self.sub, p, PM_GRID, self.nthreads)
+        t_pp = (time.perf_counter() - t0) * self.FRAC
+        t0 = time.perf_counter()
+        apm = self.port.pm(ic.pos, p, PM_GRID, self.nthreads)
+        t_pm = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        x = (ic.pos.astype(np.float64) + self.vel.astype(np.float64) * 1e-3).astype(np.float32)
+        v = (self.vel.astype(np.float64) + apm.astype(np.float64) * 1e-3).astype(np.float32)
+        t_dk = time.perf_counter() - t0
+        del x, v, acc
+        step = t_pp + t_pm + t_dk
+        return self.ic.n / step, {"pp_s_all_targets": t_pp, "pm_s": t_pm, "drift_kick_s": t_dk}
+
+
+def cpu_sample_rate(nthreads: int):
+    cs = CpuStep(nthreads)
+    v, info = cs.rate()
+    return v, cs.kind, cs.sample, info
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    cs = CpuStep(nthreads)
+    kind, sample = cs.kind, cs.sample
+    vals = []
+    info = {}
+    for k in range(args.warmup + args.steps):
+        v, info = cs.rate()
+        if k >= args.warmup:
+            vals.append(v)
+    val = float(len(vals) / np.sum(1.0 / np.array(vals)))
+    line = {
+        "impl": "reference", "metric": "particle-updates/s", "value": val, "unit": "particle-updates/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * (N_SIDE ** 3) / val, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(),
+        "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": nthreads, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": val, "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "detail": info,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- GPU arm
+
+def run_gpu_arm(args, world, rank, local):
+    from cuco_gb300 import Box, BoxConfig, ics, _native
+    lib = _native.load()
+    ic = make_ic()
+    soft = softening_h(ic)
+    a, drift, kick = schedule(ic)
+    vel0 = ic.canonical_velocity()
+    box = Box(BoxConfig(n=ic.n, pm_grid=PM_GRID, cell_grid=CELL_GRID, boxsize=ic.boxsize,
+                        mass=ic.mass, G=ics.G_INTERNAL, softening=soft, device=local))
+    K, W = args.steps, args.warmup
+    box.set_state(ic.pos, vel0)
+    for s in range(W):
+        box.step(drift[s % (NSTEPS_RUN + 1)], kick[s % (NSTEPS_RUN + 1)])
+    box.sync()
+    box.set_state(ic.pos, vel0)
+    box.enable_timing(True)
+    pairs = ctypes.c_uint64()
+    lib.cuco_box_pair_count(box.h, ctypes.byref(pairs), 1)
+    phase = np.zeros(8)
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    dist_barrier(world)
+    box.sync()
+    lib.cuco_box_timer(box.h, 0, None)
+    launches = 0
+    for s in range(K):
+        box.step(drift[s % (NSTEPS_RUN + 1)], kick[s % (NSTEPS_RUN + 1)])
+        t = box.timings()
+        phase += np.array(list(t.values()))
+        launches += box.launches()
+    ms = ctypes.c_float()
+    lib.cuco_box_timer(box.h, 1, ctypes.byref(ms))
+    box.sync()
+    dist_barrier(world)
+    clk = clocks.stop()
+    t_total = dist_max(ms.value / 1e3, world)
+    lib.cuco_box_pair_count(box.h, ctypes.byref(pairs), 1)
+    value = world * ic.n * K / t_total
+    pp_ms = phase[6] / K
+    pair_flops = 20.0 * pairs.value / K
+    peak = ctypes.c_double()
+    _native.check(lib.cuco_fp32_peak(local, ctypes.byref(peak)), "fp32 peak")
+    achieved = pair_flops / (pp_ms * 1e-3) / 1e12
+    phases = {k: round(v / K, 4) for k, v in zip(Box.PHASES, phase)}
+    line = {
+        "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": 1e3 * t_total / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(),
+        "roofline": {"bound": "fp32", "kernel": "k_shortrange", "achieved": achieved,
+                     "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
+                     "traffic": None,
+                     "convention": "20 FP32 flops per in-range pair (pairs counted in-kernel), "
+                                   "peak = measured FMA throughput"},
+        "phase_ms_per_step": phases,
+        "pairs_per_step": pairs.value / K,
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    box.close()
+    if args.e2e_steps:
+        line["e2e"] = run_e2e(min(args.e2e_steps, K), ic, soft, local)
+    if rank == 0 and not args.no_cpu:
+        try:
+            v, kind, sample, info = cpu_sample_rate(os.cpu_count() or 1)
+            line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s",
+                                    "cores": os.cpu_count(), "kind": kind, "sample": sample}
+        except Exception as e:  # the CPU baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(steps, ic, soft, device):
+    """The reference's run loop (run.c:11-20) over the drop-in C ABI with a host
+    P[] array: every call copies P[] to the device and back."""
+    from cuco_gb300 import _native, ics
+    from cuco_gb300._native import All, Header, Particle
+    lib = _native.load()
+    n = ic.n
+    parts = (Particle * n)()
+    raw = np.ctypeslib.as_array(parts).view(np.uint8).reshape(n, 60).view(np.float32)
+    raw[:, 0:3] = ic.pos
+    raw[:, 3] = ic.mass
+    raw[:, 4:7] = ic.canonical_velocity()
+    ti = np.ctypeslib.as_array(parts).view(np.uint8).reshape(n, 60)[:, 52:60].view(np.int32)
+    ti[:] = 0
+    ctypes.c_void_p.in_dll(lib, "P").value = ctypes.addressof(parts)
+    ctypes.c_uint.in_dll(lib, "NumPart").value = n
+    hdr = Header.in_dll(lib, "header")
+    hdr.NumPart, hdr.Mass, hdr.Time, hdr.BoxSize = n, ic.mass, ic.a, ic.boxsize
+    al = All.in_dll(lib, "All")
+    al.NumPart, al.BoxSize, al.Mass = n, ic.boxsize, ic.mass
+    al.G, al.Hubble = ics.G_INTERNAL, ics.HUBBLE_INTERNAL
+    al.Omega0, al.OmegaLambda, al.HubbleParam = 0.3, 0.7, 0.7
+    al.Time = al.TimeBegin = ic.a
+    al.TimeMax = 1.0
+    al.Timebase_interval = (math.log(1.0) - math.log(float(np.float32(ic.a)))) / (1 << 28)
+    al.Ti_Current = 0
+    al.PM_Ti_begstep = al.PM_Ti_endstep = 0
+    eps = np.float32(SOFT_FRAC * ic.boxsize / N_SIDE)
+    al.SofteningHalo, al.SofteningHaloMaxPhys = eps, 1e30
+    # every particle on the PM step: the acceleration criterion never binds
+    al.ErrTolIntAccuracy = 1e30
+    al.MaxSizeTimestep = (math.log(1.0) - math.log(ic.a)) / NSTEPS_RUN
+    al.MinSizeTimestep = 0.0
+    lib.cuco_dropin_configure(PM_GRID, CELL_GRID)
+    lib.set_softenings()
+    lib.long_range_init()
+    lib.linklist_init()
+    lib.init_drift_table()
+
+    def one_step():
+        # find_next_sync_point_and_drift (run.c:28-69) with no output times
+        t_end = ti.reshape(-1, 2)[:, 0]
+        min_glob = int(t_end.min())
+        if min_glob >= al.PM_Ti_endstep:
+            min_glob = al.PM_Ti_endstep
+        lib.move_particles(al.Ti_Current, min_glob)
+        al.Ti_Current = min_glob
+        al.Time = float(al.TimeBegin * math.exp(al.Ti_Current * al.Timebase_interval))
+        lib.compute_accelerations()
+        lib.advance_and_find_timesteps()
+
+    one_step()  # opening force + half kick (untimed warm-up)
+    one_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one_step()
+    dt = time.perf_counter() - t0
+    bytes_per_call = 60 * n
+    return {"value": n * steps / dt, "unit": "particle-updates/s",
+            "h2d_bytes_per_step": 3 * bytes_per_call, "d2h_bytes_per_step": 3 * bytes_per_call,
+            "steps": steps, "path": "drop-in run loop: move_particles + compute_accelerations + "
+                                    "advance_and_find_timesteps on host P[]"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=NSTEPS_RUN)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+    else:
+        run_gpu_arm(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+// Reference-named GPU helpers (gravlist.cu:18-183, radixsort.h:47-81).
+//
+// These keep the reference's signatures and its void/abort error behaviour
+// (cutilSafeCall prints and exits), work on the legacy default stream like the
+// reference, and run the engine's kernels underneath.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace cuco {
+
+struct CapiState {
+    SIMPARAM sim;
+    SOFTPARAM soft;
+    bool have_sim = false;
+    bool have_soft = false;
+    float *table = nullptr;  // device copy of sim.shortrange_table
+    int grid = 64;           // cell grid of calcHash (PMGRID in the reference)
+};
+
+CapiState &capi() {
+    static CapiState s;
+    return s;
+}
+
+void capi_set_grid(int G) { capi().grid = G; }
+
+[[noreturn]] void capi_fail(const char *where, const char *what) {
+    fprintf(stderr, "cuco_gb300: %s failed: %s\n", where, what);
+    exit(1);
+}
+
+void capi_check(cudaError_t e, const char *where) {
+    if (e != cudaSuccess) capi_fail(where, cudaGetErrorString(e));
+}
+
+void capi_status(cuco_status_t s, const char *where) {
+    if (s != CUCO_OK) capi_fail(where, last_error());
+}
+
+}  // namespace cuco
+
+using namespace cuco;
+
+extern "C" {
+
+void cudaInit(void) {
+    int dev = 0;
+    const char *env = getenv("CUCO_DEVICE");
+    if (env) dev = atoi(env);
+    capi_check(cudaSetDevice(dev), "cudaInit");
+}
+
+void allocateArray(void **devPtr, size_t size) { capi_check(cudaMalloc(devPtr, size), "allocateArray"); }
+
+void freeArray(void *devPtr) { capi_check(cudaFree(devPtr), "freeArray"); }
+
+void copyArrayFromDevice(void *host, void *device, int size) {
+    capi_check(cudaMemcpy(host, device, (size_t)size, cudaMemcpyDeviceToHost), "copyArrayFromDevice");
+}
+
+void copyArrayToDevice(void *device, void *host, int offset, int size) {
+    capi_check(cudaMemcpy((char *)device + offset, host, (size_t)size, cudaMemcpyHostToDevice),
+               "copyArrayToDevice");
+}
+
+void setSimParam(SIMPARAM *p) {
+    CapiState &s = capi();
+    s.sim = *p;
+    s.have_sim = true;
+    if (!s.table) capi_check(cudaMalloc(&s.table, sizeof(float) * kNTab), "setSimParam");
+    capi_check(cudaMemcpy(s.table, p->shortrange_table, sizeof(float) * kNTab, cudaMemcpyHostToDevice),
+               "setSimParam");
+}
+
+void setSoftParam(SOFTPARAM *p) {
+    capi().soft = *p;
+    capi().have_soft = true;
+}
+
+void calcHash(uint *gridParticleHash, uint *gridParticleIndex, float *pos, uint numParticles) {
+    CapiState &s = capi();
+    if (!s.have_sim) capi_fail("calcHash", "setSimParam has not been called");
+    capi_status(launch_cell_keys((const float4 *)pos, gridParticleHash, gridParticleIndex,
+                                 numParticles, s.sim.to_grid_fac, s.grid, 0),
+                "calcHash");
+}
+
+void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *sortedPos,
+                                 uint *gridParticleHash, uint *gridParticleIndex, float *oldPos,
+                                 uint numParticles, uint numCells) {
+    capi_status(launch_reorder_start_end(cellStart, cellEnd, (float4 *)sortedPos, gridParticleHash,
+                                         gridParticleIndex, (const float4 *)oldPos, numParticles,
+                                         numCells, 0),
+                "reorderDataAndFindCellStart");
+}
+
+void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridParticleIndex,
+                                 uint *cellStart, uint *cellEnd, uint numParticles, uint numCells) {
+    CapiState &s = capi();
+    if (!s.have_sim || !s.have_soft)
+        capi_fail("cudaForceEvaluateShortrange", "setSimParam/setSoftParam have not been called");
+    int G = (int)llround(cbrt((double)numCells));
+    if ((uint)(G * G * G) != numCells) capi_fail("cudaForceEvaluateShortrange", "numCells is not a cube");
+    ShortRangeParams p;
+    p.boxsize = s.sim.boxsize;
+    p.gridfac = s.sim.to_grid_fac;
+    p.cellw = s.sim.boxsize / G;
+    p.rcut = s.sim.rcut;
+    p.rcut2 = s.sim.rcut2;
+    p.asmthfac = s.sim.asmthfac;
+    p.mass = s.sim.mass;
+    p.G = s.sim.G;
+    p.h = s.soft.h;
+    p.hinv = s.soft.h_inv;
+    p.h3inv = s.soft.h3_inv;
+    p.grid = G;
+    p.n = numParticles;
+    KickArgs k{};
+    capi_status(launch_shortrange(p, (const float4 *)sortedPos, gridParticleIndex, cellStart, cellEnd,
+                                  kCellStartEnd, s.table, (float4 *)gravAccel, k, 0),
+                "cudaForceEvaluateShortrange");
+}
+
+void radixSort(uint *keys, uint *values, uint *tempKeys, uint *tempValues, uint *counters,
+               uint *countersSum, uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
+               uint keyBits, bool flipBits) {
+    (void)countersSum;
+    (void)blockOffsets;
+    (void)scanPlan;
+    if (flipBits) capi_fail("radixSort", "flipBits is not supported");
+    bool in_alt = false;
+    int launches = 0;
+    capi_status(sort_pairs(keys, values, values, tempKeys, tempValues, counters, numElements,
+                           (int)keyBits, 6, 0, &in_alt, &launches),
+                "radixSort");
+    if (in_alt) {
+        capi_check(cudaMemcpyAsync(keys, tempKeys, sizeof(uint) * numElements, cudaMemcpyDeviceToDevice, 0),
+                   "radixSort");
+        capi_check(cudaMemcpyAsync(values, tempValues, sizeof(uint) * numElements,
+                                   cudaMemcpyDeviceToDevice, 0),
+                   "radixSort");
+    }
+}
+
+void radixSortKeysOnly(uint *keys, uint *tempKeys, uint *counters, uint *countersSum,
+                       uint *blockOffsets, CUDPPHandle scanPlan, uint numElements, uint keyBits,
+                       bool flipBits) {
+    (void)countersSum;
+    (void)blockOffsets;
+    (void)scanPlan;
+    if (flipBits) capi_fail("radixSortKeysOnly", "flipBits is not supported");
+    bool in_alt = false;
+    int launches = 0;
+    capi_status(sort_pairs(keys, nullptr, nullptr, tempKeys, nullptr, counters, numElements,
+                           (int)keyBits, 6, 0, &in_alt, &launches),
+                "radixSortKeysOnly");
+    if (in_alt)
+        capi_check(cudaMemcpyAsync(keys, tempKeys, sizeof(uint) * numElements, cudaMemcpyDeviceToDevice, 0),
+                   "radixSortKeysOnly");
+}
+
+void initDeviceParameters(void) {}
+
+void checkCudaError(const char *msg) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) capi_fail(msg ? msg : "checkCudaError", cudaGetErrorString(e));
+}
+
+}  // extern "C"

@@ -1,0 +1,135 @@
+// Shared declarations of the GB300 force engine (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+#include "../../include/cuco_gb300.h"
+
+namespace cuco {
+
+constexpr uint32_t kEmptyCell = 0xffffffffu;
+constexpr int kNTab = CUCO_NTAB;
+
+// ---------------------------------------------------------------- errors
+
+void set_error(const std::string &msg);
+const char *last_error();
+
+#define CUCO_TRY_CUDA(expr)                                                         \
+    do {                                                                            \
+        cudaError_t _e = (expr);                                                    \
+        if (_e != cudaSuccess) {                                                    \
+            ::cuco::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+            return CUCO_ERR_CUDA;                                                   \
+        }                                                                           \
+    } while (0)
+
+#define CUCO_TRY(expr)                         \
+    do {                                       \
+        cuco_status_t _s = (expr);             \
+        if (_s != CUCO_OK) return _s;          \
+    } while (0)
+
+// -------------------------------------------------------------- sorting
+
+// Scratch a sort of n keys needs: alternate key/value buffers and the per-tile
+// digit histogram (radix * tiles entries).
+size_t sort_hist_entries(uint32_t n, int key_bits, int max_radix_bits);
+
+// Stable LSD radix sort of (keys, vals) by the low key_bits bits.  vals_in may
+// be null: the values are then the input positions 0..n-1.  The sorted data
+// ends in (keys, vals) when `result_in_alt` comes back false, else in
+// (keys_alt, vals_alt).  max_radix_bits bounds the digit width (4..8).
+cuco_status_t sort_pairs(uint32_t *keys, uint32_t *vals, const uint32_t *vals_in,
+                         uint32_t *keys_alt, uint32_t *vals_alt, uint32_t *hist, uint32_t n,
+                         int key_bits, int max_radix_bits, cudaStream_t stream,
+                         bool *result_in_alt, int *launches);
+
+// Cell keys of float4 positions (calcHashD rule); idx gets 0..n-1 when non-null.
+cuco_status_t launch_cell_keys(const float4 *pos, uint32_t *keys, uint32_t *idx, uint32_t n,
+                               float gridfac, int G, cudaStream_t stream);
+
+// Reference cell-bound format (cellStart/cellEnd, empty start = 0xffffffff) and
+// the sorted-position gather.
+cuco_status_t launch_reorder_start_end(uint32_t *cell_start, uint32_t *cell_end,
+                                       float4 *sorted_pos, const uint32_t *sorted_keys,
+                                       const uint32_t *perm, const float4 *pos, uint32_t n,
+                                       uint32_t ncells, cudaStream_t stream);
+
+// Engine cell-bound format: cell_off[c] = first sorted index with key >= c,
+// for c in [0, ncells], plus the gather.
+cuco_status_t launch_reorder_offsets(uint32_t *cell_off, float4 *sorted_pos,
+                                     const uint32_t *sorted_keys, const uint32_t *perm,
+                                     const float4 *pos, uint32_t n, uint32_t ncells,
+                                     cudaStream_t stream);
+
+// ----------------------------------------------------------- short range
+
+struct ShortRangeParams {
+    float boxsize;
+    float gridfac;   // G / L in float, the key rule's factor
+    float cellw;     // L / G
+    float rcut, rcut2;
+    float asmthfac;  // 0.5 / asmth * NTAB / 3
+    float mass;      // source mass
+    float G;         // gravitational constant (applied once per target)
+    float h, hinv, h3inv;
+    int grid;        // G
+    uint32_t n;
+};
+
+// Which cell-bound format the kernel reads.
+enum CellFormat { kCellOffsets = 0, kCellStartEnd = 1 };
+
+// Kick applied in the short-range epilogue (null vel: no kick).
+struct KickArgs {
+    float4 *vel;              // original order
+    const float4 *acc_pm_s;   // PM acceleration in sorted order (may be null)
+    float4 *acc_pm_out;       // PM acceleration scattered to original order (may be null)
+    double kick_pp, kick_pm;
+};
+
+// pair_counter: when non-null, the launch adds its in-range pair count to it.
+cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,
+                                const uint32_t *perm, const uint32_t *cell_a,
+                                const uint32_t *cell_b, CellFormat fmt, const float *table,
+                                float4 *acc_out, const KickArgs &kick, cudaStream_t stream,
+                                unsigned long long *pair_counter = nullptr);
+
+// ------------------------------------------------------------------- PM
+
+struct PMPlan {
+    int M;
+    float boxsize;
+    float to_slab_fac;  // M / L in float (pm_periodic.c:42)
+    float mass;
+    float fd_fac;       // G/(pi L) * M/(2L) (pm_periodic.c:85-86)
+    float *rho;         // M^3 real grid (density, then potential)
+    float2 *spec;       // M*M*(M/2+1) complex grid
+    float *green1d;     // M/2+1: exp(-k^2 a) / sinc(pi k/M)^4
+    float2 *twiddle;    // M: exp(-2 pi i t / M)
+};
+
+cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, float mass,
+                             double G);
+void pm_plan_destroy(PMPlan *plan);
+// Long-range acceleration of n positions (any order) into acc (same order).
+cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,
+                        cudaStream_t stream, cudaEvent_t *ev_deposit_done,
+                        cudaEvent_t *ev_fft_done, int *launches);
+
+// ------------------------------------------------------------ integrator
+
+cuco_status_t launch_drift_keys(float4 *pos, const float4 *vel, double drift, float boxsize,
+                                bool do_drift, uint32_t *keys, uint32_t n, float gridfac, int G,
+                                cudaStream_t stream);
+
+// Host FP64 cosmological integrals.
+double cosmo_integral(double a0, double a1, double omega0, double omega_lambda, double hubble,
+                      int power);
+
+}  // namespace cuco

@@ -1,0 +1,593 @@
+// Drop-in replacements for the reference's host force and integrator functions,
+// working on its globals (allvars.h:120-142).
+//
+// The reference host program keeps P[] (array of PARTICLE) in host memory and
+// calls these functions from begrun()/run().  Each call mirrors P[] to the
+// device in one copy, runs the engine's kernels on the mirror, and copies it
+// back, so the host always sees the reference's fields updated in place:
+//   pm_init_periodic / long_range_init   pm_periodic.c:25-43, longrange.c:8-12
+//   pmforce_periodic / long_range_force  pm_periodic.c:67-314, longrange.c:14-22
+//   set_softenings / linklist_init       gravlist.cpp:28-115
+//   gravity_linklist_cuda                gravlist.cpp:148-193
+//   compute_accelerations                accel.c:8-23 (one round trip for wrap+PM+PP)
+//   move_particles / do_box_wrapping     predict.c:10-41
+//   advance_and_find_timesteps           timestep.c:11-94 (individual power-of-two
+//                                        steps, evaluated per particle on the device)
+//   get_timestep                         timestep.c:96-138
+//   init_drift_table, get_*_factor       driftfac.c:14-126 (tables in FP64)
+// The globals themselves are defined weakly here so that the library loads on
+// its own (tests drive it through these symbols); a host program's own
+// allvars.c definitions take precedence.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+extern "C" {
+__attribute__((weak)) unsigned int NumPart;
+__attribute__((weak)) PARTICLE *P;
+__attribute__((weak)) HEADER header;
+__attribute__((weak)) ALL All;
+__attribute__((weak)) float DriftTable[CUCO_DRIFT_TABLE_LENGTH];
+__attribute__((weak)) float GravKickTable[CUCO_DRIFT_TABLE_LENGTH];
+__attribute__((weak)) unsigned int numParticles;
+__attribute__((weak)) unsigned int numGridCells;
+__attribute__((weak)) float *hPos;
+__attribute__((weak)) float *hGravAccel;
+__attribute__((weak)) float *dOldPos;
+__attribute__((weak)) float *dSortedPos;
+__attribute__((weak)) float *dGravAccel;
+__attribute__((weak)) unsigned int *dGridParticleHash;
+__attribute__((weak)) unsigned int *dGridParticleIndex;
+__attribute__((weak)) unsigned int *dCellStart;
+__attribute__((weak)) unsigned int *dCellEnd;
+/* `RadixSort *sorter` (gravlist.cu:20); the drop-in sorts inside
+ * gravity_linklist_cuda and leaves it null. */
+void *sorter;
+}
+
+namespace cuco {
+void capi_set_grid(int G);
+[[noreturn]] void capi_fail(const char *where, const char *what);
+void capi_check(cudaError_t e, const char *where);
+void capi_status(cuco_status_t s, const char *where);
+cuco_status_t scatter4(const float4 *src_sorted, const uint32_t *perm, float4 *dst, uint32_t n,
+                       cudaStream_t stream);
+void shortrange_table(float *t);
+}  // namespace cuco
+
+using namespace cuco;
+
+namespace {
+
+struct DropinState {
+    int pmgrid = 64;
+    int cellgrid = 0;
+    cuco_box_t *box = nullptr;
+    uint32_t box_n = 0;
+    char *dP = nullptr;  // device mirror of P[]
+    size_t dP_n = 0;
+    int *dflag = nullptr;  // timestep error flag + particle
+    double *dtab = nullptr;  // FP64 kick table on the device
+    double drift64[CUCO_DRIFT_TABLE_LENGTH];
+    double kick64[CUCO_DRIFT_TABLE_LENGTH];
+    double logTimeBegin = 0, logTimeMax = 0;
+    bool tables = false;
+    SOFTPARAM soft{};
+    // short-range constants as gravlist.cpp keeps them
+    double h = 0, h_inv = 0, h3_inv = 0;
+};
+
+DropinState &ds() {
+    static DropinState s;
+    return s;
+}
+
+int cell_grid() { return ds().cellgrid > 0 ? ds().cellgrid : ds().pmgrid; }
+
+// ---------------------------------------------------------------- kernels
+
+__global__ void k_unpack_particles(const PARTICLE *__restrict__ p, float4 *__restrict__ pos,
+                                   float4 *__restrict__ vel, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PARTICLE &q = p[i];
+    pos[i] = make_float4(q.Pos[0], q.Pos[1], q.Pos[2], 0.f);
+    if (vel) vel[i] = make_float4(q.Vel[0], q.Vel[1], q.Vel[2], 0.f);
+}
+
+enum { kPackPos = 1, kPackVel = 2, kPackPP = 4, kPackPM = 8 };
+
+__global__ void k_pack_particles(PARTICLE *__restrict__ p, const float4 *__restrict__ pos,
+                                 const float4 *__restrict__ vel, const float4 *__restrict__ app,
+                                 const float4 *__restrict__ apm, uint32_t n, int what) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PARTICLE &q = p[i];
+    if (what & kPackPos) {
+        float4 v = pos[i];
+        q.Pos[0] = v.x;
+        q.Pos[1] = v.y;
+        q.Pos[2] = v.z;
+    }
+    if (what & kPackVel) {
+        float4 v = vel[i];
+        q.Vel[0] = v.x;
+        q.Vel[1] = v.y;
+        q.Vel[2] = v.z;
+    }
+    if (what & kPackPP) {
+        float4 v = app[i];
+        q.GravAccel[0] = v.x;
+        q.GravAccel[1] = v.y;
+        q.GravAccel[2] = v.z;
+    }
+    if (what & kPackPM) {
+        float4 v = apm[i];
+        q.GravPM[0] = v.x;
+        q.GravPM[1] = v.y;
+        q.GravPM[2] = v.z;
+    }
+}
+
+// predict.c:10-41 on the mirror: drift (no wrap) and/or wrap
+__global__ void k_drift_wrap(PARTICLE *__restrict__ p, uint32_t n, double dt, int drift, int wrap,
+                             double boxsize) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PARTICLE &q = p[i];
+    for (int j = 0; j < 3; ++j) {
+        float x = q.Pos[j];
+        if (drift) x = (float)((double)x + (double)q.Vel[j] * dt);
+        if (wrap) {
+            for (int it = 0; it < 64 && x < 0; ++it) x = (float)((double)x + boxsize);
+            for (int it = 0; it < 64 && x >= (float)boxsize; ++it) x = (float)((double)x - boxsize);
+        }
+        q.Pos[j] = x;
+    }
+}
+
+struct TimestepArgs {
+    double fac1, atime, hubble_a, dt_displacement;
+    double errtol, softening_table, min_timestep, timebase_interval;
+    double loga0, loga1;
+    int ti_current;
+    int pm_kick;         // PM kick due this call
+    double pm_dt;        // its factor
+};
+
+__device__ double table_factor(const double *T, double loga0, double loga1, double tbi, int t0,
+                               int t1) {
+    const int n = CUCO_DRIFT_TABLE_LENGTH;
+    double a1 = loga0 + t0 * tbi, a2 = loga0 + t1 * tbi;
+    double u1 = (a1 - loga0) / (loga1 - loga0) * n, u2 = (a2 - loga0) / (loga1 - loga0) * n;
+    int i1 = (int)u1, i2 = (int)u2;
+    if (i1 >= n) i1 = n - 1;
+    if (i2 >= n) i2 = n - 1;
+    double df1 = i1 < 1 ? u1 * T[0] : T[i1 - 1] + (T[i1] - T[i1 - 1]) * (u1 - i1);
+    double df2 = i2 < 1 ? u2 * T[0] : T[i2 - 1] + (T[i2] - T[i2 - 1]) * (u2 - i2);
+    return df2 - df1;
+}
+
+// timestep.c:26-61 and 86-91 per particle
+__global__ void k_timesteps(PARTICLE *__restrict__ p, uint32_t n, TimestepArgs a,
+                            const double *__restrict__ kick_table, int *__restrict__ flag) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PARTICLE &q = p[i];
+    const int TIMEBASE = CUCO_TIMEBASE;
+    if (q.Ti_endstep == a.ti_current) {
+        // get_timestep (timestep.c:96-138)
+        double ax = a.fac1 * q.GravAccel[0], ay = a.fac1 * q.GravAccel[1], az = a.fac1 * q.GravAccel[2];
+        ax += a.fac1 * q.GravPM[0];
+        ay += a.fac1 * q.GravPM[1];
+        az += a.fac1 * q.GravPM[2];
+        double ac = sqrt(ax * ax + ay * ay + az * az);
+        if (ac == 0) ac = 1.0e-30;
+        double dt = sqrt(2 * a.errtol * a.atime * a.softening_table / ac);
+        dt *= a.hubble_a;
+        if (dt >= a.dt_displacement) dt = a.dt_displacement;
+        if (dt < a.min_timestep) dt = a.min_timestep;
+        int ti_step = (int)(dt / a.timebase_interval);
+        if (!(ti_step > 0 && ti_step < TIMEBASE)) {
+            if (atomicCAS(&flag[0], 0, 1) == 0) {
+                flag[1] = (int)i;
+                flag[2] = ti_step;
+            }
+            return;
+        }
+        int ti_min = TIMEBASE;
+        while (ti_min > ti_step) ti_min >>= 1;
+        ti_step = ti_min;
+        if (ti_step > (q.Ti_endstep - q.Ti_begstep)) {
+            if (((TIMEBASE - q.Ti_endstep) % ti_step) > 0) ti_step = q.Ti_endstep - q.Ti_begstep;
+        }
+        if (a.ti_current == TIMEBASE) ti_step = 0;
+        if ((TIMEBASE - a.ti_current) < ti_step) ti_step = TIMEBASE - a.ti_current;
+        int tstart = (q.Ti_begstep + q.Ti_endstep) / 2;
+        int tend = q.Ti_endstep + ti_step / 2;
+        double dt_gravkick = table_factor(kick_table, a.loga0, a.loga1, a.timebase_interval, tstart, tend);
+        q.Ti_begstep = q.Ti_endstep;
+        q.Ti_endstep = q.Ti_begstep + ti_step;
+        for (int j = 0; j < 3; ++j) {
+            float dv = (float)(q.GravAccel[j] * dt_gravkick);
+            q.Vel[j] += dv;
+        }
+    }
+    if (a.pm_kick)
+        for (int j = 0; j < 3; ++j) q.Vel[j] = (float)((double)q.Vel[j] + (double)q.GravPM[j] * a.pm_dt);
+}
+
+// --------------------------------------------------------------- helpers
+
+cuco_config_t dropin_config() {
+    cuco_config_t c{};
+    c.n = NumPart;
+    c.pm_grid = ds().pmgrid;
+    c.cell_grid = cell_grid();
+    c.boxsize = All.BoxSize;
+    c.mass = header.Mass;
+    c.G = All.G;
+    c.asmth = All.Asmth;
+    c.rcut = All.Rcut;
+    c.softening = ds().h > 0 ? (float)ds().h : (All.ForceSoftening > 0 ? All.ForceSoftening : 1.0f);
+    c.mode = CUCO_MODE_PLAIN;
+    c.device = 0;
+    cudaGetDevice(&c.device);
+    return c;
+}
+
+void ensure_box() {
+    DropinState &s = ds();
+    if (s.box && s.box_n == NumPart) return;
+    if (s.box) cuco_box_destroy(s.box);
+    s.box = nullptr;
+    cuco_config_t c = dropin_config();
+    capi_status(cuco_box_create(&c, &s.box), "drop-in engine set-up");
+    s.box_n = NumPart;
+    if (s.dP_n < NumPart) {
+        cudaFree(s.dP);
+        capi_check(cudaMalloc(&s.dP, sizeof(PARTICLE) * (NumPart ? NumPart : 1)), "drop-in P[] mirror");
+        s.dP_n = NumPart;
+    }
+    if (!s.dflag) capi_check(cudaMalloc(&s.dflag, sizeof(int) * 4), "drop-in flag");
+}
+
+struct BoxView {
+    float4 *pos, *vel, *acc_pp, *acc_pm;
+    cudaStream_t stream;
+};
+
+}  // namespace
+
+// engine internals the drop-in reaches into (same library, not exported)
+extern "C" cuco_status_t cuco_box_internal_arrays(cuco_box_t *b, float4 **pos, float4 **vel,
+                                                  float4 **acc_pp, float4 **acc_pm,
+                                                  void **stream, uint32_t **keys, uint32_t **perm,
+                                                  float4 **spos);
+
+namespace {
+
+BoxView view() {
+    BoxView v;
+    void *st = nullptr;
+    uint32_t *k, *pm;
+    float4 *sp;
+    cuco_box_internal_arrays(ds().box, &v.pos, &v.vel, &v.acc_pp, &v.acc_pm, &st, &k, &pm, &sp);
+    v.stream = (cudaStream_t)st;
+    return v;
+}
+
+void upload_P(bool with_vel) {
+    ensure_box();
+    DropinState &s = ds();
+    BoxView v = view();
+    capi_check(cudaMemcpyAsync(s.dP, P, sizeof(PARTICLE) * NumPart, cudaMemcpyHostToDevice, v.stream),
+               "P[] upload");
+    if (NumPart)
+        k_unpack_particles<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((const PARTICLE *)s.dP, v.pos,
+                                                                        with_vel ? v.vel : nullptr, NumPart);
+    capi_check(cudaGetLastError(), "P[] unpack");
+}
+
+void download_P(int what) {
+    DropinState &s = ds();
+    BoxView v = view();
+    if (what && NumPart)
+        k_pack_particles<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((PARTICLE *)s.dP, v.pos, v.vel,
+                                                                      v.acc_pp, v.acc_pm, NumPart, what);
+    capi_check(cudaGetLastError(), "P[] pack");
+    capi_check(cudaMemcpyAsync(P, s.dP, sizeof(PARTICLE) * NumPart, cudaMemcpyDeviceToHost, v.stream),
+               "P[] download");
+    capi_check(cudaStreamSynchronize(v.stream), "P[] download");
+}
+
+void mirror_drift_wrap(double dt, bool drift, bool wrap) {
+    DropinState &s = ds();
+    BoxView v = view();
+    if (NumPart)
+        k_drift_wrap<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((PARTICLE *)s.dP, NumPart, dt,
+                                                                  drift ? 1 : 0, wrap ? 1 : 0,
+                                                                  (double)All.BoxSize);
+    capi_check(cudaGetLastError(), "drift/wrap");
+}
+
+void mirror_to_box(bool with_vel) {
+    DropinState &s = ds();
+    BoxView v = view();
+    if (NumPart)
+        k_unpack_particles<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((const PARTICLE *)s.dP, v.pos,
+                                                                        with_vel ? v.vel : nullptr, NumPart);
+    capi_check(cudaGetLastError(), "P[] unpack");
+}
+
+}  // namespace
+
+extern "C" cuco_status_t cuco_box_mark_state(cuco_box_t *b);
+
+
+extern "C" {
+
+void cuco_dropin_configure(int pmgrid, int cellgrid) {
+    if (pmgrid < 8 || (pmgrid & (pmgrid - 1)) || pmgrid > 1024) capi_fail("cuco_dropin_configure", "pmgrid must be a power of two in [8, 1024]");
+    ds().pmgrid = pmgrid;
+    ds().cellgrid = cellgrid;
+    capi_set_grid(cell_grid());
+}
+
+void pm_init_periodic(void) {
+    All.Asmth = (float)(CUCO_ASMTH * (double)All.BoxSize / ds().pmgrid);
+    All.Rcut = (float)(CUCO_RCUT * (double)All.Asmth);
+    capi_set_grid(cell_grid());
+}
+
+void long_range_init(void) { pm_init_periodic(); }
+
+void pm_init_periodic_allocate(void) { ensure_box(); }
+
+void pm_init_periodic_free(void) {}
+
+void pmforce_periodic(void) {
+    upload_P(false);
+    cuco_box_mark_state(ds().box);
+    capi_status(cuco_box_forces(ds().box, 1, 0), "pmforce_periodic");
+    download_P(kPackPM);
+}
+
+void long_range_force(void) { pmforce_periodic(); }
+
+void set_softenings(void) {
+    if (All.SofteningHalo * All.Time > All.SofteningHaloMaxPhys)
+        All.SofteningTable = All.SofteningHaloMaxPhys / All.Time;
+    else
+        All.SofteningTable = All.SofteningHalo;
+    All.ForceSoftening = (float)(2.8 * All.SofteningTable);
+    DropinState &s = ds();
+    s.h = All.ForceSoftening;
+    s.h_inv = 1.0 / s.h;
+    s.h3_inv = s.h_inv * s.h_inv * s.h_inv;
+    s.soft.h = (float)s.h;
+    s.soft.h_inv = (float)s.h_inv;
+    s.soft.h3_inv = (float)s.h3_inv;
+    if (s.box) cuco_box_set_softening(s.box, s.soft.h);
+}
+
+void linklist_init(void) {
+    DropinState &s = ds();
+    SIMPARAM sim;
+    shortrange_table(sim.shortrange_table);
+    const int G = cell_grid();
+    double to_grid_fac = (float)G / All.BoxSize;
+    sim.boxsize = All.BoxSize;
+    sim.boxhalf = (float)(All.BoxSize / 2.0);
+    sim.to_grid_fac = (float)to_grid_fac;
+    sim.rcut = All.Rcut;
+    sim.rcut2 = (float)((double)All.Rcut * All.Rcut);
+    sim.asmth = All.Asmth;
+    sim.asmthfac = (float)(0.5 / (double)All.Asmth * (CUCO_NTAB / 3.0));
+    sim.mass = header.Mass;
+    sim.G = (float)All.G;
+    numParticles = NumPart;
+    numGridCells = (unsigned)G * G * G;
+    if (s.h <= 0) set_softenings();
+    ensure_box();
+    float4 *pos, *vel, *app, *apm, *spos;
+    uint32_t *keys, *perm;
+    void *st;
+    cuco_box_internal_arrays(s.box, &pos, &vel, &app, &apm, &st, &keys, &perm, &spos);
+    dOldPos = (float *)pos;
+    dSortedPos = (float *)spos;
+    dGravAccel = (float *)app;
+    dGridParticleHash = keys;
+    dGridParticleIndex = perm;
+    setSimParam(&sim);
+}
+
+void copyPosToDevice(void) {
+    upload_P(false);
+    capi_check(cudaStreamSynchronize(view().stream), "copyPosToDevice");
+}
+
+void copyAccelFromDevice(void) {
+    DropinState &s = ds();
+    ensure_box();
+    BoxView v = view();
+    capi_check(cudaMemcpyAsync(s.dP, P, sizeof(PARTICLE) * NumPart, cudaMemcpyHostToDevice, v.stream),
+               "copyAccelFromDevice");
+    download_P(kPackPP);
+}
+
+void gravity_linklist_cuda(void) {
+    set_softenings();
+    upload_P(false);
+    cuco_box_mark_state(ds().box);
+    capi_status(cuco_box_forces(ds().box, 0, 1), "gravity_linklist_cuda");
+    download_P(kPackPP);
+}
+
+void do_box_wrapping(void) {
+    upload_P(false);
+    mirror_drift_wrap(0.0, false, true);
+    download_P(0);
+}
+
+void move_particles(int time0, int time1) {
+    double dt = get_drift_factor(time0, time1);
+    upload_P(false);
+    mirror_drift_wrap(dt, true, false);
+    download_P(0);
+}
+
+void compute_accelerations(void) {
+    set_softenings();
+    upload_P(false);
+    mirror_drift_wrap(0.0, false, true);
+    mirror_to_box(false);
+    cuco_box_mark_state(ds().box);
+    int pm = All.PM_Ti_endstep == All.Ti_Current;
+    capi_status(cuco_box_forces(ds().box, pm, 1), "compute_accelerations");
+    download_P(kPackPos | kPackPP | (pm ? kPackPM : 0));
+}
+
+int get_timestep(int p) {
+    double fac1 = 1 / (All.Time * All.Time);
+    double atime = All.Time;
+    double hubble_a = All.Omega0 / (atime * atime * atime) +
+                      (1 - All.Omega0 - All.OmegaLambda) / (atime * atime) + All.OmegaLambda;
+    hubble_a = All.Hubble * sqrt(hubble_a);
+    double ax = fac1 * P[p].GravAccel[0], ay = fac1 * P[p].GravAccel[1], az = fac1 * P[p].GravAccel[2];
+    ax += fac1 * P[p].GravPM[0];
+    ay += fac1 * P[p].GravPM[1];
+    az += fac1 * P[p].GravPM[2];
+    double ac = sqrt(ax * ax + ay * ay + az * az);
+    if (ac == 0) ac = 1.0e-30;
+    double dt = sqrt(2 * All.ErrTolIntAccuracy * atime * All.SofteningTable / ac);
+    dt *= hubble_a;
+    if (dt >= All.MaxSizeTimestep) dt = All.MaxSizeTimestep;
+    if (dt < All.MinSizeTimestep) {
+        printf("warning: Timestep will be below the limit of MinSizeTimestep!\n");
+        dt = All.MinSizeTimestep;
+    }
+    int ti_step = (int)(dt / All.Timebase_interval);
+    if (!(ti_step > 0 && ti_step < CUCO_TIMEBASE)) {
+        printf("Error: a timestep of size zero was assigned on the integer timeline!\n");
+        printf("ti_step: %d\n", ti_step);
+        exit(1);
+    }
+    return ti_step;
+}
+
+void advance_and_find_timesteps(void) {
+    DropinState &s = ds();
+    if (!s.tables) init_drift_table();
+    upload_P(false);
+    BoxView v = view();
+    TimestepArgs a;
+    a.fac1 = 1 / (All.Time * All.Time);
+    a.atime = All.Time;
+    double h = All.Omega0 / (a.atime * a.atime * a.atime) +
+               (1 - All.Omega0 - All.OmegaLambda) / (a.atime * a.atime) + All.OmegaLambda;
+    a.hubble_a = All.Hubble * sqrt(h);
+    a.dt_displacement = All.MaxSizeTimestep;
+    a.errtol = All.ErrTolIntAccuracy;
+    a.softening_table = All.SofteningTable;
+    a.min_timestep = All.MinSizeTimestep;
+    a.timebase_interval = All.Timebase_interval;
+    a.loga0 = s.logTimeBegin;
+    a.loga1 = s.logTimeMax;
+    a.ti_current = All.Ti_Current;
+    a.pm_kick = 0;
+    a.pm_dt = 0;
+    // global PM step (timestep.c:63-93), scalar on the host
+    if (All.PM_Ti_endstep == All.Ti_Current) {
+        int ti_step = CUCO_TIMEBASE;
+        while (ti_step > (a.dt_displacement / All.Timebase_interval)) ti_step >>= 1;
+        if (ti_step > (All.PM_Ti_endstep - All.PM_Ti_begstep)) {
+            if (((CUCO_TIMEBASE - All.PM_Ti_endstep) % ti_step) > 0)
+                ti_step = All.PM_Ti_endstep - All.PM_Ti_begstep;
+        }
+        if (All.Ti_Current == CUCO_TIMEBASE) ti_step = 0;
+        int tstart = (All.PM_Ti_begstep + All.PM_Ti_endstep) / 2;
+        int tend = All.PM_Ti_endstep + ti_step / 2;
+        a.pm_dt = get_gravkick_factor(tstart, tend);
+        a.pm_kick = 1;
+        All.PM_Ti_begstep = All.PM_Ti_endstep;
+        All.PM_Ti_endstep = All.PM_Ti_begstep + ti_step;
+    }
+    capi_check(cudaMemsetAsync(s.dflag, 0, sizeof(int) * 4, v.stream), "timesteps");
+    if (NumPart)
+        k_timesteps<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((PARTICLE *)s.dP, NumPart, a, s.dtab, s.dflag);
+    capi_check(cudaGetLastError(), "advance_and_find_timesteps");
+    int flag[4];
+    capi_check(cudaMemcpyAsync(flag, s.dflag, sizeof(flag), cudaMemcpyDeviceToHost, v.stream), "timesteps");
+    download_P(0);
+    if (flag[0]) {
+        printf("Error: a timestep of size zero was assigned on the integer timeline!\n");
+        printf("ti_step: %d\n", flag[2]);
+        printf("timebase interval: %g\n", All.Timebase_interval);
+        printf("particle: %d\n", flag[1]);
+        exit(1);
+    }
+}
+
+double drift_integ(double a, void *param) {
+    (void)param;
+    double h = All.Omega0 / (a * a * a) + (1 - All.Omega0 - All.OmegaLambda) / (a * a) + All.OmegaLambda;
+    h = All.Hubble * sqrt(h);
+    return 1 / (h * a * a * a);
+}
+
+double gravkick_integ(double a, void *param) {
+    (void)param;
+    double h = All.Omega0 / (a * a * a) + (1 - All.Omega0 - All.OmegaLambda) / (a * a) + All.OmegaLambda;
+    h = All.Hubble * sqrt(h);
+    return 1 / (h * a * a);
+}
+
+void init_drift_table(void) {
+    DropinState &s = ds();
+    s.logTimeBegin = log(All.TimeBegin);
+    s.logTimeMax = log(All.TimeMax);
+    const int n = CUCO_DRIFT_TABLE_LENGTH;
+    double a0 = exp(s.logTimeBegin);
+    for (int i = 0; i < n; ++i) {
+        double a1 = exp(s.logTimeBegin + ((s.logTimeMax - s.logTimeBegin) / n) * (i + 1));
+        s.drift64[i] = cosmo_integral(a0, a1, All.Omega0, All.OmegaLambda, All.Hubble, 3);
+        s.kick64[i] = cosmo_integral(a0, a1, All.Omega0, All.OmegaLambda, All.Hubble, 2);
+        DriftTable[i] = (float)s.drift64[i];
+        GravKickTable[i] = (float)s.kick64[i];
+    }
+    if (!s.dtab) capi_check(cudaMalloc(&s.dtab, sizeof(double) * n), "init_drift_table");
+    capi_check(cudaMemcpy(s.dtab, s.kick64, sizeof(double) * n, cudaMemcpyHostToDevice), "init_drift_table");
+    s.tables = true;
+}
+
+static double host_table_factor(const double *T, int t0, int t1) {
+    DropinState &s = ds();
+    const int n = CUCO_DRIFT_TABLE_LENGTH;
+    double a1 = s.logTimeBegin + t0 * All.Timebase_interval;
+    double a2 = s.logTimeBegin + t1 * All.Timebase_interval;
+    double u1 = (a1 - s.logTimeBegin) / (s.logTimeMax - s.logTimeBegin) * n;
+    double u2 = (a2 - s.logTimeBegin) / (s.logTimeMax - s.logTimeBegin) * n;
+    int i1 = (int)u1, i2 = (int)u2;
+    if (i1 >= n) i1 = n - 1;
+    if (i2 >= n) i2 = n - 1;
+    double df1 = i1 < 1 ? u1 * T[0] : T[i1 - 1] + (T[i1] - T[i1 - 1]) * (u1 - i1);
+    double df2 = i2 < 1 ? u2 * T[0] : T[i2 - 1] + (T[i2] - T[i2 - 1]) * (u2 - i2);
+    return df2 - df1;
+}
+
+double get_drift_factor(int time0, int time1) {
+    if (!ds().tables) init_drift_table();
+    return host_table_factor(ds().drift64, time0, time1);
+}
+
+double get_gravkick_factor(int time0, int time1) {
+    if (!ds().tables) init_drift_table();
+    return host_table_factor(ds().kick64, time0, time1);
+}
+
+}  // extern "C"

@@ -1,0 +1,672 @@
+// Engine: one resident simulation box per handle and its force/step pipeline.
+//
+// A step (run.c:11-20 for a global timestep) is, on one stream:
+//   k_drift_keys      drift + periodic wrap + cell key (predict.c:10-41,
+//                     gravlist_kernel.cu:92-118), fused
+//   sort_pairs        stable LSD radix sort of (key, index)
+//   reorder           cell offsets + gather of positions into cell order
+//   pm_forces         PM long-range force on the cell-ordered particles
+//   shortrange        P3M short-range force; its epilogue scatters both forces
+//                     to original order and kicks the velocities
+// Particle state (pos, vel, forces) is kept in original particle order so that
+// the permutation the sort produces is the reference's (stable sort of the keys
+// of P[] in index order).
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cuco {
+
+static thread_local std::string g_error;
+
+void set_error(const std::string &msg) { g_error = msg; }
+const char *last_error() { return g_error.c_str(); }
+
+namespace {
+
+__global__ void k_drift_keys(float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                             double drift, float boxsize, int do_drift,
+                             uint32_t *__restrict__ keys, uint32_t n, float gridfac, int G) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    float c[3] = {p.x, p.y, p.z};
+    if (do_drift) {
+        float4 v = vel[i];
+        float vv[3] = {v.x, v.y, v.z};
+        const double L = (double)boxsize;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            // P.Pos += P.Vel * dt_drift (predict.c:19), then the wrap loops
+            // of do_box_wrapping (predict.c:34-38)
+            float x = (float)((double)c[d] + (double)vv[d] * drift);
+            for (int it = 0; it < 8 && x < 0.f; ++it) x = (float)((double)x + L);
+            for (int it = 0; it < 8 && x >= boxsize; ++it) x = (float)((double)x - L);
+            c[d] = x;
+        }
+        pos[i] = make_float4(c[0], c[1], c[2], p.w);
+    }
+    int k[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int v = (int)__fmul_rn(gridfac, c[d]);
+        v = v < 0 ? 0 : v;
+        k[d] = v >= G ? G - 1 : v;
+    }
+    keys[i] = ((uint32_t)k[0] * G + k[1]) * G + k[2];
+}
+
+__global__ void k_scatter4(const float4 *__restrict__ src_sorted, const uint32_t *__restrict__ perm,
+                           float4 *__restrict__ dst, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[perm[i]] = src_sorted[i];
+}
+
+__global__ void k_pack3to4(const float *__restrict__ a, float4 *__restrict__ b, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = make_float4(a[3 * i], a[3 * i + 1], a[3 * i + 2], 0.f);
+}
+
+__global__ void k_unpack4to3(const float4 *__restrict__ b, float *__restrict__ a, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float4 v = b[i];
+        a[3 * i] = v.x;
+        a[3 * i + 1] = v.y;
+        a[3 * i + 2] = v.z;
+    }
+}
+
+// FMA throughput probe: 8 independent dependency chains per thread.
+__global__ void k_fma_probe(float *out, int iters, float m) {
+    float a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-3f + k;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], m, 1e-7f);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int bits_for(uint32_t ncells) {
+    int b = 1;
+    while (b < 32 && (1ull << b) < ncells) ++b;
+    return b;
+}
+
+// ----------------------------------------------------------- FP64 quadrature
+
+struct GL20 {
+    double x[20], w[20];
+    GL20() {
+        const int n = 20;
+        for (int i = 0; i < n; ++i) {
+            double t = cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0.0;
+            for (int it = 0; it < 100; ++it) {
+                double p0 = 1.0, p1 = t;
+                for (int k = 2; k <= n; ++k) {
+                    double p2 = ((2.0 * k - 1.0) * t * p1 - (k - 1.0) * p0) / k;
+                    p0 = p1;
+                    p1 = p2;
+                }
+                dp = n * (t * p1 - p0) / (t * t - 1.0);
+                double dx = p1 / dp;
+                t -= dx;
+                if (fabs(dx) < 1e-16) break;
+            }
+            x[i] = t;
+            w[i] = 2.0 / ((1.0 - t * t) * dp * dp);
+        }
+    }
+};
+
+const GL20 &gl20() {
+    static GL20 g;
+    return g;
+}
+
+struct Integrand {
+    double om, ol, hub;
+    int power;
+    double operator()(double a) const {
+        double h = om / (a * a * a) + (1 - om - ol) / (a * a) + ol;
+        h = hub * sqrt(h);
+        return power == 3 ? 1 / (h * a * a * a) : 1 / (h * a * a);
+    }
+};
+
+double gl_rule(const Integrand &f, double a, double b) {
+    const GL20 &g = gl20();
+    double c = 0.5 * (a + b), h = 0.5 * (b - a), s = 0.0;
+    for (int i = 0; i < 20; ++i) s += g.w[i] * f(c + h * g.x[i]);
+    return s * h;
+}
+
+double gl_adapt(const Integrand &f, double a, double b, double whole, double tol, int depth) {
+    double c = 0.5 * (a + b);
+    double l = gl_rule(f, a, c), r = gl_rule(f, c, b);
+    if (depth > 40 || fabs(l + r - whole) <= tol) return l + r;
+    return gl_adapt(f, a, c, l, 0.5 * tol, depth + 1) + gl_adapt(f, c, b, r, 0.5 * tol, depth + 1);
+}
+
+}  // namespace
+
+double cosmo_integral(double a0, double a1, double omega0, double omega_lambda, double hubble,
+                      int power) {
+    Integrand f{omega0, omega_lambda, hubble, power};
+    if (a1 == a0) return 0.0;
+    double whole = gl_rule(f, a0, a1);
+    return gl_adapt(f, a0, a1, whole, 1e-13 * fabs(whole) + 1e-300, 0);
+}
+
+cuco_status_t launch_drift_keys(float4 *pos, const float4 *vel, double drift, float boxsize,
+                                bool do_drift, uint32_t *keys, uint32_t n, float gridfac, int G,
+                                cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    k_drift_keys<<<(n + 255) / 256, 256, 0, stream>>>(pos, vel, drift, boxsize, do_drift ? 1 : 0,
+                                                      keys, n, gridfac, G);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t scatter4(const float4 *src_sorted, const uint32_t *perm, float4 *dst, uint32_t n,
+                       cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    k_scatter4<<<(n + 255) / 256, 256, 0, stream>>>(src_sorted, perm, dst, n);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t pack3to4(const float *a, float4 *b, uint32_t n, cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    k_pack3to4<<<(n + 255) / 256, 256, 0, stream>>>(a, b, n);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t unpack4to3(const float4 *b, float *a, uint32_t n, cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    k_unpack4to3<<<(n + 255) / 256, 256, 0, stream>>>(b, a, n);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+void shortrange_table(float *t) {
+    for (int i = 0; i < kNTab; ++i) {
+        double u = 3.0 / kNTab * (i + 0.5);
+        t[i] = (float)(erfc(u) + 2.0 * u / sqrt(M_PI) * exp(-u * u));
+    }
+}
+
+}  // namespace cuco
+
+using namespace cuco;
+
+struct cuco_box {
+    cuco_config_t cfg;
+    uint32_t n = 0;
+    int M = 0, G = 0;
+    uint32_t ncells = 0;
+    int key_bits = 0;
+    float gridfac = 0.f;
+    cudaStream_t stream = nullptr;
+    float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr;
+    float4 *spos = nullptr, *acc_pm_s = nullptr;
+    uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr;
+    uint32_t *hist = nullptr, *cell_off = nullptr;
+    uint32_t *sorted_keys = nullptr, *sorted_perm = nullptr;  // where the last sort ended
+    float *table = nullptr;
+    float *stage3 = nullptr;  // n x 3 staging for host/device float3 transfers
+    PMPlan pm{};
+    bool has_state = false;
+    bool timing = false;
+    cudaEvent_t ev[8] = {};
+    float last_ms[8] = {};
+    int launches = 0;
+    unsigned long long *pair_counter = nullptr;
+    cudaEvent_t tstart = nullptr, tstop = nullptr;
+};
+
+namespace {
+
+template <typename T>
+cuco_status_t alloc(T **p, size_t count) {
+    cudaError_t e = cudaMalloc(p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return CUCO_ERR_NOMEM;
+    }
+    return CUCO_OK;
+}
+
+ShortRangeParams make_sr_params(const cuco_box *b) {
+    ShortRangeParams p;
+    p.boxsize = b->cfg.boxsize;
+    p.gridfac = b->gridfac;
+    p.cellw = b->cfg.boxsize / b->G;
+    p.rcut = b->cfg.rcut;
+    p.rcut2 = b->cfg.rcut * b->cfg.rcut;
+    p.asmthfac = (float)(0.5 / (double)b->cfg.asmth * (kNTab / 3.0));
+    p.mass = b->cfg.mass;
+    p.G = (float)b->cfg.G;
+    p.h = b->cfg.softening;
+    p.hinv = (float)(1.0 / (double)b->cfg.softening);
+    p.h3inv = p.hinv * p.hinv * p.hinv;
+    p.grid = b->G;
+    p.n = b->n;
+    return p;
+}
+
+void record(cuco_box *b, int i) {
+    if (b->timing) cudaEventRecord(b->ev[i], b->stream);
+}
+
+// keys must already be in b->keys; runs sort, reorder, PM, short range (+kick)
+cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kick) {
+    bool in_alt = false;
+    CUCO_TRY(sort_pairs(b->keys, b->perm, nullptr, b->keys_alt, b->perm_alt, b->hist, b->n,
+                        b->key_bits, 8, b->stream, &in_alt, &b->launches));
+    b->sorted_keys = in_alt ? b->keys_alt : b->keys;
+    b->sorted_perm = in_alt ? b->perm_alt : b->perm;
+    record(b, 2);
+    CUCO_TRY(launch_reorder_offsets(b->cell_off, b->spos, b->sorted_keys, b->sorted_perm, b->pos,
+                                    b->n, b->ncells, b->stream));
+    b->launches += 1;
+    record(b, 3);
+    if (pm) {
+        CUCO_TRY(pm_forces(b->pm, b->spos, b->n, b->acc_pm_s, b->stream,
+                           b->timing ? &b->ev[4] : nullptr, b->timing ? &b->ev[5] : nullptr,
+                           &b->launches));
+    } else {
+        record(b, 4);
+        record(b, 5);
+    }
+    record(b, 6);
+    if (pp) {
+        KickArgs k{};
+        if (kick) k = *kick;
+        k.acc_pm_s = pm ? b->acc_pm_s : nullptr;
+        k.acc_pm_out = pm ? b->acc_pm : nullptr;
+        CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, b->sorted_perm, b->cell_off,
+                                   nullptr, kCellOffsets, b->table, b->acc_pp, k, b->stream,
+                                   b->timing ? b->pair_counter : nullptr));
+        b->launches += 1;
+    } else if (pm) {
+        CUCO_TRY(scatter4(b->acc_pm_s, b->sorted_perm, b->acc_pm, b->n, b->stream));
+        b->launches += 1;
+    }
+    record(b, 7);
+    return CUCO_OK;
+}
+
+cuco_status_t finish_timing(cuco_box *b) {
+    if (!b->timing) return CUCO_OK;
+    CUCO_TRY_CUDA(cudaEventSynchronize(b->ev[7]));
+    for (int i = 0; i < 7; ++i) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]);
+        b->last_ms[i] = ms;
+    }
+    float tot = 0.f;
+    cudaEventElapsedTime(&tot, b->ev[0], b->ev[7]);
+    b->last_ms[7] = tot;
+    return CUCO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cuco_last_error(void) { return cuco::last_error(); }
+const char *cuco_version(void) { return "cuco_gb300 0.1 (sm_103a)"; }
+
+cuco_status_t cuco_config_reference(cuco_config_t *cfg) {
+    if (!cfg || cfg->pm_grid <= 0 || !(cfg->boxsize > 0)) {
+        set_error("cuco_config_reference: pm_grid and boxsize must be set");
+        return CUCO_ERR_INVALID;
+    }
+    // pm_periodic.c:27-28: All.Asmth and All.Rcut are float
+    float asmth = (float)(CUCO_ASMTH * (double)cfg->boxsize / cfg->pm_grid);
+    cfg->asmth = asmth;
+    cfg->rcut = (float)(CUCO_RCUT * (double)asmth);
+    if (cfg->cell_grid <= 0) cfg->cell_grid = cfg->pm_grid;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
+    if (!cfg || !out) {
+        set_error("cuco_box_create: null argument");
+        return CUCO_ERR_INVALID;
+    }
+    if (cfg->n < 0 || cfg->n > 0xfffffff0ll || cfg->cell_grid < 4 || cfg->cell_grid > 1024 ||
+        !(cfg->boxsize > 0) || !(cfg->rcut > 0) || !(cfg->asmth > 0) || !(cfg->softening > 0)) {
+        set_error("cuco_box_create: invalid configuration");
+        return CUCO_ERR_INVALID;
+    }
+    if (cfg->mode != CUCO_MODE_PLAIN) {
+        set_error("cuco_box_create: only CUCO_MODE_PLAIN is built in this version");
+        return CUCO_ERR_UNSUPPORTED;
+    }
+    CUCO_TRY_CUDA(cudaSetDevice(cfg->device));
+    cuco_box *b = new cuco_box();
+    b->cfg = *cfg;
+    b->n = (uint32_t)cfg->n;
+    b->M = cfg->pm_grid;
+    b->G = cfg->cell_grid;
+    b->ncells = (uint32_t)b->G * b->G * b->G;
+    b->key_bits = bits_for(b->ncells);
+    b->gridfac = (float)b->G / cfg->boxsize;  // float division as gravlist.cpp:61
+    cuco_status_t s = CUCO_OK;
+    auto fail = [&](cuco_status_t st) {
+        cuco_box_destroy(b);
+        return st;
+    };
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        delete b;
+        return CUCO_ERR_CUDA;
+    }
+    const size_t n = b->n;
+    if ((s = alloc(&b->pos, n)) || (s = alloc(&b->vel, n)) || (s = alloc(&b->acc_pp, n)) ||
+        (s = alloc(&b->acc_pm, n)) || (s = alloc(&b->spos, n)) || (s = alloc(&b->acc_pm_s, n)) ||
+        (s = alloc(&b->keys, n)) || (s = alloc(&b->perm, n)) || (s = alloc(&b->keys_alt, n)) ||
+        (s = alloc(&b->perm_alt, n)) ||
+        (s = alloc(&b->hist, sort_hist_entries(b->n, b->key_bits, 8))) ||
+        (s = alloc(&b->cell_off, (size_t)b->ncells + 1)) || (s = alloc(&b->table, kNTab)) ||
+        (s = alloc(&b->stage3, 3 * n)) || (s = alloc(&b->pair_counter, 1)))
+        return fail(s);
+    cudaMemset(b->pair_counter, 0, sizeof(unsigned long long));
+    std::vector<float> t(kNTab);
+    shortrange_table(t.data());
+    if (cudaMemcpy(b->table, t.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("table upload failed");
+        return fail(CUCO_ERR_CUDA);
+    }
+    if ((s = pm_plan_create(&b->pm, b->M, cfg->boxsize, cfg->asmth, cfg->mass, cfg->G))) return fail(s);
+    cudaMemsetAsync(b->acc_pp, 0, sizeof(float4) * (n ? n : 1), b->stream);
+    cudaMemsetAsync(b->acc_pm, 0, sizeof(float4) * (n ? n : 1), b->stream);
+    cudaMemsetAsync(b->vel, 0, sizeof(float4) * (n ? n : 1), b->stream);
+    for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[i]);
+    cudaEventCreate(&b->tstart);
+    cudaEventCreate(&b->tstop);
+    *out = b;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_destroy(cuco_box_t *b) {
+    if (!b) return CUCO_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    cudaFree(b->pos);
+    cudaFree(b->vel);
+    cudaFree(b->acc_pp);
+    cudaFree(b->acc_pm);
+    cudaFree(b->spos);
+    cudaFree(b->acc_pm_s);
+    cudaFree(b->keys);
+    cudaFree(b->perm);
+    cudaFree(b->keys_alt);
+    cudaFree(b->perm_alt);
+    cudaFree(b->hist);
+    cudaFree(b->cell_off);
+    cudaFree(b->table);
+    cudaFree(b->stage3);
+    cudaFree(b->pair_counter);
+    if (b->tstart) cudaEventDestroy(b->tstart);
+    if (b->tstop) cudaEventDestroy(b->tstop);
+    if (b->pm.rho) pm_plan_destroy(&b->pm);
+    for (int i = 0; i < 8; ++i)
+        if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_set_state(cuco_box_t *b, const float *pos, const float *vel, int on_device) {
+    if (!b || !pos) {
+        set_error("cuco_box_set_state: null argument");
+        return CUCO_ERR_INVALID;
+    }
+    const size_t bytes = sizeof(float) * 3 * b->n;
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, pos, bytes, kind, b->stream));
+    CUCO_TRY(pack3to4(b->stage3, b->pos, b->n, b->stream));
+    if (vel) {
+        CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, vel, bytes, kind, b->stream));
+        CUCO_TRY(pack3to4(b->stage3, b->vel, b->n, b->stream));
+    }
+    b->has_state = true;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_get_state(cuco_box_t *b, float *pos, float *vel, float *acc_pp,
+                                 float *acc_pm, int on_device) {
+    if (!b) {
+        set_error("cuco_box_get_state: null box");
+        return CUCO_ERR_INVALID;
+    }
+    const size_t bytes = sizeof(float) * 3 * b->n;
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    float *dst[4] = {pos, vel, acc_pp, acc_pm};
+    float4 *src[4] = {b->pos, b->vel, b->acc_pp, b->acc_pm};
+    for (int k = 0; k < 4; ++k) {
+        if (!dst[k]) continue;
+        CUCO_TRY(unpack4to3(src[k], b->stage3, b->n, b->stream));
+        CUCO_TRY_CUDA(cudaMemcpyAsync(dst[k], b->stage3, bytes, kind, b->stream));
+    }
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_set_softening(cuco_box_t *b, float h) {
+    if (!b || !(h > 0)) {
+        set_error("cuco_box_set_softening: invalid argument");
+        return CUCO_ERR_INVALID;
+    }
+    b->cfg.softening = h;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_forces(cuco_box_t *b, int pm, int pp) {
+    if (!b || !b->has_state) {
+        set_error("cuco_box_forces: no state uploaded");
+        return CUCO_ERR_STATE;
+    }
+    b->launches = 0;
+    record(b, 0);
+    CUCO_TRY(launch_drift_keys(b->pos, b->vel, 0.0, b->cfg.boxsize, false, b->keys, b->n,
+                               b->gridfac, b->G, b->stream));
+    b->launches += 1;
+    record(b, 1);
+    CUCO_TRY(forces_after_keys(b, pm, pp, nullptr));
+    CUCO_TRY(finish_timing(b));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_step(cuco_box_t *b, double drift, double kick_pp, double kick_pm) {
+    if (!b || !b->has_state) {
+        set_error("cuco_box_step: no state uploaded");
+        return CUCO_ERR_STATE;
+    }
+    b->launches = 0;
+    record(b, 0);
+    CUCO_TRY(launch_drift_keys(b->pos, b->vel, drift, b->cfg.boxsize, drift != 0.0, b->keys, b->n,
+                               b->gridfac, b->G, b->stream));
+    b->launches += 1;
+    record(b, 1);
+    KickArgs k{};
+    k.vel = b->vel;
+    k.kick_pp = kick_pp;
+    k.kick_pm = kick_pm;
+    CUCO_TRY(forces_after_keys(b, 1, 1, &k));
+    CUCO_TRY(finish_timing(b));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_run(cuco_box_t *b, int nsteps, const double *drift, const double *kick_pp,
+                           const double *kick_pm) {
+    if (!b || nsteps < 0 || (nsteps && (!drift || !kick_pp || !kick_pm))) {
+        set_error("cuco_box_run: invalid argument");
+        return CUCO_ERR_INVALID;
+    }
+    for (int s = 0; s < nsteps; ++s) CUCO_TRY(cuco_box_step(b, drift[s], kick_pp[s], kick_pm[s]));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_sync(cuco_box_t *b) {
+    if (!b) return CUCO_ERR_INVALID;
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_stream(cuco_box_t *b, void **stream) {
+    if (!b || !stream) return CUCO_ERR_INVALID;
+    *stream = (void *)b->stream;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_enable_timing(cuco_box_t *b, int enable) {
+    if (!b) return CUCO_ERR_INVALID;
+    b->timing = enable != 0;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_timings(cuco_box_t *b, float *ms) {
+    if (!b || !ms) return CUCO_ERR_INVALID;
+    memcpy(ms, b->last_ms, sizeof(b->last_ms));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_debug(cuco_box_t *b, uint32_t *sorted_keys, uint32_t *perm,
+                             uint32_t *cell_start, uint32_t *cell_end) {
+    if (!b || !b->sorted_keys) {
+        set_error("cuco_box_debug: no forces computed yet");
+        return CUCO_ERR_STATE;
+    }
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    const size_t n = b->n;
+    if (sorted_keys) CUCO_TRY_CUDA(cudaMemcpy(sorted_keys, b->sorted_keys, 4 * n, cudaMemcpyDeviceToHost));
+    if (perm) CUCO_TRY_CUDA(cudaMemcpy(perm, b->sorted_perm, 4 * n, cudaMemcpyDeviceToHost));
+    if (cell_start || cell_end) {
+        std::vector<uint32_t> off(b->ncells + 1);
+        CUCO_TRY_CUDA(cudaMemcpy(off.data(), b->cell_off, 4 * off.size(), cudaMemcpyDeviceToHost));
+        for (uint32_t c = 0; c < b->ncells; ++c) {
+            bool empty = off[c] == off[c + 1];
+            if (cell_start) cell_start[c] = empty ? kEmptyCell : off[c];
+            if (cell_end) cell_end[c] = empty ? kEmptyCell : off[c + 1];
+        }
+    }
+    return CUCO_OK;
+}
+
+int cuco_box_launches_per_step(cuco_box_t *b) { return b ? b->launches : 0; }
+
+cuco_status_t cuco_box_pair_count(cuco_box_t *b, uint64_t *pairs, int reset) {
+    if (!b || !pairs) return CUCO_ERR_INVALID;
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    unsigned long long v = 0;
+    CUCO_TRY_CUDA(cudaMemcpy(&v, b->pair_counter, sizeof(v), cudaMemcpyDeviceToHost));
+    *pairs = v;
+    if (reset) CUCO_TRY_CUDA(cudaMemset(b->pair_counter, 0, sizeof(v)));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_timer(cuco_box_t *b, int op, float *ms) {
+    if (!b) return CUCO_ERR_INVALID;
+    if (op == 0) {
+        CUCO_TRY_CUDA(cudaEventRecord(b->tstart, b->stream));
+        return CUCO_OK;
+    }
+    CUCO_TRY_CUDA(cudaEventRecord(b->tstop, b->stream));
+    CUCO_TRY_CUDA(cudaEventSynchronize(b->tstop));
+    float t = 0.f;
+    CUCO_TRY_CUDA(cudaEventElapsedTime(&t, b->tstart, b->tstop));
+    if (ms) *ms = t;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_pinned_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return CUCO_ERR_INVALID;
+    CUCO_TRY_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_pinned_free(void *ptr) {
+    CUCO_TRY_CUDA(cudaFreeHost(ptr));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_fp32_peak(int device, double *tflops) {
+    if (!tflops) return CUCO_ERR_INVALID;
+    CUCO_TRY_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CUCO_TRY_CUDA(cudaGetDeviceProperties(&prop, device));
+    const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 4096;
+    float *out = nullptr;
+    CUCO_TRY_CUDA(cudaMalloc(&out, sizeof(float) * blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; ++rep) {
+        cudaEventRecord(e0);
+        k_fma_probe<<<blocks, threads>>>(out, iters, 1.0f + 1e-7f);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (e != cudaSuccess) {
+        set_error(cudaGetErrorString(e));
+        return CUCO_ERR_CUDA;
+    }
+    // 8 independent chains x iters FMAs x 2 flops per thread
+    double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return CUCO_OK;
+}
+
+// Internal (hidden) helpers for the drop-in layer in the same library.
+__attribute__((visibility("hidden"))) cuco_status_t cuco_box_internal_arrays(
+    cuco_box_t *b, float4 **pos, float4 **vel, float4 **acc_pp, float4 **acc_pm, void **stream,
+    uint32_t **keys, uint32_t **perm, float4 **spos) {
+    *pos = b->pos;
+    *vel = b->vel;
+    *acc_pp = b->acc_pp;
+    *acc_pm = b->acc_pm;
+    *stream = (void *)b->stream;
+    *keys = b->keys;
+    *perm = b->perm;
+    *spos = b->spos;
+    return CUCO_OK;
+}
+
+__attribute__((visibility("hidden"))) cuco_status_t cuco_box_mark_state(cuco_box_t *b) {
+    b->has_state = true;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_cosmo_factors(double a0, double a1, double omega0, double omega_lambda,
+                                 double hubble, double *drift, double *kick) {
+    if (!(a0 > 0) || !(a1 > 0)) {
+        set_error("cuco_cosmo_factors: scale factors must be positive");
+        return CUCO_ERR_INVALID;
+    }
+    if (drift) *drift = cosmo_integral(a0, a1, omega0, omega_lambda, hubble, 3);
+    if (kick) *kick = cosmo_integral(a0, a1, omega0, omega_lambda, hubble, 2);
+    return CUCO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,398 @@
+// Long-range PM force: CIC deposit, 3D real FFT with the Green's function,
+// FD4 gradient and CIC interpolation, all on the device.
+//
+// Reference: pmforce_periodic (pm_periodic.c:67-314), which deposits and
+// interpolates on the host and round-trips the grid through cuFFT.  Here:
+//   k_deposit      CIC mass assignment (pm_periodic.c:97-132) with float atomics
+//                  into an M^3 grid; the particles arrive cell-sorted, so a
+//                  warp's atomics hit a few neighbouring mesh cells.
+//   k_fft_z_r2c    real->complex along z.  Two real rows are packed as the real
+//                  and imaginary parts of one complex row, transformed together
+//                  and separated (X1 = (Z + conj Z_-k)/2, X2 = (Z - conj Z_-k)/2i).
+//   k_fft_axis     complex transforms along y, and along x fused with the
+//                  Green's-function multiply and the inverse x transform: the
+//                  x pass is the last forward and the first inverse pass, so the
+//                  spectrum is multiplied in shared memory and never stored.
+//   k_fft_z_c2r    the inverse of k_fft_z_r2c (Hermitian extension of each row,
+//                  imaginary parts of the self-conjugate points dropped).
+//   k_interp       the FD4 gradient of the potential (pm_periodic.c:205-270) at
+//                  the 8 CIC corners of each particle and the CIC interpolation
+//                  (pm_periodic.c:272-309), fused: the three force grids the
+//                  reference builds are never materialised.
+// All transforms are unnormalised with cuFFT's sign conventions; each 1D
+// transform is a shared-memory Stockham radix-4 (one radix-2 stage when
+// log2 M is odd) over a batch of columns, twiddles from an FP64-built table.
+// The Green's function factorises: smth(k) = -g(kx) g(ky) g(kz) / k^2 with
+// g(k) = exp(-k^2 (2 pi asmth / L)^2) / sinc(pi k / M)^4, built in FP64.
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cuco {
+
+namespace {
+
+constexpr int kFFTThreads = 256;
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// Transform B columns of length M held in x[m*pitch + b]; returns the buffer
+// holding the result.  sign = -1: forward (e^{-i}), +1: inverse.
+__device__ float2 *fft_columns(float2 *x, float2 *y, const float2 *tw, int M, int B, int pitch,
+                               int sign) {
+    int Ns = 1;
+    float2 *in = x, *out = y;
+    while (Ns < M) {
+        const int r = ((M / Ns) & 3) == 0 ? 4 : 2;
+        const int nb = M / r;
+        const int step = M / (Ns * r);
+        for (int e = threadIdx.x; e < nb * B; e += blockDim.x) {
+            const int b = e % B, j = e / B;
+            const int k = j % Ns;
+            const int dst = (j / Ns) * Ns * r + k;
+            if (r == 4) {
+                float2 v0 = in[j * pitch + b];
+                float2 v1 = in[(j + nb) * pitch + b];
+                float2 v2 = in[(j + 2 * nb) * pitch + b];
+                float2 v3 = in[(j + 3 * nb) * pitch + b];
+                if (k) {
+                    float2 w1 = tw[k * step], w2 = tw[2 * k * step], w3 = tw[3 * k * step];
+                    if (sign > 0) {
+                        w1.y = -w1.y;
+                        w2.y = -w2.y;
+                        w3.y = -w3.y;
+                    }
+                    v1 = cmul(v1, w1);
+                    v2 = cmul(v2, w2);
+                    v3 = cmul(v3, w3);
+                }
+                float2 a0 = make_float2(v0.x + v2.x, v0.y + v2.y);
+                float2 a1 = make_float2(v0.x - v2.x, v0.y - v2.y);
+                float2 a2 = make_float2(v1.x + v3.x, v1.y + v3.y);
+                float2 d = make_float2(v1.x - v3.x, v1.y - v3.y);
+                // (v1 - v3) * (sign * i)
+                float2 a3 = sign < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+                out[dst * pitch + b] = make_float2(a0.x + a2.x, a0.y + a2.y);
+                out[(dst + Ns) * pitch + b] = make_float2(a1.x + a3.x, a1.y + a3.y);
+                out[(dst + 2 * Ns) * pitch + b] = make_float2(a0.x - a2.x, a0.y - a2.y);
+                out[(dst + 3 * Ns) * pitch + b] = make_float2(a1.x - a3.x, a1.y - a3.y);
+            } else {
+                float2 v0 = in[j * pitch + b];
+                float2 v1 = in[(j + nb) * pitch + b];
+                if (k) {
+                    float2 w1 = tw[k * step];
+                    if (sign > 0) w1.y = -w1.y;
+                    v1 = cmul(v1, w1);
+                }
+                out[dst * pitch + b] = make_float2(v0.x + v1.x, v0.y + v1.y);
+                out[(dst + Ns) * pitch + b] = make_float2(v0.x - v1.x, v0.y - v1.y);
+            }
+        }
+        __syncthreads();
+        float2 *t = in;
+        in = out;
+        out = t;
+        Ns *= r;
+    }
+    return in;
+}
+
+__device__ __forceinline__ void load_twiddles(float2 *tw_s, const float2 *tw, int M) {
+    for (int i = threadIdx.x; i < M; i += blockDim.x) tw_s[i] = tw[i];
+}
+
+// rows r0 .. r0+2P-1 of the M^3 real grid (row = x*M + y) -> spectrum rows
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_z_r2c(const float *__restrict__ rho, float2 *__restrict__ spec, const float2 *tw, int M,
+                int P) {
+    extern __shared__ float2 sm[];
+    const int pitch = P + 1;
+    float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
+    const int Mh = M / 2 + 1;
+    const size_t r0 = (size_t)blockIdx.x * 2 * P;
+    load_twiddles(tw_s, tw, M);
+    for (int e = threadIdx.x; e < 2 * P * M; e += blockDim.x) {
+        int row = e / M, m = e % M;
+        float v = rho[(r0 + row) * M + m];
+        float *slot = reinterpret_cast<float *>(&x[m * pitch + (row >> 1)]);
+        slot[row & 1] = v;
+    }
+    __syncthreads();
+    float2 *res = fft_columns(x, y, tw_s, M, P, pitch, -1);
+    for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) {
+        int row = e / Mh, k = e % Mh, pr = row >> 1;
+        float2 z = res[k * pitch + pr];
+        float2 zc = res[((M - k) % M) * pitch + pr];
+        zc.y = -zc.y;
+        float2 o;
+        if ((row & 1) == 0)
+            o = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
+        else  // (z - zc) / (2i)
+            o = make_float2(0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x));
+        spec[(r0 + row) * Mh + k] = o;
+    }
+}
+
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_z_c2r(const float2 *__restrict__ spec, float *__restrict__ out, const float2 *tw, int M,
+                int P) {
+    extern __shared__ float2 sm[];
+    const int pitch = P + 1;
+    float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
+    const int Mh = M / 2 + 1;
+    const size_t r0 = (size_t)blockIdx.x * 2 * P;
+    load_twiddles(tw_s, tw, M);
+    // rows into y as h[row*Mh + k]
+    for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) {
+        int row = e / Mh, k = e % Mh;
+        float2 v = spec[(r0 + row) * Mh + k];
+        if (k == 0 || k == M / 2) v.y = 0.f;
+        y[row * Mh + k] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < P * M; e += blockDim.x) {
+        int pr = e % P, k = e / P;
+        float2 a, b;
+        if (k <= M / 2) {
+            a = y[(2 * pr) * Mh + k];
+            b = y[(2 * pr + 1) * Mh + k];
+        } else {
+            a = y[(2 * pr) * Mh + (M - k)];
+            b = y[(2 * pr + 1) * Mh + (M - k)];
+            a.y = -a.y;
+            b.y = -b.y;
+        }
+        x[k * pitch + pr] = make_float2(a.x - b.y, a.y + b.x);  // a + i b
+    }
+    __syncthreads();
+    float2 *res = fft_columns(x, y, tw_s, M, P, pitch, +1);
+    for (int e = threadIdx.x; e < 2 * P * M; e += blockDim.x) {
+        int row = e / M, m = e % M;
+        float2 z = res[m * pitch + (row >> 1)];
+        out[(r0 + row) * M + m] = (row & 1) ? z.y : z.x;
+    }
+}
+
+// axis 1: y transform for fixed x = blockIdx.y; axis 0: x transform for fixed
+// y = blockIdx.y, with the Green's multiply and inverse transform when green != 0.
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_axis(float2 *__restrict__ spec, const float2 *tw, const float *__restrict__ green1d,
+               int M, int B, int axis, int sign, int green) {
+    extern __shared__ float2 sm[];
+    const int pitch = B;
+    float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
+    const int Mh = M / 2 + 1;
+    const int o = blockIdx.y;
+    const int kz0 = blockIdx.x * B;
+    const int nb = min(B, Mh - kz0);
+    const size_t sm_stride = axis == 1 ? (size_t)Mh : (size_t)M * Mh;
+    const size_t base = axis == 1 ? (size_t)o * M * Mh : (size_t)o * Mh;
+    load_twiddles(tw_s, tw, M);
+    for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
+        int m = e / B, b = e % B;
+        x[m * pitch + b] = b < nb ? spec[base + m * sm_stride + kz0 + b] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    float2 *res = fft_columns(x, y, tw_s, M, B, pitch, sign);
+    if (green) {
+        // res holds the full forward transform: k index m along x, y index o, kz0+b
+        const int ky = o <= M / 2 ? o : M - o;
+        const float gy = green1d[ky];
+        for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
+            int m = e / B, b = e % B;
+            int kx = m <= M / 2 ? m : M - m;
+            int kz = kz0 + b;
+            float2 v = res[m * pitch + b];
+            float g = 0.f;
+            if (b < nb) {
+                int k2 = kx * kx + ky * ky + kz * kz;
+                if (k2 > 0) g = -green1d[kx] * gy * green1d[kz] / (float)k2;
+            }
+            res[m * pitch + b] = make_float2(v.x * g, v.y * g);
+        }
+        __syncthreads();
+        float2 *other = res == x ? y : x;
+        res = fft_columns(res, other, tw_s, M, B, pitch, +1);
+    }
+    for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
+        int m = e / B, b = e % B;
+        if (b < nb) spec[base + m * sm_stride + kz0 + b] = res[m * pitch + b];
+    }
+}
+
+__device__ __forceinline__ void cic_axis(float to_slab_fac, float p, int M, int *s, int *ss,
+                                         float *d) {
+    float t = __fmul_rn(to_slab_fac, p);  // pm_periodic.c:99 in float
+    int sl = (int)t;
+    if (sl >= M) sl = M - 1;
+    if (sl < 0) sl = 0;
+    *d = __fsub_rn(t, (float)sl);
+    *s = sl;
+    *ss = sl + 1 >= M ? sl + 1 - M : sl + 1;
+}
+
+__global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__restrict__ rho,
+                          int M, float to_slab_fac, float mass) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    int sx, sxx, sy, syy, sz, szz;
+    float dx, dy, dz;
+    cic_axis(to_slab_fac, p.x, M, &sx, &sxx, &dx);
+    cic_axis(to_slab_fac, p.y, M, &sy, &syy, &dy);
+    cic_axis(to_slab_fac, p.z, M, &sz, &szz, &dz);
+    const size_t Mz = M, Myz = (size_t)M * M;
+    float m0 = mass * (1.f - dx), m1 = mass * dx;
+    atomicAdd(&rho[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz));
+    atomicAdd(&rho[sx * Myz + syy * Mz + sz], m0 * dy * (1.f - dz));
+    atomicAdd(&rho[sx * Myz + sy * Mz + szz], m0 * (1.f - dy) * dz);
+    atomicAdd(&rho[sx * Myz + syy * Mz + szz], m0 * dy * dz);
+    atomicAdd(&rho[sxx * Myz + sy * Mz + sz], m1 * (1.f - dy) * (1.f - dz));
+    atomicAdd(&rho[sxx * Myz + syy * Mz + sz], m1 * dy * (1.f - dz));
+    atomicAdd(&rho[sxx * Myz + sy * Mz + szz], m1 * (1.f - dy) * dz);
+    atomicAdd(&rho[sxx * Myz + syy * Mz + szz], m1 * dy * dz);
+}
+
+__device__ __forceinline__ int wrapi(int a, int M) { return a < 0 ? a + M : (a >= M ? a - M : a); }
+
+__global__ void k_interp(const float4 *__restrict__ pos, uint32_t n, const float *__restrict__ phi,
+                         int M, float to_slab_fac, float fac, float4 *__restrict__ acc) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    int s[3][2];
+    float d[3];
+    cic_axis(to_slab_fac, p.x, M, &s[0][0], &s[0][1], &d[0]);
+    cic_axis(to_slab_fac, p.y, M, &s[1][0], &s[1][1], &d[1]);
+    cic_axis(to_slab_fac, p.z, M, &s[2][0], &s[2][1], &d[2]);
+    const size_t Mz = M, Myz = (size_t)M * M;
+    float wx[2] = {1.f - d[0], d[0]}, wy[2] = {1.f - d[1], d[1]}, wz[2] = {1.f - d[2], d[2]};
+    float out[3];
+#pragma unroll
+    for (int dim = 0; dim < 3; ++dim) {
+        float a = 0.f;
+#pragma unroll
+        for (int cx = 0; cx < 2; ++cx)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+                for (int cz = 0; cz < 2; ++cz) {
+                    int X = s[0][cx], Y = s[1][cy], Z = s[2][cz];
+                    int c[3] = {X, Y, Z};
+                    float f[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        int off = q == 0 ? -1 : q == 1 ? 1 : q == 2 ? -2 : 2;
+                        int cc[3] = {c[0], c[1], c[2]};
+                        cc[dim] = wrapi(cc[dim] + off, M);
+                        f[q] = __ldg(&phi[cc[0] * Myz + cc[1] * Mz + cc[2]]);
+                    }
+                    float F = fac * ((4.0f / 3.0f) * (f[0] - f[1]) - (1.0f / 6.0f) * (f[2] - f[3]));
+                    a += F * wx[cx] * wy[cy] * wz[cz];
+                }
+        out[dim] = a;
+    }
+    acc[i] = make_float4(out[0], out[1], out[2], 0.f);
+}
+
+int fft_batch_z(int M) {
+    int P = 4096 / M;
+    if (P > 16) P = 16;
+    if (P > M / 2) P = M / 2;  // k_fft_z_c2r stages 2P rows of M/2+1 in an M*(P+1) buffer
+    if (P < 1) P = 1;
+    // P pairs per CTA must divide the M*M/2 row pairs
+    while (P > 1 && ((M * M / 2) % P)) P >>= 1;
+    return P;
+}
+
+int fft_batch_axis(int M) {
+    int B = 4096 / M;
+    if (B > 16) B = 16;
+    if (B < 1) B = 1;
+    return B;
+}
+
+}  // namespace
+
+cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, float mass,
+                             double G) {
+    if (M < 8 || M > 1024 || (M & (M - 1))) {
+        set_error("PM mesh size must be a power of two in [8, 1024]");
+        return CUCO_ERR_UNSUPPORTED;
+    }
+    plan->M = M;
+    plan->boxsize = boxsize;
+    plan->to_slab_fac = (float)M / boxsize;
+    plan->mass = mass;
+    double fac = G / (M_PI * (double)boxsize);
+    fac *= (double)(1.0f / (2.0f * boxsize / (float)M));
+    plan->fd_fac = (float)fac;
+    const size_t Mh = M / 2 + 1;
+    CUCO_TRY_CUDA(cudaMalloc(&plan->rho, sizeof(float) * (size_t)M * M * M));
+    CUCO_TRY_CUDA(cudaMalloc(&plan->spec, sizeof(float2) * (size_t)M * M * Mh));
+    CUCO_TRY_CUDA(cudaMalloc(&plan->green1d, sizeof(float) * Mh));
+    CUCO_TRY_CUDA(cudaMalloc(&plan->twiddle, sizeof(float2) * M));
+    std::vector<float> g(Mh);
+    double asmth2 = (2 * M_PI) * (double)asmth / (double)boxsize;
+    asmth2 *= asmth2;
+    for (size_t k = 0; k < Mh; ++k) {
+        double e = exp(-(double)(k * k) * asmth2);
+        double f = 1.0;
+        if (k) {
+            f = (M_PI * (double)k) / M;
+            f = sin(f) / f;
+        }
+        g[k] = (float)(e / (f * f * f * f));
+    }
+    std::vector<float2> tw(M);
+    for (int t = 0; t < M; ++t) tw[t] = make_float2((float)cos(2 * M_PI * t / M), (float)-sin(2 * M_PI * t / M));
+    CUCO_TRY_CUDA(cudaMemcpy(plan->green1d, g.data(), sizeof(float) * Mh, cudaMemcpyHostToDevice));
+    CUCO_TRY_CUDA(cudaMemcpy(plan->twiddle, tw.data(), sizeof(float2) * M, cudaMemcpyHostToDevice));
+    const int P = fft_batch_z(M), B = fft_batch_axis(M);
+    size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
+    size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
+    CUCO_TRY_CUDA(cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
+    CUCO_TRY_CUDA(cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
+    CUCO_TRY_CUDA(cudaFuncSetAttribute(k_fft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
+    return CUCO_OK;
+}
+
+void pm_plan_destroy(PMPlan *plan) {
+    cudaFree(plan->rho);
+    cudaFree(plan->spec);
+    cudaFree(plan->green1d);
+    cudaFree(plan->twiddle);
+    plan->rho = nullptr;
+    plan->spec = nullptr;
+}
+
+cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,
+                        cudaStream_t stream, cudaEvent_t *ev_deposit_done, cudaEvent_t *ev_fft_done,
+                        int *launches) {
+    const int M = plan.M, Mh = M / 2 + 1;
+    const int P = fft_batch_z(M), B = fft_batch_axis(M);
+    const size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
+    const size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
+    CUCO_TRY_CUDA(cudaMemsetAsync(plan.rho, 0, sizeof(float) * (size_t)M * M * M, stream));
+    if (n) k_deposit<<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.mass);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    if (ev_deposit_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_deposit_done, stream));
+    const unsigned zblocks = (unsigned)((size_t)M * M / (2 * P));
+    k_fft_z_r2c<<<zblocks, kFFTThreads, smz, stream>>>(plan.rho, plan.spec, plan.twiddle, M, P);
+    dim3 ag((Mh + B - 1) / B, M);
+    k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, -1, 0);
+    k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 0, -1, 1);
+    k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, +1, 0);
+    k_fft_z_c2r<<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, M, P);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    if (ev_fft_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_fft_done, stream));
+    if (n) k_interp<<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.fd_fac, acc);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    if (launches) *launches += 8;
+    return CUCO_OK;
+}
+
+}  // namespace cuco

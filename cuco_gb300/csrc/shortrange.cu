@@ -1,0 +1,379 @@
+// Short-range P3M pair force on the cell grid.
+//
+// Reference: cudaForceEvaluateShortrangeD + calcForce (gravlist_kernel.cu:20-88,
+// 162-234) and the CPU force_evaluate_shortrange (gravlist.cpp:216-338).  The
+// pair law is the reference's: min-image separation, cut at r^2 > rcut^2, 1/r^2
+// outside the spline softening length h and GADGET's spline inside, times the
+// nearest-bin erfc split factor T[(int)(asmthfac*r)] (NTAB = 1000 bins).
+//
+// Layout of the work (GB300-first rather than one thread per particle over a
+// full cube of cells):
+//   * one CTA per z-segment of S consecutive cells (ix, iy, iz0..iz0+S-1); its
+//     targets are one contiguous range of the cell-sorted particles;
+//   * the sources are the cells of the neighbour columns (dx, dy) whose
+//     xy-distance from the segment is below rcut, over z-cells
+//     iz0-R .. iz0+S-1+R.  Within a column those cells are consecutive keys, so
+//     they are at most two contiguous runs of sorted particles (two when the
+//     z range wraps), which warps copy into shared memory with the periodic
+//     image shift already added - no per-pair minimum-image test;
+//   * each target culls columns by its own xy-distance and narrows each column
+//     to the z-cells within sqrt(rcut^2 - d_xy^2), so it visits ~2.5x fewer
+//     candidates than the reference's per-particle cube;
+//   * sparse segments give several lanes to one target (a power of two, up to
+//     a warp); the lanes' partial sums are combined with xor shuffles;
+//   * the epilogue writes the force in original particle order and, in the
+//     engine's step, applies the kick to the velocity (timestep.c:56-59,86-91).
+#include "common.cuh"
+
+namespace cuco {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kMaxStage = 2048;  // staged sources per chunk (32 KB)
+constexpr int kMaxR = 4;
+constexpr int kMaxCols = (2 * kMaxR + 1) * (2 * kMaxR + 1);
+constexpr int kMaxSeg = 4;
+constexpr int kMaxZ = kMaxSeg + 2 * kMaxR;  // z-cells per column
+constexpr unsigned kFull = 0xffffffffu;
+
+struct ColumnSet {
+    int ncols;
+    int R;
+    int S;
+    float margin;  // culling slack for the float cell assignment (length units)
+    signed char dx[kMaxCols];
+    signed char dy[kMaxCols];
+};
+
+struct Run {
+    uint32_t gsrc;  // first sorted index
+    uint32_t soff;  // first staged index (stencil order)
+    uint32_t cnt;
+    float sx, sy, sz;
+};
+
+template <CellFormat FMT>
+__device__ __forceinline__ void cell_range(const uint32_t *__restrict__ a,
+                                           const uint32_t *__restrict__ b, uint32_t c,
+                                           uint32_t *start, uint32_t *count) {
+    if (FMT == kCellOffsets) {
+        uint32_t s = a[c];
+        *start = s;
+        *count = a[c + 1] - s;
+    } else {
+        uint32_t s = a[c];
+        if (s == kEmptyCell) {
+            *start = 0;
+            *count = 0;
+        } else {
+            *start = s;
+            *count = b[c] - s;
+        }
+    }
+}
+
+template <CellFormat FMT, bool KICK, bool COUNT>
+__global__ void __launch_bounds__(kThreads)
+    k_shortrange(ShortRangeParams p, ColumnSet cs, const float4 *__restrict__ spos,
+                 const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
+                 const uint32_t *__restrict__ cb, const float *__restrict__ table_g,
+                 float4 *__restrict__ acc_out, KickArgs kick,
+                 unsigned long long *__restrict__ pair_counter) {
+    __shared__ float4 src[kMaxStage];
+    __shared__ float tab[kNTab];
+    __shared__ uint32_t coff[kMaxCols * (kMaxZ + 1)];
+    __shared__ Run runs[kMaxCols * 2];
+    __shared__ uint32_t coltot[kMaxCols];
+    __shared__ uint32_t s_total, s_tbegin, s_tend;
+
+    const int G = p.grid;
+    const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
+    const int segs = G / S;
+    const int seg = blockIdx.x;
+    const int ix = seg / (G * segs);
+    const int iy = (seg / segs) % G;
+    const int iz0 = (seg % segs) * S;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    // targets: the sorted particles of cells (ix, iy, iz0 .. iz0+S-1)
+    if (tid == 0) {
+        uint32_t c0 = ((uint32_t)ix * G + iy) * G + iz0;
+        uint32_t tb = 0, te = 0;
+        bool found = false;
+        for (int k = 0; k < S; ++k) {
+            uint32_t st, cn;
+            cell_range<FMT>(ca, cb, c0 + k, &st, &cn);
+            if (cn) {
+                if (!found) tb = st;
+                found = true;
+                te = st + cn;
+            }
+        }
+        s_tbegin = tb;
+        s_tend = found ? te : tb;
+    }
+    __syncthreads();
+    const uint32_t t_begin = s_tbegin, t_end = s_tend;
+    if (t_begin == t_end) return;
+
+    for (int i = tid; i < kNTab; i += kThreads) tab[i] = table_g[i];
+
+    // per column: counts of its z-cells, runs of consecutive cells with one shift
+    const float L = p.boxsize;
+    if (tid < ncols) {
+        const int col = tid;
+        int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
+        int cx = cxu < 0 ? cxu + G : (cxu >= G ? cxu - G : cxu);
+        int cy = cyu < 0 ? cyu + G : (cyu >= G ? cyu - G : cyu);
+        float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
+        float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
+        uint32_t acc = 0;
+        int nrun = 0;
+        int prev_wrap = -2;
+        for (int zc = 0; zc < nz; ++zc) {
+            int czu = iz0 - R + zc;
+            int wrap = czu < 0 ? -1 : (czu >= G ? 1 : 0);
+            int cz = czu - wrap * G;
+            uint32_t st, cn;
+            cell_range<FMT>(ca, cb, ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
+            coff[col * (kMaxZ + 1) + zc] = acc;  // relative, made absolute below
+            if (wrap != prev_wrap) {
+                Run &r = runs[col * 2 + (nrun < 2 ? nrun : 1)];
+                r.gsrc = 0xffffffffu;
+                r.soff = acc;
+                r.cnt = 0;
+                r.sx = sx;
+                r.sy = sy;
+                r.sz = wrap * L;
+                nrun++;
+                prev_wrap = wrap;
+            }
+            if (cn) {
+                Run &r = runs[col * 2 + (nrun - 1 < 1 ? nrun - 1 : 1)];
+                if (r.gsrc == 0xffffffffu) r.gsrc = st;
+                r.cnt += cn;
+            }
+            acc += cn;
+        }
+        coff[col * (kMaxZ + 1) + nz] = acc;
+        if (nrun < 2) runs[col * 2 + 1].cnt = 0;
+        coltot[col] = acc;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t run = 0;
+        for (int col = 0; col < ncols; ++col) {
+            uint32_t t = coltot[col];
+            coltot[col] = run;
+            run += t;
+        }
+        s_total = run;
+    }
+    __syncthreads();
+    for (int e = tid; e < ncols * (nz + 1); e += kThreads) {
+        int col = e / (nz + 1), zc = e % (nz + 1);
+        coff[col * (kMaxZ + 1) + zc] += coltot[col];
+    }
+    if (tid < ncols) {
+        runs[tid * 2].soff += coltot[tid];
+        runs[tid * 2 + 1].soff += coltot[tid];
+    }
+    __syncthreads();
+    const uint32_t total = s_total;
+    const bool single_chunk = total <= (uint32_t)kMaxStage;
+
+    // lanes per target
+    const uint32_t nt = t_end - t_begin;
+    int tpt = 1;
+    while (tpt < 32 && (uint32_t)(tpt * 2) * nt <= (uint32_t)kThreads) tpt *= 2;
+    const int tpc = kThreads / tpt;
+    const int sub = tid & (tpt - 1);
+
+    const float w = p.cellw;
+    const float rc2m = (p.rcut + cs.margin) * (p.rcut + cs.margin);
+    const float zbase = (float)(iz0 - R);
+    const float winv = 1.0f / w;
+    bool staged = false;
+    uint32_t npairs = 0;
+
+    for (uint32_t tb = 0; tb < nt; tb += tpc) {
+        const uint32_t t = tb + tid / tpt;
+        const bool active = t < nt;
+        float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
+            const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
+            if (!(single_chunk && staged)) {
+                __syncthreads();
+                // stage [c0, c1): warp per run
+                for (int rr = warp; rr < ncols * 2; rr += kThreads / 32) {
+                    const Run r = runs[rr];
+                    if (r.cnt == 0) continue;
+                    uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
+                    for (uint32_t s = lo + lane; s < hi; s += 32) {
+                        float4 q = spos[r.gsrc + (s - r.soff)];
+                        src[s - c0] = make_float4(q.x + r.sx, q.y + r.sy, q.z + r.sz, 0.f);
+                    }
+                }
+                __syncthreads();
+                staged = true;
+            }
+            if (active) {
+                for (int col = 0; col < ncols; ++col) {
+                    float x0 = (ix + cs.dx[col]) * w, y0 = (iy + cs.dy[col]) * w;
+                    float ddx = fmaxf(fmaxf(x0 - pt.x, pt.x - (x0 + w)), 0.f);
+                    float ddy = fmaxf(fmaxf(y0 - pt.y, pt.y - (y0 + w)), 0.f);
+                    float d2 = ddx * ddx + ddy * ddy;
+                    if (d2 > rc2m) continue;
+                    float hz = sqrtf(rc2m - d2);
+                    int zlo = (int)floorf((pt.z - hz) * winv - zbase);
+                    int zhi = (int)floorf((pt.z + hz) * winv - zbase);
+                    zlo = max(zlo, 0);
+                    zhi = min(zhi, nz - 1);
+                    if (zlo > zhi) continue;
+                    uint32_t b = coff[col * (kMaxZ + 1) + zlo];
+                    uint32_t e = coff[col * (kMaxZ + 1) + zhi + 1];
+                    b = max(b, c0);
+                    e = min(e, c1);
+                    for (uint32_t j = b + sub; j < e; j += tpt) {
+                        float4 s = src[j - c0];
+                        float dx = s.x - pt.x, dy = s.y - pt.y, dz = s.z - pt.z;
+                        float r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 > p.rcut2 || r2 == 0.f) continue;
+                        if (COUNT) ++npairs;
+                        float rinv = rsqrtf(r2);
+                        float r = r2 * rinv;
+                        float fac;
+                        if (r >= p.h) {
+                            fac = rinv * rinv * rinv;
+                        } else {
+                            float u = r * p.hinv;
+                            if (u < 0.5f)
+                                fac = p.h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
+                            else
+                                fac = p.h3inv * (21.33333f - 48.0f * u + 38.4f * u * u -
+                                                 10.66667f * u * u * u - 0.06667f / (u * u * u));
+                        }
+                        int ti = (int)(p.asmthfac * r);
+                        if (ti < kNTab) {
+                            fac *= tab[ti];
+                            ax += dx * fac;
+                            ay += dy * fac;
+                            az += dz * fac;
+                        }
+                    }
+                }
+            }
+        }
+        if (COUNT) {
+            // one atomic per warp
+            uint32_t wsum = npairs;
+            for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
+            if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
+            npairs = 0;
+        }
+        for (int off = tpt >> 1; off > 0; off >>= 1) {
+            ax += __shfl_xor_sync(kFull, ax, off);
+            ay += __shfl_xor_sync(kFull, ay, off);
+            az += __shfl_xor_sync(kFull, az, off);
+        }
+        if (active && sub == 0) {
+            const uint32_t i = t_begin + t;
+            const uint32_t o = perm[i];
+            const float mg = p.mass * p.G;
+            float4 a = make_float4(ax * mg, ay * mg, az * mg, 0.f);
+            acc_out[o] = a;
+            if (KICK) {
+                float4 v = kick.vel[o];
+                // dv = (float)(acc * dt); vel += dv  (timestep.c:57-58)
+                v.x += (float)((double)a.x * kick.kick_pp);
+                v.y += (float)((double)a.y * kick.kick_pp);
+                v.z += (float)((double)a.z * kick.kick_pp);
+                if (kick.acc_pm_s) {
+                    float4 g = kick.acc_pm_s[i];
+                    // vel += GravPM * dt (timestep.c:88)
+                    v.x = (float)((double)v.x + (double)g.x * kick.kick_pm);
+                    v.y = (float)((double)v.y + (double)g.y * kick.kick_pm);
+                    v.z = (float)((double)v.z + (double)g.z * kick.kick_pm);
+                    if (kick.acc_pm_out) kick.acc_pm_out[o] = g;
+                }
+                kick.vel[o] = v;
+            }
+        }
+    }
+}
+
+// Neighbour columns (dx, dy) whose xy cell distance is within rcut (+margin).
+bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
+    const double w = (double)p.boxsize / p.grid;
+    const double margin = 1e-5 * (double)p.boxsize + 1e-4 * w;
+    const double rc = (double)p.rcut + margin;
+    int R = (int)ceil(rc / w);
+    if (R > kMaxR) return false;
+    if (2.0 * p.rcut >= p.boxsize) return false;
+    int S = kMaxSeg;
+    while (S > 1 && p.grid % S) S >>= 1;
+    if (p.grid < S + 2 * R) return false;
+    cs->R = R;
+    cs->S = S;
+    cs->margin = (float)margin;
+    int n = 0;
+    for (int dx = -R; dx <= R; ++dx)
+        for (int dy = -R; dy <= R; ++dy) {
+            double ex = fmax(abs(dx) - 1, 0) * w, ey = fmax(abs(dy) - 1, 0) * w;
+            if (ex * ex + ey * ey > rc * rc) continue;
+            cs->dx[n] = (signed char)dx;
+            cs->dy[n] = (signed char)dy;
+            n++;
+        }
+    cs->ncols = n;
+    return true;
+}
+
+}  // namespace
+
+template <CellFormat FMT, bool KICK>
+void launch_fmt_kick(unsigned blocks, cudaStream_t stream, const ShortRangeParams &p,
+                     const ColumnSet &cs, const float4 *sorted_pos, const uint32_t *perm,
+                     const uint32_t *cell_a, const uint32_t *cell_b, const float *table,
+                     float4 *acc_out, const KickArgs &kick, unsigned long long *counter) {
+    if (counter)
+        k_shortrange<FMT, KICK, true><<<blocks, kThreads, 0, stream>>>(
+            p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
+    else
+        k_shortrange<FMT, KICK, false><<<blocks, kThreads, 0, stream>>>(
+            p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
+}
+
+cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,
+                                const uint32_t *perm, const uint32_t *cell_a,
+                                const uint32_t *cell_b, CellFormat fmt, const float *table,
+                                float4 *acc_out, const KickArgs &kick, cudaStream_t stream,
+                                unsigned long long *pair_counter) {
+    ColumnSet cs;
+    if (!build_columns(p, &cs)) {
+        set_error("short range: cell grid too coarse for rcut (need rcut <= 4 cells, rcut < L/2 "
+                  "and at least S+2R cells per dimension)");
+        return CUCO_ERR_UNSUPPORTED;
+    }
+    if (p.n == 0) return CUCO_OK;
+    const int G = p.grid;
+    const unsigned blocks = (unsigned)G * G * (G / cs.S);
+    const bool kick_on = kick.vel != nullptr;
+    if (fmt == kCellOffsets) {
+        if (kick_on)
+            launch_fmt_kick<kCellOffsets, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+        else
+            launch_fmt_kick<kCellOffsets, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+    } else {
+        if (kick_on)
+            launch_fmt_kick<kCellStartEnd, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+        else
+            launch_fmt_kick<kCellStartEnd, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+    }
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+}  // namespace cuco

@@ -1,0 +1,365 @@
+// Cell keys, stable LSD radix sort, and the reorder / cell-bound kernels.
+//
+// Reference: calcHashD (gravlist_kernel.cu:92-118), RadixSort::sort ->
+// radixSort (radixsort.h:170-187, radixsort.cu:1048-1145), and
+// reorderDataAndFindCellStartD (gravlist_kernel.cu:121-160).
+//
+// The sort is a three-kernel-per-pass LSD radix sort designed for sm_103a:
+//   1. k_sort_hist:   per 4096-key tile, a digit histogram (warp match_any
+//                     aggregation into shared-memory counters);
+//   2. k_sort_scan:   one CTA turns the [digit][tile] histogram into global
+//                     scatter offsets (coalesced warp scans per digit);
+//   3. k_sort_scatter: each tile ranks its keys stably with warp ballots
+//                     (the lanes sharing a digit are found from RB ballots, the
+//                     rank is a popcount below the lane), stages the tile in
+//                     digit order in shared memory and writes out digit runs
+//                     with coalesced stores.
+// Digits are 4..8 bits; a pass count of ceil(bits/8) with equal digit widths
+// is used (18-bit keys: three 6-bit passes).
+#include "common.cuh"
+
+namespace cuco {
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 keys
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int cell_coord(float t, int G) {
+    int c = (int)t;  // truncation toward zero (cvt.rzi), as calcHashD's int3 assignment
+    c = c < 0 ? 0 : c;
+    return c >= G ? G - 1 : c;
+}
+
+__global__ void k_cell_keys(const float4 *__restrict__ pos, uint32_t *__restrict__ keys,
+                            uint32_t *__restrict__ idx, uint32_t n, float gridfac, int G) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 p = pos[i];
+        int ix = cell_coord(__fmul_rn(gridfac, p.x), G);
+        int iy = cell_coord(__fmul_rn(gridfac, p.y), G);
+        int iz = cell_coord(__fmul_rn(gridfac, p.z), G);
+        keys[i] = ((uint32_t)ix * G + iy) * G + iz;
+        if (idx) idx[i] = i;
+    }
+}
+
+template <int RB>
+__global__ void __launch_bounds__(kSortThreads)
+    k_sort_hist(const uint32_t *__restrict__ keys, uint32_t n, int shift,
+                uint32_t *__restrict__ hist, uint32_t tiles) {
+    constexpr int RADIX = 1 << RB;
+    __shared__ uint32_t h[RADIX];
+    for (int d = threadIdx.x; d < RADIX; d += kSortThreads) h[d] = 0;
+    __syncthreads();
+    const uint32_t tile = blockIdx.x;
+    const uint32_t base = tile * kSortTile;
+    const int lane = threadIdx.x & 31;
+#pragma unroll 4
+    for (int k = 0; k < kSortItems; ++k) {
+        uint32_t i = base + k * kSortThreads + threadIdx.x;
+        bool valid = i < n;
+        uint32_t d = valid ? (keys[i] >> shift) & (RADIX - 1) : (uint32_t)RADIX;
+        uint32_t peers = __match_any_sync(kFull, d);
+        if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RADIX; d += kSortThreads) hist[d * tiles + tile] = h[d];
+}
+
+// hist[d*tiles + t] (count of digit d in tile t) -> global offset of that run.
+template <int RB>
+__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist, uint32_t tiles) {
+    constexpr int RADIX = 1 << RB;
+    __shared__ uint32_t total[RADIX];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int d = warp; d < RADIX; d += 32) {
+        uint32_t carry = 0;
+        for (uint32_t t0 = 0; t0 < tiles; t0 += 32) {
+            uint32_t t = t0 + lane;
+            uint32_t v = t < tiles ? hist[d * tiles + t] : 0;
+            uint32_t incl = v;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                uint32_t y = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl += y;
+            }
+            if (t < tiles) hist[d * tiles + t] = carry + incl - v;
+            carry += __shfl_sync(kFull, incl, 31);
+        }
+        if (lane == 0) total[d] = carry;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int PER = (RADIX + 31) / 32;
+        uint32_t v[PER], s = 0;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            int d = lane * PER + j;
+            v[j] = d < RADIX ? total[d] : 0;
+            s += v[j];
+        }
+        uint32_t incl = s;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += y;
+        }
+        uint32_t run = incl - s;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            int d = lane * PER + j;
+            if (d < RADIX) {
+                total[d] = run;
+                run += v[j];
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t entries = (uint32_t)RADIX * tiles;
+    for (uint32_t e = threadIdx.x; e < entries; e += blockDim.x) hist[e] += total[e / tiles];
+}
+
+template <int RB, bool WITH_VALS, bool SINGLE_TILE>
+__global__ void __launch_bounds__(kSortThreads)
+    k_sort_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
+                   uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint32_t n,
+                   int shift, const uint32_t *__restrict__ hist, uint32_t tiles) {
+    constexpr int RADIX = 1 << RB;
+    __shared__ uint32_t wcnt[kSortWarps][RADIX];
+    __shared__ uint32_t dstart[RADIX];
+    __shared__ uint32_t gbase[RADIX];
+    __shared__ uint32_t skeys[kSortTile];
+    __shared__ uint32_t svals[WITH_VALS ? kSortTile : 1];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tile = blockIdx.x;
+    const uint32_t base = tile * kSortTile;
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int e = threadIdx.x; e < kSortWarps * RADIX; e += kSortThreads) (&wcnt[0][0])[e] = 0;
+    __syncthreads();
+
+    uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+    // Warp w owns tile elements [w*512, w*512+512); item k covers 32 of them in
+    // lane order, so (k, lane) order is input order and the ranks are stable.
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        uint32_t i = base + warp * (32 * kSortItems) + k * 32 + lane;
+        bool valid = i < n;
+        key[k] = valid ? kin[i] : 0xffffffffu;
+        if (WITH_VALS) val[k] = valid ? (vin ? vin[i] : i) : 0u;
+        uint32_t d = (key[k] >> shift) & (RADIX - 1);
+        uint32_t peers = __ballot_sync(kFull, valid);
+#pragma unroll
+        for (int b = 0; b < RB; ++b) {
+            uint32_t bit = (d >> b) & 1u;
+            uint32_t m = __ballot_sync(kFull, bit);
+            peers &= bit ? m : ~m;
+        }
+        uint32_t cnt = wcnt[warp][d];
+        rank[k] = cnt + __popc(peers & lt);
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = cnt + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RADIX; d += kSortThreads) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < kSortWarps; ++w) {
+            uint32_t c = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += c;
+        }
+        dstart[d] = run;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int PER = (RADIX + 31) / 32;
+        uint32_t v[PER], s = 0;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            int d = lane * PER + j;
+            v[j] = d < RADIX ? dstart[d] : 0;
+            s += v[j];
+        }
+        uint32_t incl = s;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            uint32_t y = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += y;
+        }
+        uint32_t run = incl - s;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            int d = lane * PER + j;
+            if (d < RADIX) {
+                dstart[d] = run;
+                run += v[j];
+            }
+        }
+    }
+    __syncthreads();
+    for (int d = threadIdx.x; d < RADIX; d += kSortThreads)
+        gbase[d] = SINGLE_TILE ? dstart[d] : hist[d * tiles + tile];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kSortItems; ++k) {
+        uint32_t i = base + warp * (32 * kSortItems) + k * 32 + lane;
+        if (i < n) {
+            uint32_t d = (key[k] >> shift) & (RADIX - 1);
+            uint32_t lp = dstart[d] + wcnt[warp][d] + rank[k];
+            skeys[lp] = key[k];
+            if (WITH_VALS) svals[lp] = val[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t tile_n = min((uint32_t)kSortTile, n - base);
+    for (uint32_t j = threadIdx.x; j < tile_n; j += kSortThreads) {
+        uint32_t kk = skeys[j];
+        uint32_t d = (kk >> shift) & (RADIX - 1);
+        uint32_t o = gbase[d] + j - dstart[d];
+        kout[o] = kk;
+        if (WITH_VALS) vout[o] = svals[j];
+    }
+}
+
+template <int RB>
+cuco_status_t sort_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *kout, uint32_t *vout,
+                        bool with_vals, uint32_t *hist, uint32_t n, int shift,
+                        cudaStream_t stream, int *launches) {
+    const uint32_t tiles = (n + kSortTile - 1) / kSortTile;
+    if (tiles == 1) {
+        if (with_vals)
+            k_sort_scatter<RB, true, true><<<1, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n,
+                                                                          shift, hist, tiles);
+        else
+            k_sort_scatter<RB, false, true><<<1, kSortThreads, 0, stream>>>(kin, vin, kout, vout,
+                                                                           n, shift, hist, tiles);
+        *launches += 1;
+    } else {
+        k_sort_hist<RB><<<tiles, kSortThreads, 0, stream>>>(kin, n, shift, hist, tiles);
+        k_sort_scan<RB><<<1, 1024, 0, stream>>>(hist, tiles);
+        if (with_vals)
+            k_sort_scatter<RB, true, false><<<tiles, kSortThreads, 0, stream>>>(
+                kin, vin, kout, vout, n, shift, hist, tiles);
+        else
+            k_sort_scatter<RB, false, false><<<tiles, kSortThreads, 0, stream>>>(
+                kin, vin, kout, vout, n, shift, hist, tiles);
+        *launches += 3;
+    }
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+void split_bits(int key_bits, int max_radix_bits, int *passes, int *rb) {
+    if (key_bits < 1) key_bits = 1;
+    if (max_radix_bits > 8) max_radix_bits = 8;
+    if (max_radix_bits < 4) max_radix_bits = 4;
+    *passes = (key_bits + max_radix_bits - 1) / max_radix_bits;
+    *rb = (key_bits + *passes - 1) / *passes;
+    if (*rb < 4) *rb = 4;
+}
+
+__global__ void k_reorder_start_end(uint32_t *__restrict__ cell_start, uint32_t *__restrict__ cell_end,
+                                    float4 *__restrict__ sorted_pos,
+                                    const uint32_t *__restrict__ skeys,
+                                    const uint32_t *__restrict__ perm,
+                                    const float4 *__restrict__ pos, uint32_t n) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t k = skeys[i];
+    if (i == 0 || k != skeys[i - 1]) {
+        cell_start[k] = i;
+        if (i > 0) cell_end[skeys[i - 1]] = i;
+    }
+    if (i == n - 1) cell_end[k] = i + 1;
+    sorted_pos[i] = pos[perm[i]];
+}
+
+__global__ void k_reorder_offsets(uint32_t *__restrict__ cell_off, float4 *__restrict__ sorted_pos,
+                                  const uint32_t *__restrict__ skeys,
+                                  const uint32_t *__restrict__ perm,
+                                  const float4 *__restrict__ pos, uint32_t n, uint32_t ncells) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    // cells (prev, cur] start at i; thread n closes the tail up to ncells
+    uint32_t prev = i == 0 ? 0u : skeys[i - 1] + 1u;
+    uint32_t cur = i == n ? ncells : skeys[i];
+    for (uint32_t c = prev; c <= cur; ++c) cell_off[c] = i;
+    if (i < n) sorted_pos[i] = pos[perm[i]];
+}
+
+}  // namespace
+
+size_t sort_hist_entries(uint32_t n, int key_bits, int max_radix_bits) {
+    int passes, rb;
+    split_bits(key_bits, max_radix_bits, &passes, &rb);
+    size_t tiles = (n + kSortTile - 1) / kSortTile;
+    return (size_t)(1u << rb) * (tiles ? tiles : 1);
+}
+
+cuco_status_t sort_pairs(uint32_t *keys, uint32_t *vals, const uint32_t *vals_in,
+                         uint32_t *keys_alt, uint32_t *vals_alt, uint32_t *hist, uint32_t n,
+                         int key_bits, int max_radix_bits, cudaStream_t stream,
+                         bool *result_in_alt, int *launches) {
+    int passes, rb;
+    split_bits(key_bits, max_radix_bits, &passes, &rb);
+    bool with_vals = vals != nullptr;
+    *result_in_alt = false;
+    if (n == 0) return CUCO_OK;
+    uint32_t *kbuf[2] = {keys, keys_alt};
+    uint32_t *vbuf[2] = {vals, vals_alt};
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        const uint32_t *vin = (p == 0) ? vals_in : vbuf[cur];
+        int shift = p * rb;
+        cuco_status_t s;
+        switch (rb) {
+            case 4: s = sort_pass<4>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
+            case 5: s = sort_pass<5>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
+            case 6: s = sort_pass<6>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
+            case 7: s = sort_pass<7>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
+            default: s = sort_pass<8>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
+        }
+        if (s != CUCO_OK) return s;
+        cur ^= 1;
+    }
+    *result_in_alt = cur == 1;
+    return CUCO_OK;
+}
+
+cuco_status_t launch_cell_keys(const float4 *pos, uint32_t *keys, uint32_t *idx, uint32_t n,
+                               float gridfac, int G, cudaStream_t stream) {
+    if (n == 0) return CUCO_OK;
+    int blocks = (int)((n + 255) / 256);
+    k_cell_keys<<<blocks, 256, 0, stream>>>(pos, keys, idx, n, gridfac, G);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t launch_reorder_start_end(uint32_t *cell_start, uint32_t *cell_end,
+                                       float4 *sorted_pos, const uint32_t *sorted_keys,
+                                       const uint32_t *perm, const float4 *pos, uint32_t n,
+                                       uint32_t ncells, cudaStream_t stream) {
+    CUCO_TRY_CUDA(cudaMemsetAsync(cell_start, 0xff, sizeof(uint32_t) * ncells, stream));
+    if (n == 0) return CUCO_OK;
+    k_reorder_start_end<<<(n + 255) / 256, 256, 0, stream>>>(cell_start, cell_end, sorted_pos,
+                                                           sorted_keys, perm, pos, n);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t launch_reorder_offsets(uint32_t *cell_off, float4 *sorted_pos,
+                                     const uint32_t *sorted_keys, const uint32_t *perm,
+                                     const float4 *pos, uint32_t n, uint32_t ncells,
+                                     cudaStream_t stream) {
+    k_reorder_offsets<<<(n + 1 + 255) / 256, 256, 0, stream>>>(cell_off, sorted_pos, sorted_keys,
+                                                             perm, pos, n, ncells);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+}  // namespace cuco

@@ -1,0 +1,266 @@
+/* cuco_gb300.h - C ABI of libcuco_gb300.so, the GB300 (sm_103a) force engine.
+ *
+ * Two groups of entry points:
+ *
+ * 1. The reference's own names and signatures (liulei/cuco), so that its host
+ *    program links against this library in place of gravlist.cu, radixsort.cu,
+ *    gravlist.cpp, pm_periodic.c, longrange.c, accel.c, predict.c, timestep.c
+ *    and driftfac.c.  Each declaration cites the reference function it
+ *    replaces.  The GPU-side helpers take plain device pointers and sizes; the
+ *    host-side force/integrator functions work on the reference's globals
+ *    (P, NumPart, All, header, DriftTable, GravKickTable), which the host
+ *    program defines (allvars.c) - the library carries weak fallbacks of them.
+ *    As in the reference these functions return void and abort on a CUDA error
+ *    (cutilSafeCall semantics); the message is printed first.
+ *
+ * 2. The engine API (cuco_*): one resident simulation box per handle, status
+ *    returns, explicit configuration, host or device buffers.  The drop-in
+ *    functions are built on it.
+ *
+ * Device state stays resident between calls; nothing is copied between host
+ * and device except where a function says so. */
+#ifndef CUCO_GB300_H
+#define CUCO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#include "cuco_allvars.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef unsigned int uint;
+typedef size_t CUDPPHandle; /* accepted and ignored: the sort needs no CUDPP plan */
+
+/* ------------------------------------------------------------------------
+ * 1a. GPU-side helpers of gravlist.cu and radixsort.cu (reference names)
+ * ---------------------------------------------------------------------- */
+
+/* gravlist.cu:25-31.  Selects device 0 (CUCO_DEVICE overrides). */
+void cudaInit(void);
+/* gravlist.cu:33-37 */
+void allocateArray(void **devPtr, size_t size);
+/* gravlist.cu:39-43 */
+void freeArray(void *devPtr);
+/* gravlist.cu:45-49 */
+void copyArrayFromDevice(void *host, void *device, int size);
+/* gravlist.cu:51-54 */
+void copyArrayToDevice(void *device, void *host, int offset, int size);
+/* gravlist.cu:173-177: table, box, cut and mass constants for the kernels below */
+void setSimParam(SIMPARAM *pHostSimParam);
+/* gravlist.cu:179-181: spline softening constants */
+void setSoftParam(SOFTPARAM *pHostSoftParam);
+/* gravlist.cu:56-68: P[i].Pos -> dOldPos (float4) */
+void copyPosToDevice(void);
+/* gravlist.cu:70-83: dGravAccel (float4) -> P[i].GravAccel */
+void copyAccelFromDevice(void);
+
+/* gravlist.cu:85-104 + gravlist_kernel.cu:92-118.  Cell key of each particle on
+ * a G^3 grid, G = cbrt of the cell count last set by setSimParam's
+ * to_grid_fac and cuco_dropin_configure (64 by default):
+ * key = (ix*G+iy)*G+iz, i = (int)(to_grid_fac*p) in float32; index = i.
+ * Unlike the reference every particle is keyed for any numParticles, and a
+ * coordinate whose product rounds to G is clamped to cell G-1. */
+void calcHash(uint *gridParticleHash, uint *gridParticleIndex, float *pos, uint numParticles);
+
+/* gravlist.cu:108-142 + gravlist_kernel.cu:121-160.  cellStart[c] = first
+ * sorted index of cell c (0xffffffff when empty), cellEnd[c] = one past the
+ * last; sortedPos[i] = oldPos[gridParticleIndex[i]] (float4). */
+void reorderDataAndFindCellStart(uint *cellStart, uint *cellEnd, float *sortedPos,
+                                 uint *gridParticleHash, uint *gridParticleIndex,
+                                 float *oldPos, uint numParticles, uint numCells);
+
+/* gravlist.cu:144-171 + gravlist_kernel.cu:20-88,162-234.  Short-range P3M
+ * force on every sorted particle from all particles within rcut, with the
+ * constants of setSimParam/setSoftParam; gravAccel[gridParticleIndex[i]] =
+ * (ax, ay, az, 0).  numCells = G^3 of the grid the keys were made on. */
+void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridParticleIndex,
+                                 uint *cellStart, uint *cellEnd, uint numParticles,
+                                 uint numCells);
+
+/* radixsort.h:47-58 / radixsort.cu:1048-1145.  Stable LSD sort of
+ * (keys, values) by the low keyBits bits, in place.  tempKeys/tempValues hold
+ * numElements entries each; `counters` holds at least 32*ceil(n/1024) entries
+ * (the reference RadixSort's allocation, radixsort.h:271-275) and is used as
+ * the per-tile digit histogram; countersSum, blockOffsets and scanPlan are not
+ * used.  flipBits must be false. */
+void radixSort(uint *keys, uint *values, uint *tempKeys, uint *tempValues, uint *counters,
+               uint *countersSum, uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
+               uint keyBits, bool flipBits);
+/* radixsort.h:73-81: key-only variant of radixSort. */
+void radixSortKeysOnly(uint *keys, uint *tempKeys, uint *counters, uint *countersSum,
+                       uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
+                       uint keyBits, bool flipBits);
+/* radixsort.h:47: no device-specific tuning is needed on sm_103a; kept for linkage. */
+void initDeviceParameters(void);
+/* radixsort.h:46: aborts with `msg` if a CUDA error is pending. */
+void checkCudaError(const char *msg);
+
+/* ------------------------------------------------------------------------
+ * 1b. Host force / integrator functions over the reference's globals
+ * ---------------------------------------------------------------------- */
+
+/* Mesh size PMGRID (allvars.h:9) and short-range cell grid of the drop-in.
+ * The reference fixes both at compile time (G = PMGRID); call before
+ * pm_init_periodic().  Defaults: pmgrid 64, cellgrid = pmgrid. */
+void cuco_dropin_configure(int pmgrid, int cellgrid);
+
+/* longrange.c:8-12 */
+void long_range_init(void);
+/* longrange.c:14-22: zero GravPM, then pmforce_periodic() */
+void long_range_force(void);
+/* pm_periodic.c:25-43: All.Asmth, All.Rcut; mesh buffers */
+void pm_init_periodic(void);
+/* pm_periodic.c:45-65 (mesh buffers live on the device and are kept) */
+void pm_init_periodic_allocate(void);
+void pm_init_periodic_free(void);
+/* pm_periodic.c:67-314: P[i].GravPM for every particle, on the device */
+void pmforce_periodic(void);
+/* gravlist.cpp:28-45 */
+void set_softenings(void);
+/* gravlist.cpp:48-115: split table, device arrays, SIMPARAM */
+void linklist_init(void);
+/* gravlist.cpp:148-193: P[i].GravAccel for every particle, on the device */
+void gravity_linklist_cuda(void);
+/* accel.c:8-23 */
+void compute_accelerations(void);
+/* predict.c:10-22 */
+void move_particles(int time0, int time1);
+/* predict.c:24-41 */
+void do_box_wrapping(void);
+/* timestep.c:11-94 */
+void advance_and_find_timesteps(void);
+/* timestep.c:96-138 */
+int get_timestep(int p);
+/* driftfac.c:14-42 (tables integrated in FP64; the float tables DriftTable /
+ * GravKickTable are filled too) */
+void init_drift_table(void);
+/* driftfac.c:44-64 */
+double drift_integ(double a, void *param);
+double gravkick_integ(double a, void *param);
+/* driftfac.c:66-126 */
+double get_drift_factor(int time0, int time1);
+double get_gravkick_factor(int time0, int time1);
+
+/* ------------------------------------------------------------------------
+ * 2. Engine API
+ * ---------------------------------------------------------------------- */
+
+typedef enum {
+    CUCO_OK = 0,
+    CUCO_ERR_INVALID = 1,     /* bad argument or configuration */
+    CUCO_ERR_NOMEM = 2,       /* device allocation failed */
+    CUCO_ERR_CUDA = 3,        /* a CUDA call failed; see cuco_last_error() */
+    CUCO_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+    CUCO_ERR_STATE = 5,       /* call out of order (e.g. no state uploaded) */
+    CUCO_ERR_UNSUPPORTED = 6  /* configuration this build does not handle */
+} cuco_status_t;
+
+typedef enum {
+    CUCO_MODE_PLAIN = 0, /* float32 positions, the reference's arithmetic */
+    CUCO_MODE_FIXED = 1  /* uint32 fixed-point positions, compensated sums */
+} cuco_mode_t;
+
+typedef struct {
+    int64_t n;        /* particles */
+    int pm_grid;      /* PM mesh size M (power of two, 16..1024) */
+    int cell_grid;    /* short-range cell grid G (cell width >= rcut/2) */
+    float boxsize;    /* L, internal length units */
+    float mass;       /* particle mass */
+    double G;         /* gravitational constant, internal units */
+    float asmth;      /* split scale r_s (All.Asmth), length units */
+    float rcut;       /* short-range cutoff (All.Rcut), length units */
+    float softening;  /* spline softening length h = 2.8 eps (All.ForceSoftening) */
+    int mode;         /* cuco_mode_t */
+    int device;       /* CUDA device ordinal */
+} cuco_config_t;
+
+typedef struct cuco_box cuco_box_t;
+
+/* Fill `cfg` with the reference's derived constants for a box:
+ * asmth = ASMTH*L/M and rcut = RCUT*asmth rounded to float as pm_periodic.c:27-28
+ * stores them; cell_grid = M (the reference's grid) unless already set. */
+cuco_status_t cuco_config_reference(cuco_config_t *cfg);
+
+cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **box);
+cuco_status_t cuco_box_destroy(cuco_box_t *box);
+
+/* State in original particle order, n x 3 floats each.  `on_device` selects
+ * whether the pointers are device (1) or host (0) memory.  vel is the
+ * integrator's variable a^2 dx/dt (the reference's P[].Vel after init.c:30). */
+cuco_status_t cuco_box_set_state(cuco_box_t *box, const float *pos, const float *vel,
+                                 int on_device);
+cuco_status_t cuco_box_get_state(cuco_box_t *box, float *pos, float *vel, float *acc_pp,
+                                 float *acc_pm, int on_device);
+/* Spline softening length h (changes with time when softening is physical). */
+cuco_status_t cuco_box_set_softening(cuco_box_t *box, float h);
+
+/* Forces at the current positions: keys, sort, reorder, then the PM force
+ * (when pm != 0) and the short-range force (when pp != 0). */
+cuco_status_t cuco_box_forces(cuco_box_t *box, int pm, int pp);
+
+/* One step of the leapfrog in the reference's kick-drift-kick form (run.c:11-20
+ * with timestep.c:26-93 for a global step): positions drift by `drift` and wrap,
+ * forces are recomputed, velocities kick by acc_pp*kick_pp + acc_pm*kick_pm.
+ * The factors are cosmological integrals (cuco_cosmo_factors). */
+cuco_status_t cuco_box_step(cuco_box_t *box, double drift, double kick_pp, double kick_pm);
+
+/* Run `nsteps` steps with per-step factors (arrays of nsteps), recorded once as
+ * a CUDA graph and replayed. */
+cuco_status_t cuco_box_run(cuco_box_t *box, int nsteps, const double *drift,
+                           const double *kick_pp, const double *kick_pm);
+
+cuco_status_t cuco_box_sync(cuco_box_t *box);
+/* The box's CUDA stream (cudaStream_t). */
+cuco_status_t cuco_box_stream(cuco_box_t *box, void **stream);
+
+/* Device time (ms) of each phase of the last cuco_box_forces/cuco_box_step:
+ * [0] drift+keys, [1] sort, [2] reorder, [3] PM deposit, [4] PM FFT+Green,
+ * [5] PM gradient+interpolation, [6] short range (+kick), [7] total.
+ * Only filled when phase timing is enabled. */
+cuco_status_t cuco_box_enable_timing(cuco_box_t *box, int enable);
+cuco_status_t cuco_box_timings(cuco_box_t *box, float *ms /* 8 */);
+
+/* Copies of internal arrays for inspection (device -> host): keys and the
+ * sort permutation in sorted order, cell bounds.  Any pointer may be NULL. */
+cuco_status_t cuco_box_debug(cuco_box_t *box, uint32_t *sorted_keys, uint32_t *perm,
+                             uint32_t *cell_start, uint32_t *cell_end);
+
+/* Number of kernel launches one cuco_box_step issues. */
+int cuco_box_launches_per_step(cuco_box_t *box);
+
+/* In-range pair count (r^2 <= rcut^2, self excluded) of the short-range
+ * launches since the last reset; counted only while phase timing is enabled. */
+cuco_status_t cuco_box_pair_count(cuco_box_t *box, uint64_t *pairs, int reset);
+
+/* Device-time bracket on the box's stream: op 0 records the start event,
+ * op 1 records the stop event, waits for it and returns the elapsed ms. */
+cuco_status_t cuco_box_timer(cuco_box_t *box, int op, float *ms);
+
+/* Page-locked host memory for transfers (cudaHostAlloc / cudaFreeHost). */
+cuco_status_t cuco_pinned_alloc(size_t bytes, void **ptr);
+cuco_status_t cuco_pinned_free(void *ptr);
+
+/* Measured FP32 FMA throughput of `device` in TFLOP/s (2 flops per FMA): a
+ * register-resident FMA chain on every SM, timed with CUDA events. */
+cuco_status_t cuco_fp32_peak(int device, double *tflops);
+
+/* Drift and kick factors between scale factors a0 < a1 in FP64:
+ * drift = int da/(H a^3), kick = int da/(H a^2), H = hubble*sqrt(Om/a^3 +
+ * (1-Om-OL)/a^2 + OL) (driftfac.c:44-64). */
+cuco_status_t cuco_cosmo_factors(double a0, double a1, double omega0, double omega_lambda,
+                                 double hubble, double *drift, double *kick);
+
+/* Message of the last failed call on this thread. */
+const char *cuco_last_error(void);
+const char *cuco_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -32,7 +32,9 @@ _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
 def build_port() -> str:
-    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    r = subprocess.run(["make", "-s", "-C", HERE, "port"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle port build failed:\n" + r.stdout + r.stderr)
     return PORT_LIB
 
 
@@ -44,8 +46,10 @@ def build_reference(pmgrids=(32, 64, 128, 256)) -> list[str]:
     """Compile the reference's CPU path (one library per PM mesh size)."""
     if not reference_available():
         raise FileNotFoundError("reference sources not present at " + REFERENCE_SOURCES)
-    subprocess.run(["make", "-s", "-j4", "-C", HERE, "ref", "REF=" + REFERENCE_SOURCES,
-                    "PMGRIDS=" + " ".join(str(m) for m in pmgrids)], check=True)
+    r = subprocess.run(["make", "-s", "-j4", "-C", HERE, "ref", "REF=" + REFERENCE_SOURCES,
+                        "PMGRIDS=" + " ".join(str(m) for m in pmgrids)], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("reference oracle build failed:\n" + r.stdout + r.stderr)
     return [os.path.join(REF_DIR, f"libcucoref_pm{m}.so") for m in pmgrids]
 
 
@@ -79,6 +83,10 @@ class Port:
         lib.op_shortrange_table.argtypes = [_f32p]
         lib.op_pp.argtypes = [_f32p, ctypes.c_int64, ctypes.POINTER(OpParams), ctypes.c_int,
                               ctypes.c_int, _f32p]
+        lib.op_pp_targets.argtypes = [_f32p, ctypes.c_int64,
+                                      np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS"),
+                                      ctypes.c_int64, ctypes.POINTER(OpParams), ctypes.c_int,
+                                      ctypes.c_int, _f32p]
         lib.op_pair_count.argtypes = [_f32p, ctypes.c_int64, ctypes.POINTER(OpParams), ctypes.c_int,
                                       ctypes.c_int]
         lib.op_pair_count.restype = ctypes.c_int64
@@ -124,6 +132,14 @@ class Port:
         acc = np.empty_like(pos)
         self.lib.op_pp(pos.reshape(-1), pos.shape[0], ctypes.byref(params), G, nthreads, acc.reshape(-1))
         return acc
+
+    def pp_targets(self, pos, targets, params: OpParams, G: int, nthreads: int = 1):
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        tg = np.ascontiguousarray(targets, dtype=np.int64)
+        acc = np.zeros_like(pos)
+        self.lib.op_pp_targets(pos.reshape(-1), pos.shape[0], tg, tg.size, ctypes.byref(params), G,
+                               nthreads, acc.reshape(-1))
+        return acc[tg]
 
     def pair_count(self, pos, params: OpParams, G: int, nthreads: int = 1) -> int:
         pos = np.ascontiguousarray(pos, dtype=np.float32)

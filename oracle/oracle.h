@@ -50,6 +50,10 @@ void op_shortrange_table(float *table /* 1000 */);
  * G = PMGRID, gravlist.cpp:117-146).  FP64 accumulation; acc is n x 3. */
 void op_pp(const float *pos, int64_t n, const op_params *p, int G, int nthreads, float *acc);
 
+/* op_pp for the listed targets only (acc is n x 3; other rows untouched). */
+void op_pp_targets(const float *pos, int64_t n, const int64_t *targets, int64_t nt,
+                   const op_params *p, int G, int nthreads, float *acc);
+
 /* Number of ordered pairs (i != j) with float-computed r^2 <= rcut^2, as the
  * reference's pair test (gravlist_kernel.cu:46-55). */
 int64_t op_pair_count(const float *pos, int64_t n, const op_params *p, int G, int nthreads);

@@ -253,6 +253,29 @@ void op_pp(const float *pos, int64_t n, const op_params *p, int G, int nthreads,
     free(c);
 }
 
+typedef struct {
+    pp_ctx *c;
+    const int64_t *targets;
+} pp_sub_ctx;
+
+static void pp_sub_range(void *ctx, int64_t b, int64_t e, int tid) {
+    (void)tid;
+    pp_sub_ctx *s = (pp_sub_ctx *)ctx;
+    for (int64_t i = b; i < e; ++i) pp_target(s->c, s->targets[i], s->c->acc, NULL);
+}
+
+void op_pp_targets(const float *pos, int64_t n, const int64_t *targets, int64_t nt,
+                   const op_params *p, int G, int nthreads, float *acc) {
+    pp_ctx *c = (pp_ctx *)malloc(sizeof(pp_ctx));
+    pp_setup(c, pos, n, p, G);
+    c->acc = acc;
+    c->pair_counts = NULL;
+    pp_sub_ctx s = {c, targets};
+    parallel_for(nt, nthreads, pp_sub_range, &s);
+    pp_free(c);
+    free(c);
+}
+
 int64_t op_pair_count(const float *pos, int64_t n, const op_params *p, int G, int nthreads) {
     pp_ctx *c = (pp_ctx *)malloc(sizeof(pp_ctx));
     int64_t counts[256] = {0};

@@ -237,3 +237,25 @@ void cref_set_output(const char *dir, const char *base) {
 }
 
 void cref_save_snapshot(int num) { savepositions(num); }
+
+/* Layout of the reference's global structs, for the ABI checks of the drop-in
+ * headers: sizeof(ALL) and the offsets of fields the drop-in reads/writes. */
+#include <stddef.h>
+void cref_layout(long *out /* 16 */) {
+    out[0] = (long)sizeof(ALL);
+    out[1] = (long)offsetof(ALL, G);
+    out[2] = (long)offsetof(ALL, Hubble);
+    out[3] = (long)offsetof(ALL, Time);
+    out[4] = (long)offsetof(ALL, Timebase_interval);
+    out[5] = (long)offsetof(ALL, Ti_Current);
+    out[6] = (long)offsetof(ALL, PM_Ti_endstep);
+    out[7] = (long)offsetof(ALL, Asmth);
+    out[8] = (long)offsetof(ALL, ForceSoftening);
+    out[9] = (long)offsetof(ALL, OutputListTimes);
+    out[10] = (long)offsetof(ALL, InitCondFile);
+    out[11] = (long)sizeof(PARTICLE);
+    out[12] = (long)sizeof(HEADER);
+    out[13] = (long)offsetof(PARTICLE, GravPM);
+    out[14] = (long)offsetof(PARTICLE, Ti_endstep);
+    out[15] = (long)offsetof(ALL, SofteningTable);
+}
