@@ -112,6 +112,8 @@ void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridP
     p.rcut = s.sim.rcut;
     p.rcut2 = s.sim.rcut2;
     p.asmthfac = s.sim.asmthfac;
+    // gravlist.cpp:67 keeps asmthfac in double; SIMPARAM carries Asmth itself
+    p.asmthfac_d = 0.5 / (double)s.sim.asmth * (kNTab / 3.0);
     p.mass = s.sim.mass;
     p.G = s.sim.G;
     p.h = s.soft.h;

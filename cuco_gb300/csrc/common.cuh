@@ -75,6 +75,7 @@ struct ShortRangeParams {
     float cellw;     // L / G
     float rcut, rcut2;
     float asmthfac;  // 0.5 / asmth * NTAB / 3
+    double asmthfac_d;  // the same in double (gravlist.cpp:67), for bin-edge pairs
     float mass;      // source mass
     float G;         // gravitational constant (applied once per target)
     float h, hinv, h3inv;

@@ -86,7 +86,17 @@ DropinState &ds() {
     return s;
 }
 
+// Grid of calcHash and of the cellStart/cellEnd arrays: PMGRID, as the
+// reference fixes it (gravlist_kernel.cu:114), unless configured.
 int cell_grid() { return ds().cellgrid > 0 ? ds().cellgrid : ds().pmgrid; }
+
+// Grid of the drop-in's own short-range pass: PMGRID/4 (cell width 4 mesh
+// cells, rcut = 1.4 cells), unless configured.  The forces do not depend on it.
+int engine_grid() {
+    if (ds().cellgrid > 0) return ds().cellgrid;
+    int g = ds().pmgrid / 4;
+    return g < 8 ? 8 : g;
+}
 
 // ---------------------------------------------------------------- kernels
 
@@ -227,7 +237,7 @@ cuco_config_t dropin_config() {
     cuco_config_t c{};
     c.n = NumPart;
     c.pm_grid = ds().pmgrid;
-    c.cell_grid = cell_grid();
+    c.cell_grid = engine_grid();
     c.boxsize = All.BoxSize;
     c.mass = header.Mass;
     c.G = All.G;

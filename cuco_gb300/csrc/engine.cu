@@ -254,7 +254,8 @@ ShortRangeParams make_sr_params(const cuco_box *b) {
     p.cellw = b->cfg.boxsize / b->G;
     p.rcut = b->cfg.rcut;
     p.rcut2 = b->cfg.rcut * b->cfg.rcut;
-    p.asmthfac = (float)(0.5 / (double)b->cfg.asmth * (kNTab / 3.0));
+    p.asmthfac_d = 0.5 / (double)b->cfg.asmth * (kNTab / 3.0);
+    p.asmthfac = (float)p.asmthfac_d;
     p.mass = b->cfg.mass;
     p.G = (float)b->cfg.G;
     p.h = b->cfg.softening;
@@ -337,7 +338,7 @@ cuco_status_t cuco_config_reference(cuco_config_t *cfg) {
     float asmth = (float)(CUCO_ASMTH * (double)cfg->boxsize / cfg->pm_grid);
     cfg->asmth = asmth;
     cfg->rcut = (float)(CUCO_RCUT * (double)asmth);
-    if (cfg->cell_grid <= 0) cfg->cell_grid = cfg->pm_grid;
+    if (cfg->cell_grid <= 0) cfg->cell_grid = cfg->pm_grid / 4 < 8 ? 8 : cfg->pm_grid / 4;
     return CUCO_OK;
 }
 

@@ -31,10 +31,9 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr int kMaxStage = 2048;  // staged sources per chunk (32 KB)
-constexpr int kMaxR = 4;
+constexpr int kMaxR = 8;         // neighbour reach in cells (the reference's G = PMGRID needs 6)
 constexpr int kMaxCols = (2 * kMaxR + 1) * (2 * kMaxR + 1);
 constexpr int kMaxSeg = 4;
-constexpr int kMaxZ = kMaxSeg + 2 * kMaxR;  // z-cells per column
 constexpr unsigned kFull = 0xffffffffu;
 
 struct ColumnSet {
@@ -52,6 +51,14 @@ struct Run {
     uint32_t cnt;
     float sx, sy, sz;
 };
+
+// Dynamic shared memory: staged sources, split table, per-(column, z-cell)
+// staged offsets, column runs, column totals.
+__host__ __device__ inline size_t smem_bytes(int ncols, int nz) {
+    return sizeof(float4) * kMaxStage + sizeof(float) * kNTab +
+           sizeof(uint32_t) * (size_t)ncols * (nz + 1) + sizeof(Run) * 2 * (size_t)ncols +
+           sizeof(uint32_t) * (size_t)ncols;
+}
 
 template <CellFormat FMT>
 __device__ __forceinline__ void cell_range(const uint32_t *__restrict__ a,
@@ -80,15 +87,17 @@ __global__ void __launch_bounds__(kThreads)
                  const uint32_t *__restrict__ cb, const float *__restrict__ table_g,
                  float4 *__restrict__ acc_out, KickArgs kick,
                  unsigned long long *__restrict__ pair_counter) {
-    __shared__ float4 src[kMaxStage];
-    __shared__ float tab[kNTab];
-    __shared__ uint32_t coff[kMaxCols * (kMaxZ + 1)];
-    __shared__ Run runs[kMaxCols * 2];
-    __shared__ uint32_t coltot[kMaxCols];
+    extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
 
     const int G = p.grid;
     const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
+    const int zst = nz + 1;  // coff stride per column
+    float4 *src = smem_f4;
+    float *tab = reinterpret_cast<float *>(src + kMaxStage);
+    uint32_t *coff = reinterpret_cast<uint32_t *>(tab + kNTab);
+    Run *runs = reinterpret_cast<Run *>(coff + ncols * zst);
+    uint32_t *coltot = reinterpret_cast<uint32_t *>(runs + 2 * ncols);
     const int segs = G / S;
     const int seg = blockIdx.x;
     const int ix = seg / (G * segs);
@@ -121,8 +130,7 @@ __global__ void __launch_bounds__(kThreads)
 
     // per column: counts of its z-cells, runs of consecutive cells with one shift
     const float L = p.boxsize;
-    if (tid < ncols) {
-        const int col = tid;
+    for (int col = tid; col < ncols; col += kThreads) {
         int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
         int cx = cxu < 0 ? cxu + G : (cxu >= G ? cxu - G : cxu);
         int cy = cyu < 0 ? cyu + G : (cyu >= G ? cyu - G : cyu);
@@ -137,7 +145,7 @@ __global__ void __launch_bounds__(kThreads)
             int cz = czu - wrap * G;
             uint32_t st, cn;
             cell_range<FMT>(ca, cb, ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
-            coff[col * (kMaxZ + 1) + zc] = acc;  // relative, made absolute below
+            coff[col * zst + zc] = acc;  // relative, made absolute below
             if (wrap != prev_wrap) {
                 Run &r = runs[col * 2 + (nrun < 2 ? nrun : 1)];
                 r.gsrc = 0xffffffffu;
@@ -156,7 +164,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             acc += cn;
         }
-        coff[col * (kMaxZ + 1) + nz] = acc;
+        coff[col * zst + nz] = acc;
         if (nrun < 2) runs[col * 2 + 1].cnt = 0;
         coltot[col] = acc;
     }
@@ -171,13 +179,10 @@ __global__ void __launch_bounds__(kThreads)
         s_total = run;
     }
     __syncthreads();
-    for (int e = tid; e < ncols * (nz + 1); e += kThreads) {
-        int col = e / (nz + 1), zc = e % (nz + 1);
-        coff[col * (kMaxZ + 1) + zc] += coltot[col];
-    }
-    if (tid < ncols) {
-        runs[tid * 2].soff += coltot[tid];
-        runs[tid * 2 + 1].soff += coltot[tid];
+    for (int e = tid; e < ncols * zst; e += kThreads) coff[e] += coltot[e / zst];
+    for (int col = tid; col < ncols; col += kThreads) {
+        runs[col * 2].soff += coltot[col];
+        runs[col * 2 + 1].soff += coltot[col];
     }
     __syncthreads();
     const uint32_t total = s_total;
@@ -194,6 +199,18 @@ __global__ void __launch_bounds__(kThreads)
     const float rc2m = (p.rcut + cs.margin) * (p.rcut + cs.margin);
     const float zbase = (float)(iz0 - R);
     const float winv = 1.0f / w;
+    // Coordinates relative to an integer origin at the segment's corner: for a
+    // box size below 2^23 the origin and origin -/+ L are exact floats, so a
+    // staged source (x_j + shift - o) and the target (x_i - o) each carry at
+    // most one rounding and dx = s - t carries one more, with no rounding of a
+    // +-L image shift.
+    const float ox = floorf(ix * w), oy = floorf(iy * w), oz = floorf(iz0 * w);
+    // pairs whose float r^2 or table coordinate asmthfac*r lies within this
+    // relative distance of the cut or of a bin edge are decided in double,
+    // as the reference's CPU path computes them (gravlist.cpp:298-320)
+    const float kEdge = 4e-7f;
+    const float rc2_lo = p.rcut2 * (1.f - 2.f * kEdge), rc2_hi = p.rcut2 * (1.f + 2.f * kEdge);
+    const double rcut2_d = (double)p.rcut * (double)p.rcut;
     bool staged = false;
     uint32_t npairs = 0;
 
@@ -201,6 +218,7 @@ __global__ void __launch_bounds__(kThreads)
         const uint32_t t = tb + tid / tpt;
         const bool active = t < nt;
         float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float tx = pt.x - ox, ty = pt.y - oy, tz = pt.z - oz;
         float ax = 0.f, ay = 0.f, az = 0.f;
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
@@ -210,10 +228,11 @@ __global__ void __launch_bounds__(kThreads)
                 for (int rr = warp; rr < ncols * 2; rr += kThreads / 32) {
                     const Run r = runs[rr];
                     if (r.cnt == 0) continue;
+                    const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
                     uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
                     for (uint32_t s = lo + lane; s < hi; s += 32) {
                         float4 q = spos[r.gsrc + (s - r.soff)];
-                        src[s - c0] = make_float4(q.x + r.sx, q.y + r.sy, q.z + r.sz, 0.f);
+                        src[s - c0] = make_float4(q.x - cx, q.y - cy, q.z - cz, 0.f);
                     }
                 }
                 __syncthreads();
@@ -232,18 +251,30 @@ __global__ void __launch_bounds__(kThreads)
                     zlo = max(zlo, 0);
                     zhi = min(zhi, nz - 1);
                     if (zlo > zhi) continue;
-                    uint32_t b = coff[col * (kMaxZ + 1) + zlo];
-                    uint32_t e = coff[col * (kMaxZ + 1) + zhi + 1];
+                    uint32_t b = coff[col * zst + zlo];
+                    uint32_t e = coff[col * zst + zhi + 1];
                     b = max(b, c0);
                     e = min(e, c1);
                     for (uint32_t j = b + sub; j < e; j += tpt) {
                         float4 s = src[j - c0];
-                        float dx = s.x - pt.x, dy = s.y - pt.y, dz = s.z - pt.z;
+                        float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
                         float r2 = dx * dx + dy * dy + dz * dz;
-                        if (r2 > p.rcut2 || r2 == 0.f) continue;
-                        if (COUNT) ++npairs;
+                        if (r2 > rc2_hi || r2 == 0.f) continue;
                         float rinv = rsqrtf(r2);
                         float r = r2 * rinv;
+                        // bin = floor(asmthfac * r) without a conversion instruction:
+                        // a round-toward-zero add of 2^23 leaves floor(x) in the mantissa
+                        float xt = p.asmthfac * r;
+                        float xf = __fadd_rz(xt, 8388608.0f);
+                        int ti = __float_as_int(xf) - 0x4B000000;
+                        float frac = xt - (xf - 8388608.0f);
+                        if (frac < kEdge * xt || frac > 1.f - kEdge * xt || r2 > rc2_lo) {
+                            double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
+                            if (dd > rcut2_d) continue;
+                            ti = (int)(p.asmthfac_d * sqrt(dd));
+                        }
+                        if (ti >= kNTab) continue;
+                        if (COUNT) ++npairs;
                         float fac;
                         if (r >= p.h) {
                             fac = rinv * rinv * rinv;
@@ -255,13 +286,10 @@ __global__ void __launch_bounds__(kThreads)
                                 fac = p.h3inv * (21.33333f - 48.0f * u + 38.4f * u * u -
                                                  10.66667f * u * u * u - 0.06667f / (u * u * u));
                         }
-                        int ti = (int)(p.asmthfac * r);
-                        if (ti < kNTab) {
-                            fac *= tab[ti];
-                            ax += dx * fac;
-                            ay += dy * fac;
-                            az += dz * fac;
-                        }
+                        fac *= tab[ti];
+                        ax += dx * fac;
+                        ay += dy * fac;
+                        az += dz * fac;
                     }
                 }
             }
@@ -284,6 +312,11 @@ __global__ void __launch_bounds__(kThreads)
             const float mg = p.mass * p.G;
             float4 a = make_float4(ax * mg, ay * mg, az * mg, 0.f);
             acc_out[o] = a;
+            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (kick.acc_pm_s) {
+                g = kick.acc_pm_s[i];
+                if (kick.acc_pm_out) kick.acc_pm_out[o] = g;
+            }
             if (KICK) {
                 float4 v = kick.vel[o];
                 // dv = (float)(acc * dt); vel += dv  (timestep.c:57-58)
@@ -291,12 +324,10 @@ __global__ void __launch_bounds__(kThreads)
                 v.y += (float)((double)a.y * kick.kick_pp);
                 v.z += (float)((double)a.z * kick.kick_pp);
                 if (kick.acc_pm_s) {
-                    float4 g = kick.acc_pm_s[i];
                     // vel += GravPM * dt (timestep.c:88)
                     v.x = (float)((double)v.x + (double)g.x * kick.kick_pm);
                     v.y = (float)((double)v.y + (double)g.y * kick.kick_pm);
                     v.z = (float)((double)v.z + (double)g.z * kick.kick_pm);
-                    if (kick.acc_pm_out) kick.acc_pm_out[o] = g;
                 }
                 kick.vel[o] = v;
             }
@@ -338,11 +369,21 @@ void launch_fmt_kick(unsigned blocks, cudaStream_t stream, const ShortRangeParam
                      const ColumnSet &cs, const float4 *sorted_pos, const uint32_t *perm,
                      const uint32_t *cell_a, const uint32_t *cell_b, const float *table,
                      float4 *acc_out, const KickArgs &kick, unsigned long long *counter) {
+    const size_t sm = smem_bytes(cs.ncols, cs.S + 2 * cs.R);
+    static const size_t sm_max = smem_bytes(kMaxCols, kMaxSeg + 2 * kMaxR);
+    static bool attr = [] {
+        cudaFuncSetAttribute(k_shortrange<FMT, KICK, true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange<FMT, KICK, false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        return true;
+    }();
+    (void)attr;
     if (counter)
-        k_shortrange<FMT, KICK, true><<<blocks, kThreads, 0, stream>>>(
+        k_shortrange<FMT, KICK, true><<<blocks, kThreads, sm, stream>>>(
             p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
     else
-        k_shortrange<FMT, KICK, false><<<blocks, kThreads, 0, stream>>>(
+        k_shortrange<FMT, KICK, false><<<blocks, kThreads, sm, stream>>>(
             p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
 }
 
@@ -353,8 +394,8 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
                                 unsigned long long *pair_counter) {
     ColumnSet cs;
     if (!build_columns(p, &cs)) {
-        set_error("short range: cell grid too coarse for rcut (need rcut <= 4 cells, rcut < L/2 "
-                  "and at least S+2R cells per dimension)");
+        set_error("short range: cell grid does not fit rcut (need rcut <= 8 cell widths, "
+                  "rcut < L/2 and at least S+2R cells per dimension)");
         return CUCO_ERR_UNSUPPORTED;
     }
     if (p.n == 0) return CUCO_OK;

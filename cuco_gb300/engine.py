@@ -85,7 +85,7 @@ class BoxConfig:
         c = CucoConfig()
         c.n = self.n
         c.pm_grid = self.pm_grid
-        c.cell_grid = self.cell_grid or self.pm_grid
+        c.cell_grid = self.cell_grid or max(self.pm_grid // 4, 8)
         c.boxsize = self.boxsize
         c.mass = self.mass
         c.G = self.G

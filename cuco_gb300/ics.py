@@ -151,7 +151,7 @@ def zeldovich(n_side: int, boxsize_mpc: float, z_init: float, seed: int,
     disp = np.empty((n, n, n, 3), dtype=np.float64)
     for d, K in enumerate((KX, KY, KZ)):
         psi_k = 1j * K * inv_k2 * delta_k           # Mpc/h at z = 0
-        disp[..., d] = np.fft.irfftn(psi_k, s=(n, n, n)) * 1000.0 * D   # kpc/h at a
+        disp[..., d] = np.fft.irfftn(psi_k, s=(n, n, n), axes=(0, 1, 2)) * 1000.0 * D  # kpc/h at a
     q = (np.arange(n) + 0.5) * (L / n)
     Q = np.stack(np.meshgrid(q, q, q, indexing="ij"), axis=-1)
     pos = np.mod(Q + disp, L).reshape(-1, 3)

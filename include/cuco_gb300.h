@@ -184,7 +184,9 @@ typedef struct cuco_box cuco_box_t;
 
 /* Fill `cfg` with the reference's derived constants for a box:
  * asmth = ASMTH*L/M and rcut = RCUT*asmth rounded to float as pm_periodic.c:27-28
- * stores them; cell_grid = M (the reference's grid) unless already set. */
+ * stores them; cell_grid = M/4 (cell width 4 mesh cells, rcut = 1.4 cells)
+ * unless already set.  Any cell grid with rcut <= 8 cell widths gives the
+ * same forces; the reference's own grid is cell_grid = M. */
 cuco_status_t cuco_config_reference(cuco_config_t *cfg);
 
 cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **box);

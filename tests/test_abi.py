@@ -1,0 +1,103 @@
+"""The C ABI: the library loads without a GPU, exports every function the
+public headers declare, and its structs have the reference's layout."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle
+from cuco_gb300 import _native
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in ("cuco_gb300.h", "cuco_allvars.h")]
+
+
+def declared_functions():
+    names = set()
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", text, flags=re.M):
+            name = m.group(1)
+            if name not in ("if", "while", "for", "sizeof", "defined"):
+                names.add(name)
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cuco_gb300 import build
+    build.build()
+    return _native.load()
+
+
+def test_library_exports_every_declared_function(lib):
+    names = declared_functions()
+    assert len(names) >= 59
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the ctypes binding covers them all
+    assert names <= set(_native.SIGNATURES), names - set(_native.SIGNATURES)
+
+
+def test_reference_globals_are_exported(lib):
+    for g in ("P", "NumPart", "All", "header", "DriftTable", "GravKickTable", "sorter", "dOldPos",
+              "dSortedPos", "dGravAccel", "dGridParticleHash", "dGridParticleIndex", "dCellStart",
+              "dCellEnd", "numParticles", "numGridCells", "hPos", "hGravAccel"):
+        ctypes.c_void_p.in_dll(lib, g)
+
+
+def test_struct_sizes():
+    assert ctypes.sizeof(_native.Particle) == 60
+    assert ctypes.sizeof(_native.Header) == 32
+    assert ctypes.sizeof(_native.SimParam) == 4 * 1009
+    assert ctypes.sizeof(_native.SoftParam) == 12
+
+
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference sources not present")
+def test_layout_matches_reference_build():
+    ref = oracle.Reference(32)
+    out = (ctypes.c_long * 16)()
+    ref.lib.cref_layout(out)
+    A = _native.All
+    mine = [ctypes.sizeof(A), A.G.offset, A.Hubble.offset, A.Time.offset, A.Timebase_interval.offset,
+            A.Ti_Current.offset, A.PM_Ti_endstep.offset, A.Asmth.offset, A.ForceSoftening.offset,
+            A.OutputListTimes.offset, A.InitCondFile.offset, ctypes.sizeof(_native.Particle),
+            ctypes.sizeof(_native.Header), _native.Particle.GravPM.offset,
+            _native.Particle.Ti_endstep.offset, A.SofteningTable.offset]
+    assert list(out) == mine
+
+
+def test_header_compiles_as_c_with_reference_layout():
+    src = r'''
+#include <stddef.h>
+#include "cuco_gb300.h"
+_Static_assert(sizeof(PARTICLE) == 60, "PARTICLE");
+_Static_assert(sizeof(HEADER) == 32, "HEADER");
+_Static_assert(offsetof(ALL, Timebase_interval) == %d, "ALL");
+_Static_assert(sizeof(ALL) == %d, "ALL size");
+int main(void) { return 0; }
+''' % (_native.All.Timebase_interval.offset, ctypes.sizeof(_native.All))
+    with tempfile.TemporaryDirectory() as td:
+        f = os.path.join(td, "t.c")
+        open(f, "w").write(src)
+        r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                            f, "-o", os.path.join(td, "t")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
+def test_host_only_entry_points(lib):
+    """FP64 integrals run on the host: no device needed."""
+    d, k = ctypes.c_double(), ctypes.c_double()
+    assert lib.cuco_cosmo_factors(0.02, 1.0, 0.3, 0.7, 0.1, ctypes.byref(d), ctypes.byref(k)) == 0
+    port = oracle.Port()
+    dt, kt = port.drift_tables(0.02, 1.0, 0.3, 0.7, 0.1, 10)
+    assert d.value == pytest.approx(dt[-1], rel=1e-12)
+    assert k.value == pytest.approx(kt[-1], rel=1e-12)
+    assert lib.cuco_cosmo_factors(-1.0, 1.0, 0.3, 0.7, 0.1, ctypes.byref(d), ctypes.byref(k)) == 1
+    assert b"positive" in lib.cuco_last_error()
+    assert lib.cuco_version().startswith(b"cuco_gb300")

@@ -172,7 +172,9 @@ def test_dropin_drift_factors_and_move(port):
     ic = zeldovich(16, 50.0, seed=2)
     d = DropIn(ic, 32, 32, np.float32(0.03 * ic.boxsize / 16))
     lib = d.lib
-    drift, kick = port.drift_tables(float(np.float32(ic.a)), 1.0, 0.3, 0.7, ics.HUBBLE_INTERNAL)
+    # drift_integ reads All.Omega0, All.OmegaLambda, All.Hubble: floats (allvars.h:73-75)
+    f32 = lambda v: float(np.float32(v))  # noqa: E731
+    drift, kick = port.drift_tables(f32(ic.a), 1.0, f32(0.3), f32(0.7), f32(ics.HUBBLE_INTERNAL))
     l0, l1, tbi = np.log(np.float32(ic.a)), np.log(1.0), d.All.Timebase_interval
     for t0, t1 in [(0, 1 << 20), (1 << 20, 1 << 24), (12345, 1 << 28)]:
         assert lib.get_drift_factor(t0, t1) == pytest.approx(port.table_factor(drift, l0, l1, tbi, t0, t1), rel=1e-12)

@@ -1,0 +1,54 @@
+"""The GPU path against fixtures produced by the reference's own CPU code
+(tests/golden/make_golden.py): forces at the IC, and three passes of the
+reference's run loop driven through the drop-in C ABI."""
+import os
+
+import numpy as np
+import pytest
+
+from cuco_gb300 import Box, BoxConfig
+from conftest import rms_rel
+from dropin_host import DropIn
+
+pytestmark = pytest.mark.gpu
+
+FIX = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_n16_pm32.npz")
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return dict(np.load(FIX))
+
+
+@pytest.mark.parametrize("cell_grid", [32, 16, 8])
+def test_forces_vs_reference_fixture(gold, cell_grid):
+    M = int(gold["pmgrid"])
+    n = gold["pos"].shape[0]
+    box = Box(BoxConfig(n=n, pm_grid=M, cell_grid=cell_grid, boxsize=float(gold["boxsize"]),
+                        mass=float(gold["mass"]), G=float(gold["G"]), softening=float(gold["softening"]),
+                        asmth=float(gold["asmth"]), rcut=float(gold["rcut"])))
+    box.set_state(gold["pos"], gold["vel"])
+    box.forces()
+    _, _, app, apm = box.get_state()
+    e_pp, e_pm = rms_rel(app, gold["acc_pp"]), rms_rel(apm, gold["acc_pm"])
+    print(f"G={cell_grid}: pp {e_pp:.2e} pm {e_pm:.2e}")
+    assert e_pp < 1e-4 and e_pm < 1e-4
+    box.close()
+
+
+def test_dropin_run_loop_vs_reference(gold):
+    M = int(gold["pmgrid"])
+    d = DropIn(gold["pos"], gold["vel"], float(gold["mass"]), float(gold["boxsize"]),
+               float(gold["a_begin"]), M, 0, float(gold["eps"]))
+    assert d.All.Asmth == np.float32(gold["asmth"]) and d.All.Rcut == np.float32(gold["rcut"])
+    tis = [d.run_pass() for _ in range(3)]
+    assert tis == list(gold["run_ti_current"])
+    beg, end = d.timeline()
+    assert np.array_equal(beg, gold["run_ti_beg"]) and np.array_equal(end, gold["run_ti_end"])
+    assert [d.All.PM_Ti_begstep, d.All.PM_Ti_endstep, d.All.Ti_Current] == list(gold["run_pm_ti"])
+    assert rms_rel(d.field("GravAccel"), gold["run_acc_pp"]) < 1e-4
+    assert rms_rel(d.field("GravPM"), gold["run_acc_pm"]) < 1e-4
+    assert rms_rel(d.field("Vel"), gold["run_vel"]) < 1e-4
+    dx = np.abs(d.field("Pos") - gold["run_pos"])
+    dx = np.minimum(dx, float(gold["boxsize"]) - dx)
+    assert dx.max() < 1e-4 * float(gold["boxsize"])
