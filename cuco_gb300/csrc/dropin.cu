@@ -72,6 +72,7 @@ struct DropinState {
     size_t dP_n = 0;
     int *dflag = nullptr;  // timestep error flag + particle
     double *dtab = nullptr;  // FP64 kick table on the device
+    bool dtab_valid = false;
     double drift64[CUCO_DRIFT_TABLE_LENGTH];
     double kick64[CUCO_DRIFT_TABLE_LENGTH];
     double logTimeBegin = 0, logTimeMax = 0;
@@ -493,6 +494,12 @@ int get_timestep(int p) {
 void advance_and_find_timesteps(void) {
     DropinState &s = ds();
     if (!s.tables) init_drift_table();
+    if (!s.dtab_valid) {
+        const size_t bytes = sizeof(double) * CUCO_DRIFT_TABLE_LENGTH;
+        if (!s.dtab) capi_check(cudaMalloc(&s.dtab, bytes), "advance_and_find_timesteps");
+        capi_check(cudaMemcpy(s.dtab, s.kick64, bytes, cudaMemcpyHostToDevice), "advance_and_find_timesteps");
+        s.dtab_valid = true;
+    }
     upload_P(false);
     BoxView v = view();
     TimestepArgs a;
@@ -559,8 +566,10 @@ double gravkick_integ(double a, void *param) {
 
 void init_drift_table(void) {
     DropinState &s = ds();
-    s.logTimeBegin = log(All.TimeBegin);
-    s.logTimeMax = log(All.TimeMax);
+    // in C the float argument is promoted to double (driftfac.c:23-24); C++
+    // would pick the float overload of log
+    s.logTimeBegin = log((double)All.TimeBegin);
+    s.logTimeMax = log((double)All.TimeMax);
     const int n = CUCO_DRIFT_TABLE_LENGTH;
     double a0 = exp(s.logTimeBegin);
     for (int i = 0; i < n; ++i) {
@@ -570,9 +579,8 @@ void init_drift_table(void) {
         DriftTable[i] = (float)s.drift64[i];
         GravKickTable[i] = (float)s.kick64[i];
     }
-    if (!s.dtab) capi_check(cudaMalloc(&s.dtab, sizeof(double) * n), "init_drift_table");
-    capi_check(cudaMemcpy(s.dtab, s.kick64, sizeof(double) * n, cudaMemcpyHostToDevice), "init_drift_table");
     s.tables = true;
+    s.dtab_valid = false;  // uploaded by the next advance_and_find_timesteps
 }
 
 static double host_table_factor(const double *T, int t0, int t1) {

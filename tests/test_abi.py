@@ -90,6 +90,28 @@ int main(void) { return 0; }
         assert r.returncode == 0, r.stderr
 
 
+def test_dropin_drift_tables_host(lib):
+    """init_drift_table / get_drift_factor / get_gravkick_factor are host code:
+    FP64 tables with driftfac.c's interpolation, equal to the oracle's."""
+    from cuco_gb300._native import All
+    f32 = lambda v: float(np.float32(v))  # noqa: E731
+    al = All.in_dll(lib, "All")
+    al.Omega0, al.OmegaLambda, al.Hubble = 0.3, 0.7, 0.1
+    al.TimeBegin, al.TimeMax = 0.02, 1.0
+    al.Timebase_interval = (np.log(1.0) - np.log(np.float32(0.02))) / (1 << 28)
+    lib.init_drift_table()
+    port = oracle.Port()
+    d, k = port.drift_tables(f32(0.02), 1.0, f32(0.3), f32(0.7), f32(0.1))
+    l0 = np.log(f32(0.02))
+    for t0, t1 in [(0, 1 << 20), (1 << 20, 1 << 22), (7, 1 << 28)]:
+        assert lib.get_drift_factor(t0, t1) == port.table_factor(d, l0, 0.0, al.Timebase_interval, t0, t1)
+        assert lib.get_gravkick_factor(t0, t1) == port.table_factor(k, l0, 0.0, al.Timebase_interval, t0, t1)
+    tab = (ctypes.c_float * 1000).in_dll(lib, "DriftTable")
+    assert np.array_equal(np.array(tab[:], dtype=np.float32), d.astype(np.float32))
+    a = 0.5
+    assert lib.drift_integ(a, None) == pytest.approx(1 / (0.1 * np.sqrt(f32(0.3) / a ** 3 + f32(0.7)) * a ** 3), rel=1e-7)
+
+
 def test_host_only_entry_points(lib):
     """FP64 integrals run on the host: no device needed."""
     d, k = ctypes.c_double(), ctypes.c_double()
