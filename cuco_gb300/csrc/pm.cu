@@ -34,6 +34,7 @@ namespace cuco {
 namespace {
 
 constexpr int kFFTThreads = 256;
+constexpr int kLoadBatch = 8;  // global loads issued per thread before use
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -114,11 +115,23 @@ __global__ void __launch_bounds__(kFFTThreads)
     const int Mh = M / 2 + 1;
     const size_t r0 = (size_t)blockIdx.x * 2 * P;
     load_twiddles(tw_s, tw, M);
-    for (int e = threadIdx.x; e < 2 * P * M; e += blockDim.x) {
-        int row = e / M, m = e % M;
-        float v = rho[(r0 + row) * M + m];
-        float *slot = reinterpret_cast<float *>(&x[m * pitch + (row >> 1)]);
-        slot[row & 1] = v;
+    // kLoadBatch loads in flight per thread before their shared-memory stores
+    for (int e0 = threadIdx.x; e0 < 2 * P * M; e0 += kLoadBatch * blockDim.x) {
+        float v[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            int e = e0 + u * blockDim.x;
+            v[u] = e < 2 * P * M ? rho[r0 * M + e] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            int e = e0 + u * blockDim.x;
+            if (e < 2 * P * M) {
+                int row = e / M, m = e % M;
+                float *slot = reinterpret_cast<float *>(&x[m * pitch + (row >> 1)]);
+                slot[row & 1] = v[u];
+            }
+        }
     }
     __syncthreads();
     float2 *res = fft_columns(x, y, tw_s, M, P, pitch, -1);
@@ -146,11 +159,22 @@ __global__ void __launch_bounds__(kFFTThreads)
     const size_t r0 = (size_t)blockIdx.x * 2 * P;
     load_twiddles(tw_s, tw, M);
     // rows into y as h[row*Mh + k]
-    for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) {
-        int row = e / Mh, k = e % Mh;
-        float2 v = spec[(r0 + row) * Mh + k];
-        if (k == 0 || k == M / 2) v.y = 0.f;
-        y[row * Mh + k] = v;
+    for (int e0 = threadIdx.x; e0 < 2 * P * Mh; e0 += kLoadBatch * blockDim.x) {
+        float2 v[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            int e = e0 + u * blockDim.x;
+            v[u] = e < 2 * P * Mh ? spec[r0 * Mh + e] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            int e = e0 + u * blockDim.x;
+            if (e < 2 * P * Mh) {
+                int k = e % Mh;
+                if (k == 0 || k == M / 2) v[u].y = 0.f;
+                y[e] = v[u];
+            }
+        }
     }
     __syncthreads();
     for (int e = threadIdx.x; e < P * M; e += blockDim.x) {
@@ -191,9 +215,19 @@ __global__ void __launch_bounds__(kFFTThreads)
     const size_t sm_stride = axis == 1 ? (size_t)Mh : (size_t)M * Mh;
     const size_t base = axis == 1 ? (size_t)o * M * Mh : (size_t)o * Mh;
     load_twiddles(tw_s, tw, M);
-    for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
-        int m = e / B, b = e % B;
-        x[m * pitch + b] = b < nb ? spec[base + m * sm_stride + kz0 + b] : make_float2(0.f, 0.f);
+    for (int e0 = threadIdx.x; e0 < M * B; e0 += kLoadBatch * blockDim.x) {
+        float2 v[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            int e = e0 + u * blockDim.x;
+            int m = e / B, b = e % B;
+            v[u] = (e < M * B && b < nb) ? spec[base + m * sm_stride + kz0 + b] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            int e = e0 + u * blockDim.x;
+            if (e < M * B) x[e] = v[u];  // pitch == B
+        }
     }
     __syncthreads();
     float2 *res = fft_columns(x, y, tw_s, M, B, pitch, sign);

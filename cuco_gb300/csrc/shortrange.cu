@@ -2,27 +2,39 @@
 //
 // Reference: cudaForceEvaluateShortrangeD + calcForce (gravlist_kernel.cu:20-88,
 // 162-234) and the CPU force_evaluate_shortrange (gravlist.cpp:216-338).  The
-// pair law is the reference's: min-image separation, cut at r^2 > rcut^2, 1/r^2
-// outside the spline softening length h and GADGET's spline inside, times the
-// nearest-bin erfc split factor T[(int)(asmthfac*r)] (NTAB = 1000 bins).
+// pair law is the reference's: minimum-image separation, cut at r^2 > rcut^2,
+// 1/r^2 outside the spline softening length h and GADGET's spline inside,
+// times the nearest-bin erfc split factor T[(int)(asmthfac*r)] (NTAB = 1000).
 //
-// Layout of the work (GB300-first rather than one thread per particle over a
-// full cube of cells):
+// Work layout (GB300-first rather than one thread per particle over a full
+// cube of cells):
 //   * one CTA per z-segment of S consecutive cells (ix, iy, iz0..iz0+S-1); its
 //     targets are one contiguous range of the cell-sorted particles;
-//   * the sources are the cells of the neighbour columns (dx, dy) whose
-//     xy-distance from the segment is below rcut, over z-cells
-//     iz0-R .. iz0+S-1+R.  Within a column those cells are consecutive keys, so
-//     they are at most two contiguous runs of sorted particles (two when the
-//     z range wraps), which warps copy into shared memory with the periodic
-//     image shift already added - no per-pair minimum-image test;
-//   * each target culls columns by its own xy-distance and narrows each column
-//     to the z-cells within sqrt(rcut^2 - d_xy^2), so it visits ~2.5x fewer
-//     candidates than the reference's per-particle cube;
-//   * sparse segments give several lanes to one target (a power of two, up to
-//     a warp); the lanes' partial sums are combined with xor shuffles;
-//   * the epilogue writes the force in original particle order and, in the
-//     engine's step, applies the kick to the velocity (timestep.c:56-59,86-91).
+//   * the sources are the neighbour columns (dx, dy) within rcut of the
+//     segment in xy, over z-cells iz0-R .. iz0+S-1+R.  A column's cells are
+//     consecutive keys, so it is at most two contiguous runs of sorted
+//     particles (two when the z range wraps); warps copy the runs into shared
+//     memory relative to an integer origin at the segment corner, with the
+//     periodic image shift applied once per run;
+//   * candidate generation: every lane owns (a share of) one target, culls
+//     columns by the target's xy distance, narrows each column to the z-cells
+//     within sqrt(rcut^2 - d_xy^2), and tests candidates by r^2 only.
+//     Accepted pairs go to a per-warp queue in shared memory (ballot + popc);
+//   * force evaluation runs on full batches of 32 queued pairs, so the
+//     rsqrt, split-table lookup and bin-edge test are spent only on in-range
+//     pairs (about a third of the candidates) with every lane busy; partial
+//     sums are added into per-target shared-memory accumulators;
+//   * the epilogue scatters the force to original particle order and, in the
+//     engine's step, kicks the velocity (timestep.c:56-59,86-91).
+//
+// Precision of the plain path.  A float computation of asmthfac*r lands in the
+// neighbouring table bin for ~3e-5 of the pairs, and at high redshift (net
+// force a small residual of cancelling pair terms) that alone costs ~1.6e-4
+// rms against the reference's double path.  Coordinates relative to an integer
+// origin make the image shift exact (origin -/+ L is an exact float for
+// L < 2^23) and dx exact for ~97% of pairs; pairs whose r^2 lies within
+// 4e-7 of rcut^2 or whose asmthfac*r lies within 4e-7 (relative) of a bin edge
+// are decided in double as gravlist.cpp:298-320 does.
 #include "common.cuh"
 
 namespace cuco {
@@ -30,10 +42,12 @@ namespace cuco {
 namespace {
 
 constexpr int kThreads = 128;
+constexpr int kWarps = kThreads / 32;
 constexpr int kMaxStage = 2048;  // staged sources per chunk (32 KB)
 constexpr int kMaxR = 8;         // neighbour reach in cells (the reference's G = PMGRID needs 6)
 constexpr int kMaxCols = (2 * kMaxR + 1) * (2 * kMaxR + 1);
 constexpr int kMaxSeg = 4;
+constexpr int kQueue = 64;       // per-warp pair queue (ring)
 constexpr unsigned kFull = 0xffffffffu;
 
 struct ColumnSet {
@@ -52,11 +66,13 @@ struct Run {
     float sx, sy, sz;
 };
 
-// Dynamic shared memory: staged sources, split table, per-(column, z-cell)
-// staged offsets, column runs, column totals.
+// Dynamic shared memory, in order: staged sources, target positions, target
+// accumulators, split table, pair queues, per-(column, z-cell) staged offsets,
+// cell starts and counts, column runs, column totals.
 __host__ __device__ inline size_t smem_bytes(int ncols, int nz) {
-    return sizeof(float4) * kMaxStage + sizeof(float) * kNTab +
-           sizeof(uint32_t) * (size_t)ncols * (nz + 1) + sizeof(Run) * 2 * (size_t)ncols +
+    return sizeof(float4) * (kMaxStage + 2 * kThreads) + sizeof(float) * kNTab +
+           sizeof(uint32_t) * kWarps * kQueue + sizeof(uint32_t) * (size_t)ncols * (nz + 1) +
+           2 * sizeof(uint32_t) * (size_t)ncols * nz + sizeof(Run) * 2 * (size_t)ncols +
            sizeof(uint32_t) * (size_t)ncols;
 }
 
@@ -80,6 +96,12 @@ __device__ __forceinline__ void cell_range(const uint32_t *__restrict__ a,
     }
 }
 
+// r^2 with a fixed operation order: the candidate test and the force pass
+// must agree on it bit for bit.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
 template <CellFormat FMT, bool KICK, bool COUNT>
 __global__ void __launch_bounds__(kThreads)
     k_shortrange(ShortRangeParams p, ColumnSet cs, const float4 *__restrict__ spos,
@@ -94,25 +116,46 @@ __global__ void __launch_bounds__(kThreads)
     const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
     const int zst = nz + 1;  // coff stride per column
     float4 *src = smem_f4;
-    float *tab = reinterpret_cast<float *>(src + kMaxStage);
-    uint32_t *coff = reinterpret_cast<uint32_t *>(tab + kNTab);
-    Run *runs = reinterpret_cast<Run *>(coff + ncols * zst);
+    float4 *tgt = src + kMaxStage;
+    float4 *accs = tgt + kThreads;
+    float *tab = reinterpret_cast<float *>(accs + kThreads);
+    uint32_t *queue = reinterpret_cast<uint32_t *>(tab + kNTab);
+    uint32_t *coff = queue + kWarps * kQueue;
+    uint32_t *cst = coff + ncols * zst;
+    uint32_t *ccn = cst + ncols * nz;
+    Run *runs = reinterpret_cast<Run *>(ccn + ncols * nz);
     uint32_t *coltot = reinterpret_cast<uint32_t *>(runs + 2 * ncols);
+
     const int segs = G / S;
     const int seg = blockIdx.x;
     const int ix = seg / (G * segs);
     const int iy = (seg / segs) % G;
     const int iz0 = (seg % segs) * S;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float L = p.boxsize;
 
-    // targets: the sorted particles of cells (ix, iy, iz0 .. iz0+S-1)
+    // every (column, z-cell) range, loaded in parallel
+    for (int e = tid; e < ncols * nz; e += kThreads) {
+        const int col = e / nz, zc = e % nz;
+        int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col], czu = iz0 - R + zc;
+        int cx = cxu < 0 ? cxu + G : (cxu >= G ? cxu - G : cxu);
+        int cy = cyu < 0 ? cyu + G : (cyu >= G ? cyu - G : cyu);
+        int cz = czu < 0 ? czu + G : (czu >= G ? czu - G : czu);
+        uint32_t st, cn;
+        cell_range<FMT>(ca, cb, ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
+        cst[e] = st;
+        ccn[e] = cn;
+    }
+    __syncthreads();
     if (tid == 0) {
-        uint32_t c0 = ((uint32_t)ix * G + iy) * G + iz0;
+        // the segment's cells are column (0, 0), z-cells R .. R+S-1
+        int c00 = -1;
+        for (int col = 0; col < ncols; ++col)
+            if (cs.dx[col] == 0 && cs.dy[col] == 0) c00 = col;
         uint32_t tb = 0, te = 0;
         bool found = false;
         for (int k = 0; k < S; ++k) {
-            uint32_t st, cn;
-            cell_range<FMT>(ca, cb, c0 + k, &st, &cn);
+            const uint32_t st = cst[c00 * nz + R + k], cn = ccn[c00 * nz + R + k];
             if (cn) {
                 if (!found) tb = st;
                 found = true;
@@ -128,12 +171,9 @@ __global__ void __launch_bounds__(kThreads)
 
     for (int i = tid; i < kNTab; i += kThreads) tab[i] = table_g[i];
 
-    // per column: counts of its z-cells, runs of consecutive cells with one shift
-    const float L = p.boxsize;
+    // per column: staged offsets of its z-cells, runs of consecutive cells with one shift
     for (int col = tid; col < ncols; col += kThreads) {
         int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
-        int cx = cxu < 0 ? cxu + G : (cxu >= G ? cxu - G : cxu);
-        int cy = cyu < 0 ? cyu + G : (cyu >= G ? cyu - G : cyu);
         float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
         float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
         uint32_t acc = 0;
@@ -142,9 +182,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int zc = 0; zc < nz; ++zc) {
             int czu = iz0 - R + zc;
             int wrap = czu < 0 ? -1 : (czu >= G ? 1 : 0);
-            int cz = czu - wrap * G;
-            uint32_t st, cn;
-            cell_range<FMT>(ca, cb, ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
+            const uint32_t st = cst[col * nz + zc], cn = ccn[col * nz + zc];
             coff[col * zst + zc] = acc;  // relative, made absolute below
             if (wrap != prev_wrap) {
                 Run &r = runs[col * 2 + (nrun < 2 ? nrun : 1)];
@@ -188,129 +226,169 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t total = s_total;
     const bool single_chunk = total <= (uint32_t)kMaxStage;
 
-    // lanes per target
+    // lanes per target (a power of two): sparse segments split a target's
+    // columns over several lanes
     const uint32_t nt = t_end - t_begin;
     int tpt = 1;
     while (tpt < 32 && (uint32_t)(tpt * 2) * nt <= (uint32_t)kThreads) tpt *= 2;
     const int tpc = kThreads / tpt;
     const int sub = tid & (tpt - 1);
+    const int slot = tid / tpt;
 
     const float w = p.cellw;
     const float rc2m = (p.rcut + cs.margin) * (p.rcut + cs.margin);
     const float zbase = (float)(iz0 - R);
     const float winv = 1.0f / w;
-    // Coordinates relative to an integer origin at the segment's corner: for a
-    // box size below 2^23 the origin and origin -/+ L are exact floats, so a
-    // staged source (x_j + shift - o) and the target (x_i - o) each carry at
-    // most one rounding and dx = s - t carries one more, with no rounding of a
-    // +-L image shift.
+    // integer origin at the segment corner (see the file comment)
     const float ox = floorf(ix * w), oy = floorf(iy * w), oz = floorf(iz0 * w);
-    // pairs whose float r^2 or table coordinate asmthfac*r lies within this
-    // relative distance of the cut or of a bin edge are decided in double,
-    // as the reference's CPU path computes them (gravlist.cpp:298-320)
     const float kEdge = 4e-7f;
     const float rc2_lo = p.rcut2 * (1.f - 2.f * kEdge), rc2_hi = p.rcut2 * (1.f + 2.f * kEdge);
     const double rcut2_d = (double)p.rcut * (double)p.rcut;
+    uint32_t *q = queue + warp * kQueue;
+    const uint32_t lt = (1u << lane) - 1u;
     bool staged = false;
     uint32_t npairs = 0;
 
+    // Force on up to 32 queued pairs starting at ring position `head`.
+    auto flush = [&](uint32_t head, uint32_t n, uint32_t c0) {
+        if ((uint32_t)lane < n) {
+            const uint32_t ent = q[(head + lane) & (kQueue - 1)];
+            const uint32_t sl = ent >> 16;
+            const float4 tp = tgt[sl];
+            const float4 s = src[ent & 0xffffu];
+            const float dx = s.x - tp.x, dy = s.y - tp.y, dz = s.z - tp.z;
+            const float r2 = dist2(dx, dy, dz);
+            const float rinv = rsqrtf(r2);
+            const float r = r2 * rinv;
+            // bin = floor(asmthfac * r) without a conversion instruction: a
+            // round-toward-zero add of 2^23 leaves floor(x) in the mantissa
+            const float xt = p.asmthfac * r;
+            const float xf = __fadd_rz(xt, 8388608.0f);
+            int ti = __float_as_int(xf) - 0x4B000000;
+            const float frac = xt - (xf - 8388608.0f);
+            bool use = true;
+            if (frac < kEdge * xt || frac > 1.f - kEdge * xt || r2 > rc2_lo) {
+                const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
+                use = dd <= rcut2_d;
+                ti = (int)(p.asmthfac_d * sqrt(dd));
+            }
+            if (use && ti < kNTab) {
+                float fac;
+                if (r >= p.h) {
+                    fac = rinv * rinv * rinv;
+                } else {
+                    const float u = r * p.hinv;
+                    if (u < 0.5f)
+                        fac = p.h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
+                    else
+                        fac = p.h3inv * (21.33333f - 48.0f * u + 38.4f * u * u -
+                                         10.66667f * u * u * u - 0.06667f / (u * u * u));
+                }
+                fac *= tab[ti];
+                atomicAdd(&accs[sl].x, dx * fac);
+                atomicAdd(&accs[sl].y, dy * fac);
+                atomicAdd(&accs[sl].z, dz * fac);
+                if (COUNT) ++npairs;
+            }
+        }
+        (void)c0;
+    };
+
     for (uint32_t tb = 0; tb < nt; tb += tpc) {
-        const uint32_t t = tb + tid / tpt;
+        const uint32_t t = tb + slot;
         const bool active = t < nt;
-        float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float tx = pt.x - ox, ty = pt.y - oy, tz = pt.z - oz;
-        float ax = 0.f, ay = 0.f, az = 0.f;
+        if (sub == 0) {
+            tgt[slot] = make_float4(tx, ty, tz, 0.f);
+            accs[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        __syncthreads();
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
             if (!(single_chunk && staged)) {
                 __syncthreads();
                 // stage [c0, c1): warp per run
-                for (int rr = warp; rr < ncols * 2; rr += kThreads / 32) {
+                for (int rr = warp; rr < ncols * 2; rr += kWarps) {
                     const Run r = runs[rr];
                     if (r.cnt == 0) continue;
                     const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
                     uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
-                    for (uint32_t s = lo + lane; s < hi; s += 32) {
-                        float4 q = spos[r.gsrc + (s - r.soff)];
-                        src[s - c0] = make_float4(q.x - cx, q.y - cy, q.z - cz, 0.f);
+                    for (uint32_t s0 = lo + lane; s0 < hi; s0 += 64) {
+                        const uint32_t s1 = s0 + 32;
+                        const float4 a0 = spos[r.gsrc + (s0 - r.soff)];
+                        float4 a1 = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (s1 < hi) a1 = spos[r.gsrc + (s1 - r.soff)];
+                        src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
+                        if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
                     }
                 }
                 __syncthreads();
                 staged = true;
             }
-            if (active) {
-                for (int col = 0; col < ncols; ++col) {
-                    float x0 = (ix + cs.dx[col]) * w, y0 = (iy + cs.dy[col]) * w;
-                    float ddx = fmaxf(fmaxf(x0 - pt.x, pt.x - (x0 + w)), 0.f);
-                    float ddy = fmaxf(fmaxf(y0 - pt.y, pt.y - (y0 + w)), 0.f);
-                    float d2 = ddx * ddx + ddy * ddy;
+            // candidate generation: lane sub of a target takes columns sub, sub+tpt, ...
+            int col = sub - tpt;
+            uint32_t j = 0, e = 0;
+            bool done = !active;
+            uint32_t head = 0, tail = 0;
+            while (true) {
+                while (!done && j >= e) {
+                    col += tpt;
+                    if (col >= ncols) {
+                        done = true;
+                        break;
+                    }
+                    const float x0 = (ix + cs.dx[col]) * w, y0 = (iy + cs.dy[col]) * w;
+                    const float ddx = fmaxf(fmaxf(x0 - pt.x, pt.x - (x0 + w)), 0.f);
+                    const float ddy = fmaxf(fmaxf(y0 - pt.y, pt.y - (y0 + w)), 0.f);
+                    const float d2 = ddx * ddx + ddy * ddy;
                     if (d2 > rc2m) continue;
-                    float hz = sqrtf(rc2m - d2);
+                    const float hz = sqrtf(rc2m - d2);
                     int zlo = (int)floorf((pt.z - hz) * winv - zbase);
                     int zhi = (int)floorf((pt.z + hz) * winv - zbase);
                     zlo = max(zlo, 0);
                     zhi = min(zhi, nz - 1);
                     if (zlo > zhi) continue;
-                    uint32_t b = coff[col * zst + zlo];
-                    uint32_t e = coff[col * zst + zhi + 1];
-                    b = max(b, c0);
-                    e = min(e, c1);
-                    for (uint32_t j = b + sub; j < e; j += tpt) {
-                        float4 s = src[j - c0];
-                        float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
-                        float r2 = dx * dx + dy * dy + dz * dz;
-                        if (r2 > rc2_hi || r2 == 0.f) continue;
-                        float rinv = rsqrtf(r2);
-                        float r = r2 * rinv;
-                        // bin = floor(asmthfac * r) without a conversion instruction:
-                        // a round-toward-zero add of 2^23 leaves floor(x) in the mantissa
-                        float xt = p.asmthfac * r;
-                        float xf = __fadd_rz(xt, 8388608.0f);
-                        int ti = __float_as_int(xf) - 0x4B000000;
-                        float frac = xt - (xf - 8388608.0f);
-                        if (frac < kEdge * xt || frac > 1.f - kEdge * xt || r2 > rc2_lo) {
-                            double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
-                            if (dd > rcut2_d) continue;
-                            ti = (int)(p.asmthfac_d * sqrt(dd));
-                        }
-                        if (ti >= kNTab) continue;
-                        if (COUNT) ++npairs;
-                        float fac;
-                        if (r >= p.h) {
-                            fac = rinv * rinv * rinv;
-                        } else {
-                            float u = r * p.hinv;
-                            if (u < 0.5f)
-                                fac = p.h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
-                            else
-                                fac = p.h3inv * (21.33333f - 48.0f * u + 38.4f * u * u -
-                                                 10.66667f * u * u * u - 0.06667f / (u * u * u));
-                        }
-                        fac *= tab[ti];
-                        ax += dx * fac;
-                        ay += dy * fac;
-                        az += dz * fac;
-                    }
+                    j = max(coff[col * zst + zlo], c0);
+                    e = min(coff[col * zst + zhi + 1], c1);
+                }
+                const bool have = !done;
+                if (!__any_sync(kFull, have)) break;
+                bool take = false;
+                const uint32_t jj = j;
+                if (have) {
+                    const float4 s = src[j - c0];
+                    const float r2 = dist2(s.x - tx, s.y - ty, s.z - tz);
+                    take = r2 <= rc2_hi && r2 != 0.f;
+                    ++j;
+                }
+                const uint32_t m = __ballot_sync(kFull, take);
+                if (take) q[(tail + __popc(m & lt)) & (kQueue - 1)] = ((uint32_t)slot << 16) | (jj - c0);
+                tail += __popc(m);
+                if (tail - head >= 32) {
+                    __syncwarp();
+                    flush(head, 32, c0);
+                    head += 32;
+                    __syncwarp();
                 }
             }
+            __syncwarp();
+            if (tail != head) flush(head, tail - head, c0);
+            __syncwarp();
         }
         if (COUNT) {
-            // one atomic per warp
             uint32_t wsum = npairs;
             for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
             if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
             npairs = 0;
         }
-        for (int off = tpt >> 1; off > 0; off >>= 1) {
-            ax += __shfl_xor_sync(kFull, ax, off);
-            ay += __shfl_xor_sync(kFull, ay, off);
-            az += __shfl_xor_sync(kFull, az, off);
-        }
+        __syncthreads();  // every warp's pairs for this pass are in accs
         if (active && sub == 0) {
             const uint32_t i = t_begin + t;
             const uint32_t o = perm[i];
             const float mg = p.mass * p.G;
-            float4 a = make_float4(ax * mg, ay * mg, az * mg, 0.f);
+            const float4 acc = accs[slot];
+            const float4 a = make_float4(acc.x * mg, acc.y * mg, acc.z * mg, 0.f);
             acc_out[o] = a;
             float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
             if (kick.acc_pm_s) {
@@ -319,15 +397,16 @@ __global__ void __launch_bounds__(kThreads)
             }
             if (KICK) {
                 float4 v = kick.vel[o];
-                // dv = (float)(acc * dt); vel += dv  (timestep.c:57-58)
-                v.x += (float)((double)a.x * kick.kick_pp);
-                v.y += (float)((double)a.y * kick.kick_pp);
-                v.z += (float)((double)a.z * kick.kick_pp);
+                // vel += GravAccel*dt; vel += GravPM*dt (timestep.c:57-58,88), in
+                // float (the reference rounds each product to float first)
+                const float kp = (float)kick.kick_pp, km = (float)kick.kick_pm;
+                v.x += __fmul_rn(a.x, kp);
+                v.y += __fmul_rn(a.y, kp);
+                v.z += __fmul_rn(a.z, kp);
                 if (kick.acc_pm_s) {
-                    // vel += GravPM * dt (timestep.c:88)
-                    v.x = (float)((double)v.x + (double)g.x * kick.kick_pm);
-                    v.y = (float)((double)v.y + (double)g.y * kick.kick_pm);
-                    v.z = (float)((double)v.z + (double)g.z * kick.kick_pm);
+                    v.x = __fmaf_rn(g.x, km, v.x);
+                    v.y = __fmaf_rn(g.y, km, v.y);
+                    v.z = __fmaf_rn(g.z, km, v.z);
                 }
                 kick.vel[o] = v;
             }

@@ -175,7 +175,7 @@ def test_dropin_drift_factors_and_move(port):
     # drift_integ reads All.Omega0, All.OmegaLambda, All.Hubble: floats (allvars.h:73-75)
     f32 = lambda v: float(np.float32(v))  # noqa: E731
     drift, kick = port.drift_tables(f32(ic.a), 1.0, f32(0.3), f32(0.7), f32(ics.HUBBLE_INTERNAL))
-    l0, l1, tbi = np.log(np.float32(ic.a)), np.log(1.0), d.All.Timebase_interval
+    l0, l1, tbi = np.log(float(np.float32(ic.a))), np.log(1.0), d.All.Timebase_interval
     for t0, t1 in [(0, 1 << 20), (1 << 20, 1 << 24), (12345, 1 << 28)]:
         assert lib.get_drift_factor(t0, t1) == pytest.approx(port.table_factor(drift, l0, l1, tbi, t0, t1), rel=1e-12)
         assert lib.get_gravkick_factor(t0, t1) == pytest.approx(port.table_factor(kick, l0, l1, tbi, t0, t1), rel=1e-12)
