@@ -136,6 +136,7 @@ SIGNATURES = {
     "cuco_pinned_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "cuco_pinned_free": (_I, [_P]),
     "cuco_fp32_peak": (_I, [_I, ctypes.POINTER(_D)]),
+    "cuco_radix_sort_noalloc": (_I, [_P, _P, _U, _U, _P]),
     "cuco_cosmo_factors": (_I, [_D, _D, _D, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D)]),
     "cuco_last_error": (ctypes.c_char_p, []),
     "cuco_version": (ctypes.c_char_p, []),

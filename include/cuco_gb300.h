@@ -248,6 +248,21 @@ cuco_status_t cuco_box_timer(cuco_box_t *box, int op, float *ms);
 cuco_status_t cuco_pinned_alloc(size_t bytes, void **ptr);
 cuco_status_t cuco_pinned_free(void *ptr);
 
+/* Stable sort of (keys, values) by the low key_bits bits, in place, that
+ * allocates no device memory (no counterpart in the reference).  For callers
+ * that must not allocate where they sort: cudaMalloc/cudaFree can synchronize
+ * the device and stall other streams, and hosts that give each job a fixed HBM
+ * slice up front cannot let a library grow mid-run.  Scratch comes from one
+ * array compiled into the library: at most 2^20 elements per call (larger n is
+ * rejected with CUCO_ERR_INVALID); 8.25 MiB held on every GPU that loads the
+ * library, until exit.  All calls on a device share that array, so calls that
+ * overlap on the GPU race; order them on one stream.  The first call on a
+ * device (with it current) looks up the array's device address; make it
+ * before any stream capture on that device.  values may be NULL (keys only);
+ * stream is a cudaStream_t (NULL: legacy default stream). */
+cuco_status_t cuco_radix_sort_noalloc(uint32_t *keys, uint32_t *values, uint32_t n,
+                                      uint32_t key_bits, void *stream);
+
 /* Measured FP32 FMA throughput of `device` in TFLOP/s (2 flops per FMA): a
  * register-resident FMA chain on every SM, timed with CUDA events. */
 cuco_status_t cuco_fp32_peak(int device, double *tflops);
