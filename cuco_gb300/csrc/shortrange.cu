@@ -16,14 +16,19 @@
 //     particles (two when the z range wraps); warps copy the runs into shared
 //     memory relative to an integer origin at the segment corner, with the
 //     periodic image shift applied once per run;
-//   * candidate generation: every lane owns (a share of) one target, culls
-//     columns by the target's xy distance, narrows each column to the z-cells
-//     within sqrt(rcut^2 - d_xy^2), and tests candidates by r^2 only.
-//     Accepted pairs go to a per-warp queue in shared memory (ballot + popc);
-//   * force evaluation runs on full batches of 32 queued pairs, so the
-//     rsqrt, split-table lookup and bin-edge test are spent only on in-range
-//     pairs (about a third of the candidates) with every lane busy; partial
-//     sums are added into per-target shared-memory accumulators;
+//   * each target has one lane, or a power-of-two group of lanes when the
+//     segment is sparse; its lanes cull columns by the target's xy distance,
+//     narrow each column to the z-cells within sqrt(rcut^2 - d_xy^2), and walk
+//     those sources (lane k of the group takes every tpt-th one, so the group
+//     reads consecutive staged sources);
+//   * the pair law runs without branches on the common path (a candidate
+//     beyond the cut gets a zero factor), two candidates per iteration into
+//     two accumulator sets for instruction-level parallelism.  Lanes of a warp
+//     hold different targets, so any per-candidate branch would be taken by
+//     some lane and cost the whole warp anyway;
+//   * 256-thread CTAs over 8-cell segments keep 8+ warps per scheduler on the
+//     shared memory a segment needs;
+//   * the lanes of a target add their partial sums with xor shuffles;
 //   * the epilogue scatters the force to original particle order and, in the
 //     engine's step, kicks the velocity (timestep.c:56-59,86-91).
 //
@@ -41,13 +46,12 @@ namespace cuco {
 
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxStage = 2048;  // staged sources per chunk (32 KB)
 constexpr int kMaxR = 8;         // neighbour reach in cells (the reference's G = PMGRID needs 6)
 constexpr int kMaxCols = (2 * kMaxR + 1) * (2 * kMaxR + 1);
-constexpr int kMaxSeg = 4;
-constexpr int kQueue = 64;       // per-warp pair queue (ring)
+constexpr int kMaxSeg = 8;
 constexpr unsigned kFull = 0xffffffffu;
 
 struct ColumnSet {
@@ -66,12 +70,11 @@ struct Run {
     float sx, sy, sz;
 };
 
-// Dynamic shared memory, in order: staged sources, target positions, target
-// accumulators, split table, pair queues, per-(column, z-cell) staged offsets,
-// cell starts and counts, column runs, column totals.
+// Dynamic shared memory, in order: staged sources, split table,
+// per-(column, z-cell) staged offsets, cell starts and counts, column runs,
+// column totals.
 __host__ __device__ inline size_t smem_bytes(int ncols, int nz) {
-    return sizeof(float4) * (kMaxStage + 2 * kThreads) + sizeof(float) * kNTab +
-           sizeof(uint32_t) * kWarps * kQueue + sizeof(uint32_t) * (size_t)ncols * (nz + 1) +
+    return sizeof(float4) * kMaxStage + sizeof(float) * kNTab + sizeof(uint32_t) * (size_t)ncols * (nz + 1) +
            2 * sizeof(uint32_t) * (size_t)ncols * nz + sizeof(Run) * 2 * (size_t)ncols +
            sizeof(uint32_t) * (size_t)ncols;
 }
@@ -103,7 +106,7 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
 }
 
 template <CellFormat FMT, bool KICK, bool COUNT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     k_shortrange(ShortRangeParams p, ColumnSet cs, const float4 *__restrict__ spos,
                  const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
                  const uint32_t *__restrict__ cb, const float *__restrict__ table_g,
@@ -116,11 +119,8 @@ __global__ void __launch_bounds__(kThreads)
     const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
     const int zst = nz + 1;  // coff stride per column
     float4 *src = smem_f4;
-    float4 *tgt = src + kMaxStage;
-    float4 *accs = tgt + kThreads;
-    float *tab = reinterpret_cast<float *>(accs + kThreads);
-    uint32_t *queue = reinterpret_cast<uint32_t *>(tab + kNTab);
-    uint32_t *coff = queue + kWarps * kQueue;
+    float *tab = reinterpret_cast<float *>(src + kMaxStage);
+    uint32_t *coff = reinterpret_cast<uint32_t *>(tab + kNTab);
     uint32_t *cst = coff + ncols * zst;
     uint32_t *ccn = cst + ncols * nz;
     Run *runs = reinterpret_cast<Run *>(ccn + ncols * nz);
@@ -226,14 +226,13 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t total = s_total;
     const bool single_chunk = total <= (uint32_t)kMaxStage;
 
-    // lanes per target (a power of two): sparse segments split a target's
-    // columns over several lanes
+    // lanes per target (a power of two): sparse segments give a target
+    // several lanes, which take interleaved sources of each of its ranges
     const uint32_t nt = t_end - t_begin;
     int tpt = 1;
     while (tpt < 32 && (uint32_t)(tpt * 2) * nt <= (uint32_t)kThreads) tpt *= 2;
     const int tpc = kThreads / tpt;
     const int sub = tid & (tpt - 1);
-    const int slot = tid / tpt;
 
     const float w = p.cellw;
     const float rc2m = (p.rcut + cs.margin) * (p.rcut + cs.margin);
@@ -244,66 +243,65 @@ __global__ void __launch_bounds__(kThreads)
     const float kEdge = 4e-7f;
     const float rc2_lo = p.rcut2 * (1.f - 2.f * kEdge), rc2_hi = p.rcut2 * (1.f + 2.f * kEdge);
     const double rcut2_d = (double)p.rcut * (double)p.rcut;
-    uint32_t *q = queue + warp * kQueue;
-    const uint32_t lt = (1u << lane) - 1u;
     bool staged = false;
     uint32_t npairs = 0;
 
-    // Force on up to 32 queued pairs starting at ring position `head`.
-    auto flush = [&](uint32_t head, uint32_t n, uint32_t c0) {
-        if ((uint32_t)lane < n) {
-            const uint32_t ent = q[(head + lane) & (kQueue - 1)];
-            const uint32_t sl = ent >> 16;
-            const float4 tp = tgt[sl];
-            const float4 s = src[ent & 0xffffu];
-            const float dx = s.x - tp.x, dy = s.y - tp.y, dz = s.z - tp.z;
-            const float r2 = dist2(dx, dy, dz);
-            const float rinv = rsqrtf(r2);
-            const float r = r2 * rinv;
-            // bin = floor(asmthfac * r) without a conversion instruction: a
-            // round-toward-zero add of 2^23 leaves floor(x) in the mantissa
-            const float xt = p.asmthfac * r;
-            const float xf = __fadd_rz(xt, 8388608.0f);
-            int ti = __float_as_int(xf) - 0x4B000000;
-            const float frac = xt - (xf - 8388608.0f);
-            bool use = true;
-            if (frac < kEdge * xt || frac > 1.f - kEdge * xt || r2 > rc2_lo) {
+    float tx = 0.f, ty = 0.f, tz = 0.f;  // the current target, origin-relative
+
+    // Kernel parameters used per candidate, held in registers.
+    const float asmf = p.asmthfac, hh = p.h, hinv = p.hinv, h3inv = p.h3inv;
+    const double asmd = p.asmthfac_d;
+
+    // The pair law for one candidate.  The common case (inside the cut, away
+    // from a table-bin edge, outside the softening length) has no branch; the
+    // rare cases - a bin or cut edge decided in double, the spline inside h -
+    // share one branch.  A candidate beyond the cut gets a zero factor.
+    auto pair = [&](float4 s, float &ax, float &ay, float &az) {
+        const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+        const float r2 = dist2(dx, dy, dz);
+        bool ok = r2 <= rc2_hi && r2 != 0.f;
+        const float rinv = rsqrtf(ok ? r2 : 1.f);
+        const float r = r2 * rinv;
+        // bin = floor(asmthfac * r) without a conversion instruction: a
+        // round-toward-zero add of 2^23 leaves floor(x) in the mantissa
+        const float xt = asmf * r;
+        const float xf = __fadd_rz(xt, 8388608.0f);
+        int ti = __float_as_int(xf) - 0x4B000000;
+        const float frac = xt - (xf - 8388608.0f);
+        float fac = rinv * rinv * rinv;
+        const bool edge = fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f) || r2 > rc2_lo;
+        if (ok && (edge || r < hh)) {
+            if (edge) {
+                // decided in double as the reference's CPU path computes it
                 const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
-                use = dd <= rcut2_d;
-                ti = (int)(p.asmthfac_d * sqrt(dd));
+                ok = dd <= rcut2_d;
+                ti = (int)(asmd * sqrt(dd));
             }
-            if (use && ti < kNTab) {
-                float fac;
-                if (r >= p.h) {
-                    fac = rinv * rinv * rinv;
-                } else {
-                    const float u = r * p.hinv;
-                    if (u < 0.5f)
-                        fac = p.h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
-                    else
-                        fac = p.h3inv * (21.33333f - 48.0f * u + 38.4f * u * u -
-                                         10.66667f * u * u * u - 0.06667f / (u * u * u));
-                }
-                fac *= tab[ti];
-                atomicAdd(&accs[sl].x, dx * fac);
-                atomicAdd(&accs[sl].y, dy * fac);
-                atomicAdd(&accs[sl].z, dz * fac);
-                if (COUNT) ++npairs;
+            if (r < hh) {
+                const float u = r * hinv;
+                if (u < 0.5f)
+                    fac = h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
+                else
+                    fac = h3inv * (21.33333f - 48.0f * u + 38.4f * u * u - 10.66667f * u * u * u -
+                                   0.06667f / (u * u * u));
             }
         }
-        (void)c0;
+        fac = ok ? fac * tab[min(ti, kNTab - 1)] : 0.f;
+        ax = __fmaf_rn(dx, fac, ax);
+        ay = __fmaf_rn(dy, fac, ay);
+        az = __fmaf_rn(dz, fac, az);
+        if (COUNT) npairs += ok;
     };
 
     for (uint32_t tb = 0; tb < nt; tb += tpc) {
-        const uint32_t t = tb + slot;
+        const uint32_t t = tb + tid / tpt;
         const bool active = t < nt;
         const float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float tx = pt.x - ox, ty = pt.y - oy, tz = pt.z - oz;
-        if (sub == 0) {
-            tgt[slot] = make_float4(tx, ty, tz, 0.f);
-            accs[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        __syncthreads();
+        tx = pt.x - ox;
+        ty = pt.y - oy;
+        tz = pt.z - oz;
+        // two accumulator sets: the unrolled candidate pairs are independent
+        float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
             if (!(single_chunk && staged)) {
@@ -326,74 +324,57 @@ __global__ void __launch_bounds__(kThreads)
                 __syncthreads();
                 staged = true;
             }
-            // candidate generation: lane sub of a target takes columns sub, sub+tpt, ...
-            int col = sub - tpt;
-            uint32_t j = 0, e = 0;
-            bool done = !active;
-            uint32_t head = 0, tail = 0;
-            while (true) {
-                while (!done && j >= e) {
-                    col += tpt;
-                    if (col >= ncols) {
-                        done = true;
-                        break;
-                    }
-                    const float x0 = (ix + cs.dx[col]) * w, y0 = (iy + cs.dy[col]) * w;
-                    const float ddx = fmaxf(fmaxf(x0 - pt.x, pt.x - (x0 + w)), 0.f);
-                    const float ddy = fmaxf(fmaxf(y0 - pt.y, pt.y - (y0 + w)), 0.f);
-                    const float d2 = ddx * ddx + ddy * ddy;
-                    if (d2 > rc2m) continue;
-                    const float hz = sqrtf(rc2m - d2);
-                    int zlo = (int)floorf((pt.z - hz) * winv - zbase);
-                    int zhi = (int)floorf((pt.z + hz) * winv - zbase);
-                    zlo = max(zlo, 0);
-                    zhi = min(zhi, nz - 1);
-                    if (zlo > zhi) continue;
-                    j = max(coff[col * zst + zlo], c0);
-                    e = min(coff[col * zst + zhi + 1], c1);
+            if (!active) continue;
+            for (int col = 0; col < ncols; ++col) {
+                const float x0 = (ix + cs.dx[col]) * w, y0 = (iy + cs.dy[col]) * w;
+                const float ddx = fmaxf(fmaxf(x0 - pt.x, pt.x - (x0 + w)), 0.f);
+                const float ddy = fmaxf(fmaxf(y0 - pt.y, pt.y - (y0 + w)), 0.f);
+                const float d2 = ddx * ddx + ddy * ddy;
+                if (d2 > rc2m) continue;
+                const float hz = sqrtf(rc2m - d2);
+                const int zlo = max((int)floorf((pt.z - hz) * winv - zbase), 0);
+                const int zhi = min((int)floorf((pt.z + hz) * winv - zbase), nz - 1);
+                if (zlo > zhi) continue;
+                const uint32_t b = max(coff[col * zst + zlo], c0);
+                const uint32_t e = min(coff[col * zst + zhi + 1], c1);
+                uint32_t j = b + sub;
+                for (; j + 3 * tpt < e; j += 4 * tpt) {
+                    const float4 s0 = src[j - c0];
+                    const float4 s1 = src[j + tpt - c0];
+                    const float4 s2 = src[j + 2 * tpt - c0];
+                    const float4 s3 = src[j + 3 * tpt - c0];
+                    pair(s0, ax, ay, az);
+                    pair(s1, bx, by, bz);
+                    pair(s2, ax, ay, az);
+                    pair(s3, bx, by, bz);
                 }
-                const bool have = !done;
-                if (!__any_sync(kFull, have)) break;
-                bool take = false;
-                const uint32_t jj = j;
-                if (have) {
-                    const float4 s = src[j - c0];
-                    const float r2 = dist2(s.x - tx, s.y - ty, s.z - tz);
-                    take = r2 <= rc2_hi && r2 != 0.f;
-                    ++j;
-                }
-                const uint32_t m = __ballot_sync(kFull, take);
-                if (take) q[(tail + __popc(m & lt)) & (kQueue - 1)] = ((uint32_t)slot << 16) | (jj - c0);
-                tail += __popc(m);
-                if (tail - head >= 32) {
-                    __syncwarp();
-                    flush(head, 32, c0);
-                    head += 32;
-                    __syncwarp();
-                }
+                for (; j < e; j += tpt) pair(src[j - c0], ax, ay, az);
             }
-            __syncwarp();
-            if (tail != head) flush(head, tail - head, c0);
-            __syncwarp();
         }
+        ax += bx;
+        ay += by;
+        az += bz;
         if (COUNT) {
             uint32_t wsum = npairs;
             for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
             if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
             npairs = 0;
         }
-        __syncthreads();  // every warp's pairs for this pass are in accs
+        for (int off = tpt >> 1; off > 0; off >>= 1) {
+            ax += __shfl_xor_sync(kFull, ax, off);
+            ay += __shfl_xor_sync(kFull, ay, off);
+            az += __shfl_xor_sync(kFull, az, off);
+        }
         if (active && sub == 0) {
             const uint32_t i = t_begin + t;
             const uint32_t o = perm[i];
             const float mg = p.mass * p.G;
-            const float4 acc = accs[slot];
-            const float4 a = make_float4(acc.x * mg, acc.y * mg, acc.z * mg, 0.f);
+            const float4 a = make_float4(ax * mg, ay * mg, az * mg, 0.f);
             acc_out[o] = a;
-            float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 gpm = make_float4(0.f, 0.f, 0.f, 0.f);
             if (kick.acc_pm_s) {
-                g = kick.acc_pm_s[i];
-                if (kick.acc_pm_out) kick.acc_pm_out[o] = g;
+                gpm = kick.acc_pm_s[i];
+                if (kick.acc_pm_out) kick.acc_pm_out[o] = gpm;
             }
             if (KICK) {
                 float4 v = kick.vel[o];
@@ -404,9 +385,9 @@ __global__ void __launch_bounds__(kThreads)
                 v.y += __fmul_rn(a.y, kp);
                 v.z += __fmul_rn(a.z, kp);
                 if (kick.acc_pm_s) {
-                    v.x = __fmaf_rn(g.x, km, v.x);
-                    v.y = __fmaf_rn(g.y, km, v.y);
-                    v.z = __fmaf_rn(g.z, km, v.z);
+                    v.x = __fmaf_rn(gpm.x, km, v.x);
+                    v.y = __fmaf_rn(gpm.y, km, v.y);
+                    v.z = __fmaf_rn(gpm.z, km, v.z);
                 }
                 kick.vel[o] = v;
             }
@@ -422,8 +403,10 @@ bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
     int R = (int)ceil(rc / w);
     if (R > kMaxR) return false;
     if (2.0 * p.rcut >= p.boxsize) return false;
+    // segment length: a power of two dividing G, with the S + 2R z-cells of a
+    // column at most G (so a column's z range wraps at most once)
     int S = kMaxSeg;
-    while (S > 1 && p.grid % S) S >>= 1;
+    while (S > 1 && (p.grid % S || p.grid < S + 2 * R)) S >>= 1;
     if (p.grid < S + 2 * R) return false;
     cs->R = R;
     cs->S = S;

@@ -75,39 +75,32 @@ __global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist,
     constexpr int RADIX = 1 << RB;
     __shared__ uint32_t total[RADIX];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // Warp per digit; lane l owns tiles [l*per, l*per+per): a local sum with
-    // 8 loads in flight, a warp scan of the lane sums, then the local prefix.
-    const uint32_t per = (tiles + 31) / 32;
+    // Warp per digit, 32 consecutive tiles per round with 8 rounds of
+    // coalesced loads in flight, then 8 warp scans chained by the carry.
     for (int d = warp; d < RADIX; d += 32) {
         uint32_t *h = hist + (size_t)d * tiles;
-        const uint32_t t0 = min(lane * per, tiles), t1 = min(t0 + per, tiles);
-        uint32_t s = 0;
-        for (uint32_t t = t0; t < t1; t += 8) {
+        uint32_t carry = 0;
+        for (uint32_t t0 = 0; t0 < tiles; t0 += 32 * 8) {
             uint32_t v[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = t + u < t1 ? h[t + u] : 0u;
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t t = t0 + u * 32 + lane;
+                v[u] = t < tiles ? h[t] : 0u;
+            }
 #pragma unroll
-            for (int u = 0; u < 8; ++u) s += v[u];
-        }
-        uint32_t incl = s;
+            for (int u = 0; u < 8; ++u) {
+                uint32_t incl = v[u];
 #pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            uint32_t y = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += y;
-        }
-        uint32_t run = incl - s;
-        for (uint32_t t = t0; t < t1; t += 8) {
-            uint32_t v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = t + u < t1 ? h[t + u] : 0u;
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (t + u < t1) {
-                    h[t + u] = run;
-                    run += v[u];
+                for (int off = 1; off < 32; off <<= 1) {
+                    uint32_t y = __shfl_up_sync(kFull, incl, off);
+                    if (lane >= off) incl += y;
                 }
+                const uint32_t t = t0 + u * 32 + lane;
+                if (t < tiles) h[t] = carry + incl - v[u];
+                carry += __shfl_sync(kFull, incl, 31);
+            }
         }
-        if (lane == 31) total[d] = incl;
+        if (lane == 0) total[d] = carry;
     }
     __syncthreads();
     if (warp == 0) {
