@@ -16,19 +16,18 @@
 //     particles (two when the z range wraps); warps copy the runs into shared
 //     memory relative to an integer origin at the segment corner, with the
 //     periodic image shift applied once per run;
-//   * each target has one lane, or a power-of-two group of lanes when the
-//     segment is sparse; its lanes cull columns by the target's xy distance,
-//     narrow each column to the z-cells within sqrt(rcut^2 - d_xy^2), and walk
-//     those sources (lane k of the group takes every tpt-th one, so the group
-//     reads consecutive staged sources);
+//   * one target per warp: lane k culls column k by the target's xy distance
+//     and narrows it to the z-cells within sqrt(rcut^2 - d_xy^2) (each column
+//     is culled once, not once per lane); a ballot lists the non-empty
+//     columns, and all 32 lanes walk each range together on consecutive
+//     staged sources (conflict-free shared-memory reads, no lanes idling on
+//     ranges of different length);
 //   * the pair law runs without branches on the common path (a candidate
-//     beyond the cut gets a zero factor), two candidates per iteration into
-//     two accumulator sets for instruction-level parallelism.  Lanes of a warp
-//     hold different targets, so any per-candidate branch would be taken by
-//     some lane and cost the whole warp anyway;
+//     beyond the cut gets a zero factor), two candidates per lane per
+//     iteration into two accumulator sets for instruction-level parallelism;
 //   * 256-thread CTAs over 8-cell segments keep 8+ warps per scheduler on the
 //     shared memory a segment needs;
-//   * the lanes of a target add their partial sums with xor shuffles;
+//   * the warp adds its lanes' partial sums with xor shuffles;
 //   * the epilogue scatters the force to original particle order and, in the
 //     engine's step, kicks the velocity (timestep.c:56-59,86-91).
 //
@@ -70,14 +69,18 @@ struct Run {
     float sx, sy, sz;
 };
 
-// Dynamic shared memory, in order: staged sources, split table,
-// per-(column, z-cell) staged offsets, cell starts and counts, column runs,
-// column totals.
+// Dynamic shared memory, in order: staged sources and one sentinel source,
+// split table, column xy bounds, per-(column, z-cell) staged offsets, cell
+// starts and counts, column runs, column totals.
 __host__ __device__ inline size_t smem_bytes(int ncols, int nz) {
-    return sizeof(float4) * kMaxStage + sizeof(float) * kNTab + sizeof(uint32_t) * (size_t)ncols * (nz + 1) +
-           2 * sizeof(uint32_t) * (size_t)ncols * nz + sizeof(Run) * 2 * (size_t)ncols +
-           sizeof(uint32_t) * (size_t)ncols;
+    return sizeof(float4) * (kMaxStage + 1) + sizeof(float) * kNTab + sizeof(float4) * (size_t)ncols +
+           sizeof(uint32_t) * (size_t)ncols * (nz + 1) + 2 * sizeof(uint32_t) * (size_t)ncols * nz +
+           sizeof(Run) * 2 * (size_t)ncols + sizeof(uint32_t) * (size_t)ncols;
 }
+
+// A staged source this far away is beyond any cut: list positions past the
+// end of a target's candidates read it instead of branching.
+constexpr float kSentinel = 1e15f;
 
 template <CellFormat FMT>
 __device__ __forceinline__ void cell_range(const uint32_t *__restrict__ a,
@@ -114,13 +117,15 @@ __global__ void __launch_bounds__(kThreads, 4)
                  unsigned long long *__restrict__ pair_counter) {
     extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
+    __shared__ uint32_t s_wdelta[kWarps][32];
 
     const int G = p.grid;
     const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
     const int zst = nz + 1;  // coff stride per column
     float4 *src = smem_f4;
-    float *tab = reinterpret_cast<float *>(src + kMaxStage);
-    uint32_t *coff = reinterpret_cast<uint32_t *>(tab + kNTab);
+    float *tab = reinterpret_cast<float *>(src + kMaxStage + 1);
+    float4 *cgeo = reinterpret_cast<float4 *>(tab + kNTab);  // x0, x1, y0, y1 (16-B aligned: 4000 = 250 * 16)
+    uint32_t *coff = reinterpret_cast<uint32_t *>(cgeo + ncols);
     uint32_t *cst = coff + ncols * zst;
     uint32_t *ccn = cst + ncols * nz;
     Run *runs = reinterpret_cast<Run *>(ccn + ncols * nz);
@@ -170,10 +175,13 @@ __global__ void __launch_bounds__(kThreads, 4)
     if (t_begin == t_end) return;
 
     for (int i = tid; i < kNTab; i += kThreads) tab[i] = table_g[i];
+    if (tid == 0) src[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
 
     // per column: staged offsets of its z-cells, runs of consecutive cells with one shift
     for (int col = tid; col < ncols; col += kThreads) {
         int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
+        const float x0 = cxu * p.cellw, y0 = cyu * p.cellw;
+        cgeo[col] = make_float4(x0, x0 + p.cellw, y0, y0 + p.cellw);
         float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
         float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
         uint32_t acc = 0;
@@ -226,14 +234,7 @@ __global__ void __launch_bounds__(kThreads, 4)
     const uint32_t total = s_total;
     const bool single_chunk = total <= (uint32_t)kMaxStage;
 
-    // lanes per target (a power of two): sparse segments give a target
-    // several lanes, which take interleaved sources of each of its ranges
     const uint32_t nt = t_end - t_begin;
-    int tpt = 1;
-    while (tpt < 32 && (uint32_t)(tpt * 2) * nt <= (uint32_t)kThreads) tpt *= 2;
-    const int tpc = kThreads / tpt;
-    const int sub = tid & (tpt - 1);
-
     const float w = p.cellw;
     const float rc2m = (p.rcut + cs.margin) * (p.rcut + cs.margin);
     const float zbase = (float)(iz0 - R);
@@ -245,46 +246,67 @@ __global__ void __launch_bounds__(kThreads, 4)
     const double rcut2_d = (double)p.rcut * (double)p.rcut;
     bool staged = false;
     uint32_t npairs = 0;
-
+    uint32_t *wdelta = s_wdelta[warp];
+    const uint32_t lt_mask = (1u << lane) - 1u, le_mask = lt_mask | (1u << lane);
     float tx = 0.f, ty = 0.f, tz = 0.f;  // the current target, origin-relative
 
     // Kernel parameters used per candidate, held in registers.
     const float asmf = p.asmthfac, hh = p.h, hinv = p.hinv, h3inv = p.h3inv;
     const double asmd = p.asmthfac_d;
 
-    // The pair law for one candidate.  The common case (inside the cut, away
-    // from a table-bin edge, outside the softening length) has no branch; the
-    // rare cases - a bin or cut edge decided in double, the spline inside h -
-    // share one branch.  A candidate beyond the cut gets a zero factor.
-    auto pair = [&](float4 s, float &ax, float &ay, float &az) {
+    // The pair law, in two parts.  pair_fast takes the common case - inside
+    // the cut, away from a table-bin edge and from the cut, outside the
+    // softening length - without a branch, and reports the rest (its
+    // contribution there is zero): a candidate whose bin or cut decision is
+    // made in double, the spline inside h, and the self pair (r = 0 < hmin).
+    // pair_slow applies the full law to those.  Both add into the same
+    // accumulators in the same order as a single law would.
+    const float hmin = fmaxf(hh, 1e-9f);  // r2 < 1e-20 always takes the full law
+    auto pair_fast = [&](float4 s, float &ax, float &ay, float &az) -> bool {
+        const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
+        const float r2 = dist2(dx, dy, dz);
+        const float rinv = rsqrtf(fmaxf(r2, 1e-20f));
+        const float r = r2 * rinv;
+        // bin = floor(asmthfac * r) without a conversion instruction: a
+        // round-toward-zero add of 2^23 leaves floor(x) in the mantissa (and a
+        // larger non-negative value for x >= 2^23, clamped below)
+        const float xt = asmf * r;
+        const float xf = __fadd_rz(xt, 8388608.0f);
+        const uint32_t ti = (uint32_t)(__float_as_int(xf) - 0x4B000000);
+        const float frac = xt - (xf - 8388608.0f);
+        const bool edge = fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f);
+        const bool fast = r2 <= rc2_lo && !edge && r >= hmin;
+        const float fac = fast ? rinv * rinv * rinv * tab[min(ti, (uint32_t)kNTab - 1u)] : 0.f;
+        ax = __fmaf_rn(dx, fac, ax);
+        ay = __fmaf_rn(dy, fac, ay);
+        az = __fmaf_rn(dz, fac, az);
+        if (COUNT) npairs += fast;
+        return r2 <= rc2_hi && !fast;
+    };
+    auto pair_slow = [&](float4 s, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
         bool ok = r2 <= rc2_hi && r2 != 0.f;
         const float rinv = rsqrtf(ok ? r2 : 1.f);
         const float r = r2 * rinv;
-        // bin = floor(asmthfac * r) without a conversion instruction: a
-        // round-toward-zero add of 2^23 leaves floor(x) in the mantissa
         const float xt = asmf * r;
         const float xf = __fadd_rz(xt, 8388608.0f);
         int ti = __float_as_int(xf) - 0x4B000000;
         const float frac = xt - (xf - 8388608.0f);
         float fac = rinv * rinv * rinv;
-        const bool edge = fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f) || r2 > rc2_lo;
-        if (ok && (edge || r < hh)) {
-            if (edge) {
-                // decided in double as the reference's CPU path computes it
-                const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
-                ok = dd <= rcut2_d;
-                ti = (int)(asmd * sqrt(dd));
-            }
-            if (r < hh) {
-                const float u = r * hinv;
-                if (u < 0.5f)
-                    fac = h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
-                else
-                    fac = h3inv * (21.33333f - 48.0f * u + 38.4f * u * u - 10.66667f * u * u * u -
-                                   0.06667f / (u * u * u));
-            }
+        if (fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f) || r2 > rc2_lo) {
+            // decided in double as the reference's CPU path computes it
+            const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
+            ok = ok && dd <= rcut2_d;
+            ti = (int)(asmd * sqrt(dd));
+        }
+        if (r < hh) {
+            const float u = r * hinv;
+            if (u < 0.5f)
+                fac = h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
+            else
+                fac = h3inv * (21.33333f - 48.0f * u + 38.4f * u * u - 10.66667f * u * u * u -
+                               0.06667f / (u * u * u));
         }
         fac = ok ? fac * tab[min(ti, kNTab - 1)] : 0.f;
         ax = __fmaf_rn(dx, fac, ax);
@@ -293,14 +315,16 @@ __global__ void __launch_bounds__(kThreads, 4)
         if (COUNT) npairs += ok;
     };
 
-    for (uint32_t tb = 0; tb < nt; tb += tpc) {
-        const uint32_t t = tb + tid / tpt;
-        const bool active = t < nt;
+    // One target per warp: lane k culls columns k, k+32, ...; the warp then
+    // walks each non-empty column range with all lanes on consecutive sources.
+    const uint32_t rounds = (nt + kWarps - 1) / kWarps;
+    for (uint32_t round = 0; round < rounds; ++round) {
+        const uint32_t t = round * kWarps + warp;
+        const bool active = t < nt;  // warp-uniform
         const float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         tx = pt.x - ox;
         ty = pt.y - oy;
         tz = pt.z - oz;
-        // two accumulator sets: the unrolled candidate pairs are independent
         float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
@@ -325,47 +349,92 @@ __global__ void __launch_bounds__(kThreads, 4)
                 staged = true;
             }
             if (!active) continue;
-            for (int col = 0; col < ncols; ++col) {
-                const float x0 = (ix + cs.dx[col]) * w, y0 = (iy + cs.dy[col]) * w;
-                const float ddx = fmaxf(fmaxf(x0 - pt.x, pt.x - (x0 + w)), 0.f);
-                const float ddy = fmaxf(fmaxf(y0 - pt.y, pt.y - (y0 + w)), 0.f);
-                const float d2 = ddx * ddx + ddy * ddy;
-                if (d2 > rc2m) continue;
-                const float hz = sqrtf(rc2m - d2);
-                const int zlo = max((int)floorf((pt.z - hz) * winv - zbase), 0);
-                const int zhi = min((int)floorf((pt.z + hz) * winv - zbase), nz - 1);
-                if (zlo > zhi) continue;
-                const uint32_t b = max(coff[col * zst + zlo], c0);
-                const uint32_t e = min(coff[col * zst + zhi + 1], c1);
-                uint32_t j = b + sub;
-                for (; j + 3 * tpt < e; j += 4 * tpt) {
-                    const float4 s0 = src[j - c0];
-                    const float4 s1 = src[j + tpt - c0];
-                    const float4 s2 = src[j + 2 * tpt - c0];
-                    const float4 s3 = src[j + 3 * tpt - c0];
-                    pair(s0, ax, ay, az);
-                    pair(s1, bx, by, bz);
-                    pair(s2, ax, ay, az);
-                    pair(s3, bx, by, bz);
+            for (int cb = 0; cb < ncols; cb += 32) {
+                const int col = cb + lane;
+                uint32_t b = 0, e = 0;
+                if (col < ncols) {
+                    const float4 g = cgeo[col];
+                    const float ddx = fmaxf(fmaxf(g.x - pt.x, pt.x - g.y), 0.f);
+                    const float ddy = fmaxf(fmaxf(g.z - pt.y, pt.y - g.w), 0.f);
+                    const float q = rc2m - (ddx * ddx + ddy * ddy);
+                    if (q >= 0.f) {
+                        // half-height of the cut disc over this column (an
+                        // approximate square root: the margin covers it)
+                        const float hz = q * rsqrtf(fmaxf(q, 1e-30f));
+                        const int zlo = max(__float2int_rd(__fmaf_rn(pt.z - hz, winv, -zbase)), 0);
+                        const int zhi = min(__float2int_rd(__fmaf_rn(pt.z + hz, winv, -zbase)), nz - 1);
+                        if (zlo <= zhi) {
+                            b = max(coff[col * zst + zlo], c0);
+                            e = min(coff[col * zst + zhi + 1], c1);
+                        }
+                    }
                 }
-                for (; j < e; j += tpt) pair(src[j - c0], ax, ay, az);
+                // The column ranges, concatenated, form one candidate list of
+                // length T; ps is this lane's column start in it.
+                const uint32_t len = b < e ? e - b : 0u;
+                uint32_t ps = len;
+#pragma unroll
+                for (int off = 1; off < 32; off <<= 1) {
+                    const uint32_t v = __shfl_up_sync(kFull, ps, off);
+                    if (lane >= off) ps += v;
+                }
+                const uint32_t T = __shfl_sync(kFull, ps, 31);
+                ps -= len;
+                if (T == 0) continue;
+                // the k-th non-empty column's shift from list to staged index
+                const uint32_t nonempty = __ballot_sync(kFull, len > 0);
+                if (len > 0) wdelta[__popc(nonempty & lt_mask)] = b - c0 - ps;
+                if (len == 0) ps = 0xffffffffu;  // marks no start
+                __syncwarp();
+                // Each window of 64 candidates: one bit per column start, so a
+                // lane's column is (columns started before the window) +
+                // (starts at or below its position) - 1.  Positions at or past
+                // T read the sentinel.  The rare-case law runs under a
+                // warp-uniform branch.
+                uint32_t before = 0, base = 0;
+                for (; base + 32u < T; base += 64) {
+                    const uint32_t r0 = ps - base, r1 = r0 - 32u;
+                    const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
+                    const uint32_t m1 = __reduce_or_sync(kFull, r1 < 32u ? 1u << r1 : 0u);
+                    const uint32_t n0 = before + __popc(m0);
+                    const uint32_t k0 = base + lane, k1 = k0 + 32;
+                    const uint32_t i0 = k0 + wdelta[before + __popc(m0 & le_mask) - 1];
+                    const uint32_t d1 = wdelta[n0 + __popc(m1 & le_mask) - 1];
+                    const uint32_t i1 = k1 < T ? k1 + d1 : (uint32_t)kMaxStage;
+                    const float4 s0 = src[i0], s1 = src[i1];
+                    const bool x0 = pair_fast(s0, ax, ay, az);
+                    const bool x1 = pair_fast(s1, bx, by, bz);
+                    if (__any_sync(kFull, x0 || x1)) {
+                        if (x0) pair_slow(s0, ax, ay, az);
+                        if (x1) pair_slow(s1, bx, by, bz);
+                    }
+                    before = n0 + __popc(m1);
+                }
+                if (base < T) {
+                    const uint32_t r0 = ps - base;
+                    const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
+                    const uint32_t k0 = base + lane;
+                    const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
+                    const float4 s0 = src[k0 < T ? k0 + d0 : (uint32_t)kMaxStage];
+                    const bool x0 = pair_fast(s0, ax, ay, az);
+                    if (__any_sync(kFull, x0)) {
+                        if (x0) pair_slow(s0, ax, ay, az);
+                    }
+                }
+                __syncwarp();
             }
         }
+        if (!active) continue;
         ax += bx;
         ay += by;
         az += bz;
-        if (COUNT) {
-            uint32_t wsum = npairs;
-            for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
-            if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
-            npairs = 0;
-        }
-        for (int off = tpt >> 1; off > 0; off >>= 1) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
             ax += __shfl_xor_sync(kFull, ax, off);
             ay += __shfl_xor_sync(kFull, ay, off);
             az += __shfl_xor_sync(kFull, az, off);
         }
-        if (active && sub == 0) {
+        if (lane == 0) {
             const uint32_t i = t_begin + t;
             const uint32_t o = perm[i];
             const float mg = p.mass * p.G;
@@ -392,6 +461,11 @@ __global__ void __launch_bounds__(kThreads, 4)
                 kick.vel[o] = v;
             }
         }
+    }
+    if (COUNT) {
+        uint32_t wsum = npairs;
+        for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
+        if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
     }
 }
 
