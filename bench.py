@@ -338,9 +338,10 @@ def run_e2e(steps, ic, soft, device):
     lib.init_drift_table()
 
     def one_step():
-        # find_next_sync_point_and_drift (run.c:28-69) with no output times
-        t_end = ti.reshape(-1, 2)[:, 0]
-        min_glob = int(t_end.min())
+        # find_next_sync_point_and_drift (run.c:28-69) with no output times; the
+        # scan of P[].Ti_endstep (run.c:35-40) is the library's, which returns
+        # the minimum advance_and_find_timesteps computed on the device
+        min_glob = lib.cuco_dropin_min_ti_endstep()
         if min_glob >= al.PM_Ti_endstep:
             min_glob = al.PM_Ti_endstep
         lib.move_particles(al.Ti_Current, min_glob)
@@ -355,11 +356,18 @@ def run_e2e(steps, ic, soft, device):
     for _ in range(steps):
         one_step()
     dt = time.perf_counter() - t0
-    bytes_per_call = 60 * n
+    if lib.cuco_dropin_host_access():
+        # kernels stream whole 60-byte records of P[] over the host link:
+        # move_particles and advance_and_find_timesteps read and write each
+        # once; compute_accelerations reads twice (wrap, then the force write)
+        # and writes once (the wrap writes back only records that wrapped)
+        h2d, d2h, access = 4 * 60 * n, 3 * 60 * n, "kernels stream P[] records in place over the host link"
+    else:
+        h2d, d2h, access = 3 * 60 * n, 3 * 60 * n, "whole P[] copied in and out per call"
     return {"value": n * steps / dt, "unit": "particle-updates/s",
-            "h2d_bytes_per_step": 3 * bytes_per_call, "d2h_bytes_per_step": 3 * bytes_per_call,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": steps, "path": "drop-in run loop: move_particles + compute_accelerations + "
-                                    "advance_and_find_timesteps on host P[]"}
+                                    "advance_and_find_timesteps on host P[] (" + access + ")"}
 
 
 def main():

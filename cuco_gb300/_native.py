@@ -110,6 +110,8 @@ SIGNATURES = {
     "do_box_wrapping": (None, []),
     "advance_and_find_timesteps": (None, []),
     "get_timestep": (_I, [_I]),
+    "cuco_dropin_min_ti_endstep": (_I, []),
+    "cuco_dropin_host_access": (_I, []),
     "init_drift_table": (None, []),
     "drift_integ": (_D, [_D, _P]),
     "gravkick_integ": (_D, [_D, _P]),

@@ -2,9 +2,12 @@
 // working on its globals (allvars.h:120-142).
 //
 // The reference host program keeps P[] (array of PARTICLE) in host memory and
-// calls these functions from begrun()/run().  Each call mirrors P[] to the
-// device in one copy, runs the engine's kernels on the mirror, and copies it
-// back, so the host always sees the reference's fields updated in place:
+// calls these functions from begrun()/run().  Where the device reads and
+// writes pageable host memory coherently (a Grace host over NVLink-C2C), the
+// kernels of each call work on P[] in place and write back only the fields
+// the call changes; elsewhere each call copies P[] to a device mirror, runs
+// the same kernels on it, and copies it back.  Either way the host sees the
+// reference's fields updated in place when the call returns:
 //   pm_init_periodic / long_range_init   pm_periodic.c:25-43, longrange.c:8-12
 //   pmforce_periodic / long_range_force  pm_periodic.c:67-314, longrange.c:14-22
 //   set_softenings / linklist_init       gravlist.cpp:28-115
@@ -18,6 +21,7 @@
 // The globals themselves are defined weakly here so that the library loads on
 // its own (tests drive it through these symbols); a host program's own
 // allvars.c definitions take precedence.
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -80,6 +84,11 @@ struct DropinState {
     SOFTPARAM soft{};
     // short-range constants as gravlist.cpp keeps them
     double h = 0, h_inv = 0, h3_inv = 0;
+    int direct = -1;  // kernels work on the host P[] in place (1) or on dP (0)
+    int min_endstep = 0;  // min P[].Ti_endstep written by advance_and_find_timesteps
+    bool min_valid = false;
+    const void *min_P = nullptr;  // the P[] and NumPart it was taken over
+    unsigned min_n = 0;
 };
 
 DropinState &ds() {
@@ -100,66 +109,125 @@ int engine_grid() {
 }
 
 // ---------------------------------------------------------------- kernels
+//
+// Each drop-in call applies per-particle operations to P[].  An operation is a
+// functor `bool op(PARTICLE &q, uint32_t i, int &endstep)` that returns
+// whether it changed q.  It runs on the device mirror in place (k_apply) or on
+// the host's P[] through shared memory (k_apply_staged): a CTA reads its
+// contiguous run of records with coalesced 16-byte loads, applies the
+// operation, and writes the run back whole, with coalesced stores, if any
+// record changed.  The host link then carries full 16-byte words in both
+// directions at once instead of scattered 4-byte fields.
 
-__global__ void k_unpack_particles(const PARTICLE *__restrict__ p, float4 *__restrict__ pos,
-                                   float4 *__restrict__ vel, uint32_t n) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const PARTICLE &q = p[i];
-    pos[i] = make_float4(q.Pos[0], q.Pos[1], q.Pos[2], 0.f);
-    if (vel) vel[i] = make_float4(q.Vel[0], q.Vel[1], q.Vel[2], 0.f);
+constexpr int kRecThreads = 256;
+constexpr int kRecBytes = kRecThreads * (int)sizeof(PARTICLE);  // 15360 = 960 x 16
+static_assert(kRecBytes % 16 == 0, "a CTA's records are whole 16-byte words");
+
+// warp minimum of endstep into *min_end (INT_MAX: nothing to report)
+__device__ __forceinline__ void min_endstep(int endstep, int *min_end) {
+    const int m = __reduce_min_sync(0xffffffffu, endstep);
+    if (min_end && (threadIdx.x & 31) == 0 && m != INT_MAX) atomicMin(min_end, m);
 }
+
+template <class Op>
+__global__ void __launch_bounds__(kRecThreads) k_apply(PARTICLE *__restrict__ p, uint32_t n, Op op,
+                                                      int *__restrict__ min_end) {
+    const uint32_t i = blockIdx.x * kRecThreads + threadIdx.x;
+    int endstep = INT_MAX;
+    if (i < n) op(p[i], i, endstep);
+    min_endstep(endstep, min_end);
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kRecThreads) k_apply_staged(PARTICLE *__restrict__ p, uint32_t n, Op op,
+                                                             int *__restrict__ min_end) {
+    __shared__ uint4 buf[kRecBytes / 16];
+    __shared__ int changed;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t first = blockIdx.x * kRecThreads;
+    const uint32_t cnt = min(n - first, (uint32_t)kRecThreads);
+    const uint32_t bytes = cnt * (uint32_t)sizeof(PARTICLE);
+    const uint32_t words = bytes / 16, tail = (bytes % 16) / 4;  // whole words, then 4-byte words
+    // p is 16-byte aligned (checked by the caller) and first * 60 is a multiple of 16
+    uint4 *g = reinterpret_cast<uint4 *>(reinterpret_cast<char *>(p) + (size_t)first * sizeof(PARTICLE));
+    for (uint32_t w = tid; w < words; w += kRecThreads) buf[w] = g[w];
+    if (tid < tail) reinterpret_cast<uint32_t *>(buf + words)[tid] = reinterpret_cast<const uint32_t *>(g + words)[tid];
+    if (tid == 0) changed = 0;
+    __syncthreads();
+    int endstep = INT_MAX;
+    if (tid < cnt && op(reinterpret_cast<PARTICLE *>(buf)[tid], first + tid, endstep)) changed = 1;
+    __syncthreads();
+    if (changed) {
+        for (uint32_t w = tid; w < words; w += kRecThreads) g[w] = buf[w];
+        if (tid < tail) reinterpret_cast<uint32_t *>(g + words)[tid] = reinterpret_cast<const uint32_t *>(buf + words)[tid];
+    }
+    min_endstep(endstep, min_end);
+}
+
+// positions (and velocities) to the engine's float4 arrays
+struct UnpackOp {
+    float4 *pos, *vel;
+    __device__ bool operator()(PARTICLE &q, uint32_t i, int &) const {
+        pos[i] = make_float4(q.Pos[0], q.Pos[1], q.Pos[2], 0.f);
+        if (vel) vel[i] = make_float4(q.Vel[0], q.Vel[1], q.Vel[2], 0.f);
+        return false;
+    }
+};
 
 enum { kPackPos = 1, kPackVel = 2, kPackPP = 4, kPackPM = 8 };
 
-__global__ void k_pack_particles(PARTICLE *__restrict__ p, const float4 *__restrict__ pos,
-                                 const float4 *__restrict__ vel, const float4 *__restrict__ app,
-                                 const float4 *__restrict__ apm, uint32_t n, int what) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    PARTICLE &q = p[i];
-    if (what & kPackPos) {
-        float4 v = pos[i];
-        q.Pos[0] = v.x;
-        q.Pos[1] = v.y;
-        q.Pos[2] = v.z;
-    }
-    if (what & kPackVel) {
-        float4 v = vel[i];
-        q.Vel[0] = v.x;
-        q.Vel[1] = v.y;
-        q.Vel[2] = v.z;
-    }
-    if (what & kPackPP) {
-        float4 v = app[i];
-        q.GravAccel[0] = v.x;
-        q.GravAccel[1] = v.y;
-        q.GravAccel[2] = v.z;
-    }
-    if (what & kPackPM) {
-        float4 v = apm[i];
-        q.GravPM[0] = v.x;
-        q.GravPM[1] = v.y;
-        q.GravPM[2] = v.z;
-    }
-}
-
-// predict.c:10-41 on the mirror: drift (no wrap) and/or wrap
-__global__ void k_drift_wrap(PARTICLE *__restrict__ p, uint32_t n, double dt, int drift, int wrap,
-                             double boxsize) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    PARTICLE &q = p[i];
-    for (int j = 0; j < 3; ++j) {
-        float x = q.Pos[j];
-        if (drift) x = (float)((double)x + (double)q.Vel[j] * dt);
-        if (wrap) {
-            for (int it = 0; it < 64 && x < 0; ++it) x = (float)((double)x + boxsize);
-            for (int it = 0; it < 64 && x >= (float)boxsize; ++it) x = (float)((double)x - boxsize);
+// engine results into the particle's fields
+struct PackOp {
+    const float4 *pos, *vel, *app, *apm;
+    int what;
+    __device__ bool operator()(PARTICLE &q, uint32_t i, int &) const {
+        if (what & kPackPos) {
+            const float4 v = pos[i];
+            q.Pos[0] = v.x, q.Pos[1] = v.y, q.Pos[2] = v.z;
         }
-        q.Pos[j] = x;
+        if (what & kPackVel) {
+            const float4 v = vel[i];
+            q.Vel[0] = v.x, q.Vel[1] = v.y, q.Vel[2] = v.z;
+        }
+        if (what & kPackPP) {
+            const float4 v = app[i];
+            q.GravAccel[0] = v.x, q.GravAccel[1] = v.y, q.GravAccel[2] = v.z;
+        }
+        if (what & kPackPM) {
+            const float4 v = apm[i];
+            q.GravPM[0] = v.x, q.GravPM[1] = v.y, q.GravPM[2] = v.z;
+        }
+        return what != 0;
     }
-}
+};
+
+// predict.c:10-41: drift (no wrap) and/or wrap; optionally the resulting
+// positions to the engine
+struct DriftWrapOp {
+    double dt, boxsize;
+    int drift, wrap;
+    float4 *pos_out;
+    __device__ bool operator()(PARTICLE &q, uint32_t i, int &) const {
+        float out[3];
+        bool ch = false;
+        for (int j = 0; j < 3; ++j) {
+            const float x0 = q.Pos[j];
+            float x = x0;
+            if (drift) x = (float)((double)x + (double)q.Vel[j] * dt);
+            if (wrap) {
+                for (int it = 0; it < 64 && x < 0; ++it) x = (float)((double)x + boxsize);
+                for (int it = 0; it < 64 && x >= (float)boxsize; ++it) x = (float)((double)x - boxsize);
+            }
+            if (__float_as_uint(x) != __float_as_uint(x0)) {
+                q.Pos[j] = x;
+                ch = true;
+            }
+            out[j] = x;
+        }
+        if (pos_out) pos_out[i] = make_float4(out[0], out[1], out[2], 0.f);
+        return ch;
+    }
+};
 
 struct TimestepArgs {
     double fac1, atime, hubble_a, dt_displacement;
@@ -183,54 +251,72 @@ __device__ double table_factor(const double *T, double loga0, double loga1, doub
     return df2 - df1;
 }
 
-// timestep.c:26-61 and 86-91 per particle
-__global__ void k_timesteps(PARTICLE *__restrict__ p, uint32_t n, TimestepArgs a,
-                            const double *__restrict__ kick_table, int *__restrict__ flag) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    PARTICLE &q = p[i];
-    const int TIMEBASE = CUCO_TIMEBASE;
-    if (q.Ti_endstep == a.ti_current) {
-        // get_timestep (timestep.c:96-138)
-        double ax = a.fac1 * q.GravAccel[0], ay = a.fac1 * q.GravAccel[1], az = a.fac1 * q.GravAccel[2];
-        ax += a.fac1 * q.GravPM[0];
-        ay += a.fac1 * q.GravPM[1];
-        az += a.fac1 * q.GravPM[2];
-        double ac = sqrt(ax * ax + ay * ay + az * az);
-        if (ac == 0) ac = 1.0e-30;
-        double dt = sqrt(2 * a.errtol * a.atime * a.softening_table / ac);
-        dt *= a.hubble_a;
-        if (dt >= a.dt_displacement) dt = a.dt_displacement;
-        if (dt < a.min_timestep) dt = a.min_timestep;
-        int ti_step = (int)(dt / a.timebase_interval);
-        if (!(ti_step > 0 && ti_step < TIMEBASE)) {
-            if (atomicCAS(&flag[0], 0, 1) == 0) {
-                flag[1] = (int)i;
-                flag[2] = ti_step;
+// timestep.c:26-61 and 86-91 per particle; endstep = Ti_endstep after the
+// update, for the scan of find_next_sync_point_and_drift (run.c:35-40).
+struct TimestepOp {
+    TimestepArgs a;
+    const double *kick_table;
+    int *flag;  // [0] error, [1] particle, [2] its ti_step
+    __device__ bool operator()(PARTICLE &q, uint32_t i, int &endstep) const {
+        const int TIMEBASE = CUCO_TIMEBASE;
+        int beg = q.Ti_begstep, end = q.Ti_endstep;
+        bool bad = false, kicked = false, stepped = false;
+        float vel[3] = {q.Vel[0], q.Vel[1], q.Vel[2]};
+        if (end == a.ti_current) {
+            // get_timestep (timestep.c:96-138)
+            double ax = a.fac1 * q.GravAccel[0], ay = a.fac1 * q.GravAccel[1], az = a.fac1 * q.GravAccel[2];
+            ax += a.fac1 * q.GravPM[0];
+            ay += a.fac1 * q.GravPM[1];
+            az += a.fac1 * q.GravPM[2];
+            double ac = sqrt(ax * ax + ay * ay + az * az);
+            if (ac == 0) ac = 1.0e-30;
+            double dt = sqrt(2 * a.errtol * a.atime * a.softening_table / ac);
+            dt *= a.hubble_a;
+            if (dt >= a.dt_displacement) dt = a.dt_displacement;
+            if (dt < a.min_timestep) dt = a.min_timestep;
+            int ti_step = (int)(dt / a.timebase_interval);
+            if (!(ti_step > 0 && ti_step < TIMEBASE)) {
+                if (atomicCAS(&flag[0], 0, 1) == 0) {
+                    flag[1] = (int)i;
+                    flag[2] = ti_step;
+                }
+                bad = true;
+            } else {
+                int ti_min = TIMEBASE;
+                while (ti_min > ti_step) ti_min >>= 1;
+                ti_step = ti_min;
+                if (ti_step > (end - beg)) {
+                    if (((TIMEBASE - end) % ti_step) > 0) ti_step = end - beg;
+                }
+                if (a.ti_current == TIMEBASE) ti_step = 0;
+                if ((TIMEBASE - a.ti_current) < ti_step) ti_step = TIMEBASE - a.ti_current;
+                const int tstart = (beg + end) / 2;
+                const int tend = end + ti_step / 2;
+                const double dt_gravkick =
+                    table_factor(kick_table, a.loga0, a.loga1, a.timebase_interval, tstart, tend);
+                beg = end;
+                end = beg + ti_step;
+                stepped = true;
+                for (int j = 0; j < 3; ++j) vel[j] += (float)(q.GravAccel[j] * dt_gravkick);
+                kicked = true;
             }
-            return;
         }
-        int ti_min = TIMEBASE;
-        while (ti_min > ti_step) ti_min >>= 1;
-        ti_step = ti_min;
-        if (ti_step > (q.Ti_endstep - q.Ti_begstep)) {
-            if (((TIMEBASE - q.Ti_endstep) % ti_step) > 0) ti_step = q.Ti_endstep - q.Ti_begstep;
+        if (!bad && a.pm_kick) {
+            for (int j = 0; j < 3; ++j) vel[j] = (float)((double)vel[j] + (double)q.GravPM[j] * a.pm_dt);
+            kicked = true;
         }
-        if (a.ti_current == TIMEBASE) ti_step = 0;
-        if ((TIMEBASE - a.ti_current) < ti_step) ti_step = TIMEBASE - a.ti_current;
-        int tstart = (q.Ti_begstep + q.Ti_endstep) / 2;
-        int tend = q.Ti_endstep + ti_step / 2;
-        double dt_gravkick = table_factor(kick_table, a.loga0, a.loga1, a.timebase_interval, tstart, tend);
-        q.Ti_begstep = q.Ti_endstep;
-        q.Ti_endstep = q.Ti_begstep + ti_step;
-        for (int j = 0; j < 3; ++j) {
-            float dv = (float)(q.GravAccel[j] * dt_gravkick);
-            q.Vel[j] += dv;
+        if (!bad) {
+            if (kicked)
+                for (int j = 0; j < 3; ++j) q.Vel[j] = vel[j];
+            if (stepped) {
+                q.Ti_begstep = beg;
+                q.Ti_endstep = end;
+            }
         }
+        endstep = end;
+        return !bad && (kicked || stepped);
     }
-    if (a.pm_kick)
-        for (int j = 0; j < 3; ++j) q.Vel[j] = (float)((double)q.Vel[j] + (double)q.GravPM[j] * a.pm_dt);
-}
+};
 
 // --------------------------------------------------------------- helpers
 
@@ -292,47 +378,70 @@ BoxView view() {
     return v;
 }
 
-void upload_P(bool with_vel) {
-    ensure_box();
+// Whether kernels may read and write the host's P[] in place.  That needs a
+// device that accesses pageable host memory coherently (Grace hosts over
+// NVLink-C2C, or HMM) and a 16-byte aligned P[] (what malloc returns).
+// CUCO_DROPIN_MIRROR=1 forces the mirror path (a full cudaMemcpy of P[] in and
+// out around each call) on such devices too.
+bool direct_access() {
     DropinState &s = ds();
-    BoxView v = view();
-    capi_check(cudaMemcpyAsync(s.dP, P, sizeof(PARTICLE) * NumPart, cudaMemcpyHostToDevice, v.stream),
-               "P[] upload");
-    if (NumPart)
-        k_unpack_particles<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((const PARTICLE *)s.dP, v.pos,
-                                                                        with_vel ? v.vel : nullptr, NumPart);
-    capi_check(cudaGetLastError(), "P[] unpack");
+    if (s.direct < 0) {
+        int dev = 0, attr = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&attr, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) attr = 0;
+        s.direct = attr == 1 ? 1 : 0;
+    }
+    const char *env = getenv("CUCO_DROPIN_MIRROR");
+    return s.direct == 1 && !(env && env[0] == '1') && ((uintptr_t)P & 15) == 0;
 }
 
-void download_P(int what) {
+// P[] as the kernels of one call see it: the host array itself, or the device
+// mirror after a copy of the current P[].
+PARTICLE *particles_in() {
+    ensure_box();
+    DropinState &s = ds();
+    if (direct_access()) return P;
+    capi_check(cudaMemcpyAsync(s.dP, P, sizeof(PARTICLE) * NumPart, cudaMemcpyHostToDevice, view().stream),
+               "P[] upload");
+    return (PARTICLE *)s.dP;
+}
+
+// Makes the kernels' writes to P[] visible to the host and waits for them.
+void particles_out(PARTICLE *pp) {
     DropinState &s = ds();
     BoxView v = view();
-    if (what && NumPart)
-        k_pack_particles<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((PARTICLE *)s.dP, v.pos, v.vel,
-                                                                      v.acc_pp, v.acc_pm, NumPart, what);
-    capi_check(cudaGetLastError(), "P[] pack");
-    capi_check(cudaMemcpyAsync(P, s.dP, sizeof(PARTICLE) * NumPart, cudaMemcpyDeviceToHost, v.stream),
-               "P[] download");
+    if (pp != P)
+        capi_check(cudaMemcpyAsync(P, s.dP, sizeof(PARTICLE) * NumPart, cudaMemcpyDeviceToHost, v.stream),
+                   "P[] download");
     capi_check(cudaStreamSynchronize(v.stream), "P[] download");
 }
 
-void mirror_drift_wrap(double dt, bool drift, bool wrap) {
-    DropinState &s = ds();
+template <class Op>
+void apply(PARTICLE *pp, const Op &op, const char *where, int *min_end = nullptr) {
+    if (!NumPart) return;
     BoxView v = view();
-    if (NumPart)
-        k_drift_wrap<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((PARTICLE *)s.dP, NumPart, dt,
-                                                                  drift ? 1 : 0, wrap ? 1 : 0,
-                                                                  (double)All.BoxSize);
-    capi_check(cudaGetLastError(), "drift/wrap");
+    const unsigned blocks = (NumPart + kRecThreads - 1) / kRecThreads;
+    if (pp == P)
+        k_apply_staged<<<blocks, kRecThreads, 0, v.stream>>>(pp, NumPart, op, min_end);
+    else
+        k_apply<<<blocks, kRecThreads, 0, v.stream>>>(pp, NumPart, op, min_end);
+    capi_check(cudaGetLastError(), where);
 }
 
-void mirror_to_box(bool with_vel) {
-    DropinState &s = ds();
+void unpack(PARTICLE *pp, bool with_vel) {
     BoxView v = view();
-    if (NumPart)
-        k_unpack_particles<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((const PARTICLE *)s.dP, v.pos,
-                                                                        with_vel ? v.vel : nullptr, NumPart);
-    capi_check(cudaGetLastError(), "P[] unpack");
+    apply(pp, UnpackOp{v.pos, with_vel ? v.vel : nullptr}, "P[] unpack");
+}
+
+void pack(PARTICLE *pp, int what) {
+    BoxView v = view();
+    apply(pp, PackOp{v.pos, v.vel, v.acc_pp, v.acc_pm, what}, "P[] pack");
+}
+
+void drift_wrap(PARTICLE *pp, double dt, bool drift, bool wrap, bool to_engine = false) {
+    BoxView v = view();
+    apply(pp, DriftWrapOp{dt, (double)All.BoxSize, drift ? 1 : 0, wrap ? 1 : 0, to_engine ? v.pos : nullptr},
+          "drift/wrap");
 }
 
 }  // namespace
@@ -362,10 +471,12 @@ void pm_init_periodic_allocate(void) { ensure_box(); }
 void pm_init_periodic_free(void) {}
 
 void pmforce_periodic(void) {
-    upload_P(false);
+    PARTICLE *pp = particles_in();
+    unpack(pp, false);
     cuco_box_mark_state(ds().box);
     capi_status(cuco_box_forces(ds().box, 1, 0), "pmforce_periodic");
-    download_P(kPackPM);
+    pack(pp, kPackPM);
+    particles_out(pp);
 }
 
 void long_range_force(void) { pmforce_periodic(); }
@@ -418,49 +529,48 @@ void linklist_init(void) {
 }
 
 void copyPosToDevice(void) {
-    upload_P(false);
+    unpack(particles_in(), false);
     capi_check(cudaStreamSynchronize(view().stream), "copyPosToDevice");
 }
 
 void copyAccelFromDevice(void) {
-    DropinState &s = ds();
-    ensure_box();
-    BoxView v = view();
-    capi_check(cudaMemcpyAsync(s.dP, P, sizeof(PARTICLE) * NumPart, cudaMemcpyHostToDevice, v.stream),
-               "copyAccelFromDevice");
-    download_P(kPackPP);
+    PARTICLE *pp = particles_in();
+    pack(pp, kPackPP);
+    particles_out(pp);
 }
 
 void gravity_linklist_cuda(void) {
     set_softenings();
-    upload_P(false);
+    PARTICLE *pp = particles_in();
+    unpack(pp, false);
     cuco_box_mark_state(ds().box);
     capi_status(cuco_box_forces(ds().box, 0, 1), "gravity_linklist_cuda");
-    download_P(kPackPP);
+    pack(pp, kPackPP);
+    particles_out(pp);
 }
 
 void do_box_wrapping(void) {
-    upload_P(false);
-    mirror_drift_wrap(0.0, false, true);
-    download_P(0);
+    PARTICLE *pp = particles_in();
+    drift_wrap(pp, 0.0, false, true);
+    particles_out(pp);
 }
 
 void move_particles(int time0, int time1) {
     double dt = get_drift_factor(time0, time1);
-    upload_P(false);
-    mirror_drift_wrap(dt, true, false);
-    download_P(0);
+    PARTICLE *pp = particles_in();
+    drift_wrap(pp, dt, true, false);
+    particles_out(pp);
 }
 
 void compute_accelerations(void) {
     set_softenings();
-    upload_P(false);
-    mirror_drift_wrap(0.0, false, true);
-    mirror_to_box(false);
+    PARTICLE *pp = particles_in();
+    drift_wrap(pp, 0.0, false, true, true);  // wrap, and the positions to the engine
     cuco_box_mark_state(ds().box);
     int pm = All.PM_Ti_endstep == All.Ti_Current;
     capi_status(cuco_box_forces(ds().box, pm, 1), "compute_accelerations");
-    download_P(kPackPos | kPackPP | (pm ? kPackPM : 0));
+    pack(pp, kPackPP | (pm ? kPackPM : 0));
+    particles_out(pp);
 }
 
 int get_timestep(int p) {
@@ -500,7 +610,7 @@ void advance_and_find_timesteps(void) {
         capi_check(cudaMemcpy(s.dtab, s.kick64, bytes, cudaMemcpyHostToDevice), "advance_and_find_timesteps");
         s.dtab_valid = true;
     }
-    upload_P(false);
+    PARTICLE *pp = particles_in();
     BoxView v = view();
     TimestepArgs a;
     a.fac1 = 1 / (All.Time * All.Time);
@@ -534,13 +644,16 @@ void advance_and_find_timesteps(void) {
         All.PM_Ti_begstep = All.PM_Ti_endstep;
         All.PM_Ti_endstep = All.PM_Ti_begstep + ti_step;
     }
-    capi_check(cudaMemsetAsync(s.dflag, 0, sizeof(int) * 4, v.stream), "timesteps");
-    if (NumPart)
-        k_timesteps<<<(NumPart + 255) / 256, 256, 0, v.stream>>>((PARTICLE *)s.dP, NumPart, a, s.dtab, s.dflag);
-    capi_check(cudaGetLastError(), "advance_and_find_timesteps");
+    capi_check(cudaMemsetAsync(s.dflag, 0, sizeof(int) * 3, v.stream), "timesteps");
+    capi_check(cudaMemsetAsync(s.dflag + 3, 0x7f, sizeof(int), v.stream), "timesteps");
+    apply(pp, TimestepOp{a, s.dtab, s.dflag}, "advance_and_find_timesteps", s.dflag + 3);
     int flag[4];
     capi_check(cudaMemcpyAsync(flag, s.dflag, sizeof(flag), cudaMemcpyDeviceToHost, v.stream), "timesteps");
-    download_P(0);
+    particles_out(pp);
+    s.min_endstep = flag[3];
+    s.min_valid = NumPart > 0 && !flag[0];
+    s.min_P = P;
+    s.min_n = NumPart;
     if (flag[0]) {
         printf("Error: a timestep of size zero was assigned on the integer timeline!\n");
         printf("ti_step: %d\n", flag[2]);
@@ -548,6 +661,21 @@ void advance_and_find_timesteps(void) {
         printf("particle: %d\n", flag[1]);
         exit(1);
     }
+}
+
+int cuco_dropin_host_access(void) {
+    ensure_box();
+    return direct_access() ? 1 : 0;
+}
+
+int cuco_dropin_min_ti_endstep(void) {
+    DropinState &s = ds();
+    if (s.min_valid && s.min_P == P && s.min_n == NumPart) return s.min_endstep;
+    // the host scan of find_next_sync_point_and_drift (run.c:35-40)
+    int m = NumPart ? P[0].Ti_endstep : 0;
+    for (unsigned i = 1; i < NumPart; ++i)
+        if (P[i].Ti_endstep < m) m = P[i].Ti_endstep;
+    return m;
 }
 
 double drift_integ(double a, void *param) {

@@ -137,6 +137,19 @@ void do_box_wrapping(void);
 void advance_and_find_timesteps(void);
 /* timestep.c:96-138 */
 int get_timestep(int p);
+/* No counterpart in the reference.  min over P[i].Ti_endstep: the scan that
+ * find_next_sync_point_and_drift does on the host (run.c:35-40).  Right after
+ * advance_and_find_timesteps it returns the minimum that call computed on the
+ * device, without reading P[]; otherwise (or when P / NumPart changed since)
+ * it scans P[] on the host as run.c does.  A host that writes Ti_endstep
+ * itself must call it only before its own writes or after the next
+ * advance_and_find_timesteps. */
+int cuco_dropin_min_ti_endstep(void);
+/* No counterpart in the reference.  1 when the drop-in's kernels read and
+ * write the host's P[] in place (the device accesses pageable host memory
+ * coherently, e.g. a Grace host over NVLink-C2C, and CUCO_DROPIN_MIRROR is not
+ * "1"); 0 when each call copies P[] whole to a device mirror and back. */
+int cuco_dropin_host_access(void);
 /* driftfac.c:14-42 (tables integrated in FP64; the float tables DriftTable /
  * GravKickTable are filled too) */
 void init_drift_table(void);

@@ -36,12 +36,20 @@ def test_forces_vs_reference_fixture(gold, cell_grid):
     box.close()
 
 
-def test_dropin_run_loop_vs_reference(gold):
+@pytest.mark.parametrize("mirror", ["0", "1"])
+def test_dropin_run_loop_vs_reference(gold, mirror, monkeypatch):
+    # "1": P[] copied whole to a device mirror around each call; "0": the
+    # kernels work on the host P[] in place where the device allows it
+    monkeypatch.setenv("CUCO_DROPIN_MIRROR", mirror)
     M = int(gold["pmgrid"])
     d = DropIn(gold["pos"], gold["vel"], float(gold["mass"]), float(gold["boxsize"]),
                float(gold["a_begin"]), M, 0, float(gold["eps"]))
     assert d.All.Asmth == np.float32(gold["asmth"]) and d.All.Rcut == np.float32(gold["rcut"])
-    tis = [d.run_pass() for _ in range(3)]
+    tis = []
+    for _ in range(3):
+        tis.append(d.run_pass())
+        # the device-side minimum equals the host scan of run.c:35-40
+        assert d.lib.cuco_dropin_min_ti_endstep() == int(d.timeline()[1].min())
     assert tis == list(gold["run_ti_current"])
     beg, end = d.timeline()
     assert np.array_equal(beg, gold["run_ti_beg"]) and np.array_equal(end, gold["run_ti_end"])
