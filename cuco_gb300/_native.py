@@ -123,6 +123,8 @@ SIGNATURES = {
     "cuco_box_destroy": (_I, [_P]),
     "cuco_box_set_state": (_I, [_P, _P, _P, _I]),
     "cuco_box_get_state": (_I, [_P, _P, _P, _P, _P, _I]),
+    "cuco_box_set_state_fixed": (_I, [_P, _P, _P, _I]),
+    "cuco_box_get_state_fixed": (_I, [_P, _P, _I]),
     "cuco_box_set_softening": (_I, [_P, ctypes.c_float]),
     "cuco_box_forces": (_I, [_P, _I, _I]),
     "cuco_box_step": (_I, [_P, _D, _D, _D]),

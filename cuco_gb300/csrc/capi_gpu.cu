@@ -105,7 +105,7 @@ void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridP
         capi_fail("cudaForceEvaluateShortrange", "setSimParam/setSoftParam have not been called");
     int G = (int)llround(cbrt((double)numCells));
     if ((uint)(G * G * G) != numCells) capi_fail("cudaForceEvaluateShortrange", "numCells is not a cube");
-    ShortRangeParams p;
+    ShortRangeParams p{};
     p.boxsize = s.sim.boxsize;
     p.gridfac = s.sim.to_grid_fac;
     p.cellw = s.sim.boxsize / G;

@@ -81,6 +81,8 @@ struct ShortRangeParams {
     float h, hinv, h3inv;
     int grid;        // G
     uint32_t n;
+    bool fixed;      // positions are 32-bit fixed point (bit patterns in the float4s)
+    float fscale;    // L / 2^32
 };
 
 // Which cell-bound format the kernel reads.
@@ -105,6 +107,7 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
 
 struct PMPlan {
     int M;
+    bool fixed;         // positions are 32-bit fixed point (units of L / 2^32)
     float boxsize;
     float to_slab_fac;  // M / L in float (pm_periodic.c:42)
     float mass;
@@ -116,7 +119,7 @@ struct PMPlan {
 };
 
 cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, float mass,
-                             double G);
+                             double G, bool fixed = false);
 void pm_plan_destroy(PMPlan *plan);
 // Long-range acceleration of n positions (any order) into acc (same order).
 cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,

@@ -63,6 +63,51 @@ __global__ void k_drift_keys(float4 *__restrict__ pos, const float4 *__restrict_
     keys[i] = ((uint32_t)k[0] * G + k[1]) * G + k[2];
 }
 
+// Fixed-point form: positions are uint32 per axis in units of L / 2^32 (bit
+// patterns in the float4 slots).  The drift adds the displacement rounded
+// once to that grid; the uint32 add wraps modulo 2^32, i.e. modulo L, so the
+// periodic wrap is exact and needs no loop.  The key is floor(x * G / 2^32),
+// an exact integer product.
+__global__ void k_drift_keys_fixed(float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                                   float units_per_time, int do_drift, uint32_t *__restrict__ keys,
+                                   uint32_t n, int G) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos[i];
+    uint32_t c[3] = {__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z)};
+    if (do_drift) {
+        const float4 v = vel[i];
+        const float vv[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) c[d] += (uint32_t)__float2ll_rn(vv[d] * units_per_time);
+        pos[i] = make_float4(__uint_as_float(c[0]), __uint_as_float(c[1]), __uint_as_float(c[2]), p.w);
+    }
+    uint32_t k[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) k[d] = (uint32_t)(((uint64_t)c[d] * (uint32_t)G) >> 32);
+    keys[i] = (k[0] * G + k[1]) * G + k[2];
+}
+
+// float positions (any real value) -> fixed point, wrapped into [0, L)
+__global__ void k_to_fixed(const float *__restrict__ a, float4 *__restrict__ b, uint32_t n, double units_per_length) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t c[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) c[d] = (uint32_t)(unsigned long long)__double2ll_rn((double)a[3 * i + d] * units_per_length);
+    b[i] = make_float4(__uint_as_float(c[0]), __uint_as_float(c[1]), __uint_as_float(c[2]), 0.f);
+}
+
+// fixed point -> float positions in [0, L)
+__global__ void k_from_fixed(const float4 *__restrict__ b, float *__restrict__ a, uint32_t n, double length_per_unit) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 v = b[i];
+    a[3 * i + 0] = (float)((double)__float_as_uint(v.x) * length_per_unit);
+    a[3 * i + 1] = (float)((double)__float_as_uint(v.y) * length_per_unit);
+    a[3 * i + 2] = (float)((double)__float_as_uint(v.z) * length_per_unit);
+}
+
 __global__ void k_scatter4(const float4 *__restrict__ src_sorted, const uint32_t *__restrict__ perm,
                            float4 *__restrict__ dst, uint32_t n) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,6 +225,29 @@ cuco_status_t launch_drift_keys(float4 *pos, const float4 *vel, double drift, fl
     return CUCO_OK;
 }
 
+cuco_status_t launch_drift_keys_fixed(float4 *pos, const float4 *vel, double drift, float boxsize,
+                                      bool do_drift, uint32_t *keys, uint32_t n, int G, cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    const float upt = (float)(drift * 4294967296.0 / (double)boxsize);
+    k_drift_keys_fixed<<<(n + 255) / 256, 256, 0, stream>>>(pos, vel, upt, do_drift ? 1 : 0, keys, n, G);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t to_fixed(const float *a, float4 *b, uint32_t n, float boxsize, cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    k_to_fixed<<<(n + 255) / 256, 256, 0, stream>>>(a, b, n, 4294967296.0 / (double)boxsize);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+cuco_status_t from_fixed(const float4 *b, float *a, uint32_t n, float boxsize, cudaStream_t stream) {
+    if (!n) return CUCO_OK;
+    k_from_fixed<<<(n + 255) / 256, 256, 0, stream>>>(b, a, n, (double)boxsize / 4294967296.0);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
 cuco_status_t scatter4(const float4 *src_sorted, const uint32_t *perm, float4 *dst, uint32_t n,
                        cudaStream_t stream) {
     if (!n) return CUCO_OK;
@@ -251,7 +319,7 @@ cuco_status_t alloc(T **p, size_t count) {
 }
 
 ShortRangeParams make_sr_params(const cuco_box *b) {
-    ShortRangeParams p;
+    ShortRangeParams p{};
     p.boxsize = b->cfg.boxsize;
     p.gridfac = b->gridfac;
     p.cellw = b->cfg.boxsize / b->G;
@@ -266,7 +334,17 @@ ShortRangeParams make_sr_params(const cuco_box *b) {
     p.h3inv = p.hinv * p.hinv * p.hinv;
     p.grid = b->G;
     p.n = b->n;
+    p.fixed = b->cfg.mode == CUCO_MODE_FIXED;
+    p.fscale = ldexpf(b->cfg.boxsize, -32);
     return p;
+}
+
+cuco_status_t drift_keys(cuco_box *b, double drift, bool do_drift) {
+    if (b->cfg.mode == CUCO_MODE_FIXED)
+        return launch_drift_keys_fixed(b->pos, b->vel, drift, b->cfg.boxsize, do_drift, b->keys, b->n, b->G,
+                                       b->stream);
+    return launch_drift_keys(b->pos, b->vel, drift, b->cfg.boxsize, do_drift, b->keys, b->n, b->gridfac, b->G,
+                             b->stream);
 }
 
 void record(cuco_box *b, int i) {
@@ -355,9 +433,9 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         set_error("cuco_box_create: invalid configuration");
         return CUCO_ERR_INVALID;
     }
-    if (cfg->mode != CUCO_MODE_PLAIN) {
-        set_error("cuco_box_create: only CUCO_MODE_PLAIN is built in this version");
-        return CUCO_ERR_UNSUPPORTED;
+    if (cfg->mode != CUCO_MODE_PLAIN && cfg->mode != CUCO_MODE_FIXED) {
+        set_error("cuco_box_create: unknown mode");
+        return CUCO_ERR_INVALID;
     }
     CUCO_TRY_CUDA(cudaSetDevice(cfg->device));
     cuco_box *b = new cuco_box();
@@ -394,7 +472,9 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         set_error("table upload failed");
         return fail(CUCO_ERR_CUDA);
     }
-    if ((s = pm_plan_create(&b->pm, b->M, cfg->boxsize, cfg->asmth, cfg->mass, cfg->G))) return fail(s);
+    if ((s = pm_plan_create(&b->pm, b->M, cfg->boxsize, cfg->asmth, cfg->mass, cfg->G,
+                            cfg->mode == CUCO_MODE_FIXED)))
+        return fail(s);
     cudaMemsetAsync(b->acc_pp, 0, sizeof(float4) * (n ? n : 1), b->stream);
     cudaMemsetAsync(b->acc_pm, 0, sizeof(float4) * (n ? n : 1), b->stream);
     cudaMemsetAsync(b->vel, 0, sizeof(float4) * (n ? n : 1), b->stream);
@@ -441,7 +521,10 @@ cuco_status_t cuco_box_set_state(cuco_box_t *b, const float *pos, const float *v
     const size_t bytes = sizeof(float) * 3 * b->n;
     cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, pos, bytes, kind, b->stream));
-    CUCO_TRY(pack3to4(b->stage3, b->pos, b->n, b->stream));
+    if (b->cfg.mode == CUCO_MODE_FIXED)
+        CUCO_TRY(to_fixed(b->stage3, b->pos, b->n, b->cfg.boxsize, b->stream));
+    else
+        CUCO_TRY(pack3to4(b->stage3, b->pos, b->n, b->stream));
     if (vel) {
         CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, vel, bytes, kind, b->stream));
         CUCO_TRY(pack3to4(b->stage3, b->vel, b->n, b->stream));
@@ -462,9 +545,42 @@ cuco_status_t cuco_box_get_state(cuco_box_t *b, float *pos, float *vel, float *a
     float4 *src[4] = {b->pos, b->vel, b->acc_pp, b->acc_pm};
     for (int k = 0; k < 4; ++k) {
         if (!dst[k]) continue;
-        CUCO_TRY(unpack4to3(src[k], b->stage3, b->n, b->stream));
+        if (k == 0 && b->cfg.mode == CUCO_MODE_FIXED)
+            CUCO_TRY(from_fixed(src[k], b->stage3, b->n, b->cfg.boxsize, b->stream));
+        else
+            CUCO_TRY(unpack4to3(src[k], b->stage3, b->n, b->stream));
         CUCO_TRY_CUDA(cudaMemcpyAsync(dst[k], b->stage3, bytes, kind, b->stream));
     }
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_set_state_fixed(cuco_box_t *b, const uint32_t *pos, const float *vel, int on_device) {
+    if (!b || !pos || b->cfg.mode != CUCO_MODE_FIXED) {
+        set_error("cuco_box_set_state_fixed: null argument or not a fixed-point box");
+        return CUCO_ERR_INVALID;
+    }
+    const size_t bytes = sizeof(float) * 3 * b->n;
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    // the uint32 triplets move as bit patterns: pack3to4 only copies words
+    CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, pos, bytes, kind, b->stream));
+    CUCO_TRY(pack3to4(b->stage3, b->pos, b->n, b->stream));
+    if (vel) {
+        CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, vel, bytes, kind, b->stream));
+        CUCO_TRY(pack3to4(b->stage3, b->vel, b->n, b->stream));
+    }
+    b->has_state = true;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_get_state_fixed(cuco_box_t *b, uint32_t *pos, int on_device) {
+    if (!b || !pos || b->cfg.mode != CUCO_MODE_FIXED) {
+        set_error("cuco_box_get_state_fixed: null argument or not a fixed-point box");
+        return CUCO_ERR_INVALID;
+    }
+    CUCO_TRY(unpack4to3(b->pos, b->stage3, b->n, b->stream));
+    CUCO_TRY_CUDA(cudaMemcpyAsync(pos, b->stage3, sizeof(float) * 3 * b->n,
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->stream));
     CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
     return CUCO_OK;
 }
@@ -485,8 +601,7 @@ cuco_status_t cuco_box_forces(cuco_box_t *b, int pm, int pp) {
     }
     b->launches = 0;
     record(b, 0);
-    CUCO_TRY(launch_drift_keys(b->pos, b->vel, 0.0, b->cfg.boxsize, false, b->keys, b->n,
-                               b->gridfac, b->G, b->stream));
+    CUCO_TRY(drift_keys(b, 0.0, false));
     b->launches += 1;
     record(b, 1);
     CUCO_TRY(forces_after_keys(b, pm, pp, nullptr));
@@ -501,8 +616,7 @@ cuco_status_t cuco_box_step(cuco_box_t *b, double drift, double kick_pp, double 
     }
     b->launches = 0;
     record(b, 0);
-    CUCO_TRY(launch_drift_keys(b->pos, b->vel, drift, b->cfg.boxsize, drift != 0.0, b->keys, b->n,
-                               b->gridfac, b->G, b->stream));
+    CUCO_TRY(drift_keys(b, drift, drift != 0.0));
     b->launches += 1;
     record(b, 1);
     KickArgs k{};

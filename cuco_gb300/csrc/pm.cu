@@ -268,16 +268,41 @@ __device__ __forceinline__ void cic_axis(float to_slab_fac, float p, int M, int 
     *ss = sl + 1 >= M ? sl + 1 - M : sl + 1;
 }
 
+// The same for a 32-bit fixed-point coordinate x (units of L / 2^32): the
+// mesh coordinate x * M / 2^32 is exact in 32.32 fixed point, so the cell and
+// the fraction (rounded once, to float) need no float product.
+__device__ __forceinline__ void cic_axis_fixed(uint32_t x, int M, int *s, int *ss, float *d) {
+    const uint64_t t = (uint64_t)x * (uint32_t)M;
+    const int sl = (int)(t >> 32);  // < M
+    *d = (float)(uint32_t)t * 2.3283064365386963e-10f;  // 2^-32
+    *s = sl;
+    *ss = sl + 1 >= M ? sl + 1 - M : sl + 1;
+}
+
+template <bool FIXED>
+__device__ __forceinline__ void cic_point(const float4 &p, float to_slab_fac, int M, int s[3][2], float d[3]) {
+    if (FIXED) {
+        cic_axis_fixed(__float_as_uint(p.x), M, &s[0][0], &s[0][1], &d[0]);
+        cic_axis_fixed(__float_as_uint(p.y), M, &s[1][0], &s[1][1], &d[1]);
+        cic_axis_fixed(__float_as_uint(p.z), M, &s[2][0], &s[2][1], &d[2]);
+    } else {
+        cic_axis(to_slab_fac, p.x, M, &s[0][0], &s[0][1], &d[0]);
+        cic_axis(to_slab_fac, p.y, M, &s[1][0], &s[1][1], &d[1]);
+        cic_axis(to_slab_fac, p.z, M, &s[2][0], &s[2][1], &d[2]);
+    }
+}
+
+template <bool FIXED>
 __global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__restrict__ rho,
                           int M, float to_slab_fac, float mass) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float4 p = pos[i];
-    int sx, sxx, sy, syy, sz, szz;
-    float dx, dy, dz;
-    cic_axis(to_slab_fac, p.x, M, &sx, &sxx, &dx);
-    cic_axis(to_slab_fac, p.y, M, &sy, &syy, &dy);
-    cic_axis(to_slab_fac, p.z, M, &sz, &szz, &dz);
+    int s[3][2];
+    float d[3];
+    cic_point<FIXED>(p, to_slab_fac, M, s, d);
+    const int sx = s[0][0], sxx = s[0][1], sy = s[1][0], syy = s[1][1], sz = s[2][0], szz = s[2][1];
+    const float dx = d[0], dy = d[1], dz = d[2];
     const size_t Mz = M, Myz = (size_t)M * M;
     float m0 = mass * (1.f - dx), m1 = mass * dx;
     atomicAdd(&rho[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz));
@@ -292,6 +317,7 @@ __global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__r
 
 __device__ __forceinline__ int wrapi(int a, int M) { return a < 0 ? a + M : (a >= M ? a - M : a); }
 
+template <bool FIXED>
 __global__ void k_interp(const float4 *__restrict__ pos, uint32_t n, const float *__restrict__ phi,
                          int M, float to_slab_fac, float fac, float4 *__restrict__ acc) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -299,9 +325,7 @@ __global__ void k_interp(const float4 *__restrict__ pos, uint32_t n, const float
     float4 p = pos[i];
     int s[3][2];
     float d[3];
-    cic_axis(to_slab_fac, p.x, M, &s[0][0], &s[0][1], &d[0]);
-    cic_axis(to_slab_fac, p.y, M, &s[1][0], &s[1][1], &d[1]);
-    cic_axis(to_slab_fac, p.z, M, &s[2][0], &s[2][1], &d[2]);
+    cic_point<FIXED>(p, to_slab_fac, M, s, d);
     const size_t Mz = M, Myz = (size_t)M * M;
     float wx[2] = {1.f - d[0], d[0]}, wy[2] = {1.f - d[1], d[1]}, wz[2] = {1.f - d[2], d[2]};
     float out[3];
@@ -352,12 +376,13 @@ int fft_batch_axis(int M) {
 }  // namespace
 
 cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, float mass,
-                             double G) {
+                             double G, bool fixed) {
     if (M < 8 || M > 1024 || (M & (M - 1))) {
         set_error("PM mesh size must be a power of two in [8, 1024]");
         return CUCO_ERR_UNSUPPORTED;
     }
     plan->M = M;
+    plan->fixed = fixed;
     plan->boxsize = boxsize;
     plan->to_slab_fac = (float)M / boxsize;
     plan->mass = mass;
@@ -411,7 +436,12 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
     const size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
     const size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
     CUCO_TRY_CUDA(cudaMemsetAsync(plan.rho, 0, sizeof(float) * (size_t)M * M * M, stream));
-    if (n) k_deposit<<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.mass);
+    if (n) {
+        if (plan.fixed)
+            k_deposit<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.mass);
+        else
+            k_deposit<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.mass);
+    }
     CUCO_TRY_CUDA(cudaGetLastError());
     if (ev_deposit_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_deposit_done, stream));
     const unsigned zblocks = (unsigned)((size_t)M * M / (2 * P));
@@ -423,7 +453,12 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
     k_fft_z_c2r<<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, M, P);
     CUCO_TRY_CUDA(cudaGetLastError());
     if (ev_fft_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_fft_done, stream));
-    if (n) k_interp<<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.fd_fac, acc);
+    if (n) {
+        if (plan.fixed)
+            k_interp<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.fd_fac, acc);
+        else
+            k_interp<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.fd_fac, acc);
+    }
     CUCO_TRY_CUDA(cudaGetLastError());
     if (launches) *launches += 8;
     return CUCO_OK;

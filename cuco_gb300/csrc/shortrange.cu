@@ -102,13 +102,21 @@ __device__ __forceinline__ void cell_range(const uint32_t *__restrict__ a,
     }
 }
 
+// s + e = a + b exactly (Knuth's two-sum; the intrinsics keep the compiler
+// from contracting or reordering it).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 // r^2 with a fixed operation order: the candidate test and the force pass
 // must agree on it bit for bit.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
-template <CellFormat FMT, bool KICK, bool COUNT>
+template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
 __global__ void __launch_bounds__(kThreads, 4)
     k_shortrange(ShortRangeParams p, ColumnSet cs, const float4 *__restrict__ spos,
                  const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
@@ -241,8 +249,25 @@ __global__ void __launch_bounds__(kThreads, 4)
     const float winv = 1.0f / w;
     // integer origin at the segment corner (see the file comment)
     const float ox = floorf(ix * w), oy = floorf(iy * w), oz = floorf(iz0 * w);
+    // Fixed-point positions: the origin is the segment corner on the 2^32
+    // grid, and an int32 difference from it is the periodic image for free
+    // (every staged source lies within S + R < G/2 cells of it).
+    const uint32_t oxu = (uint32_t)(((uint64_t)ix << 32) / (uint32_t)G);
+    const uint32_t oyu = (uint32_t)(((uint64_t)iy << 32) / (uint32_t)G);
+    const uint32_t ozu = (uint32_t)(((uint64_t)iz0 << 32) / (uint32_t)G);
+    const float fs = p.fscale;
+    // __fmul_rn: a target's coordinates must equal its own staged copy bit
+    // for bit (the self pair then has r = 0 exactly), so the product may not
+    // be contracted into the later subtraction
+    auto rel = [&](float4 a) {
+        return make_float4(__fmul_rn((float)(int32_t)(__float_as_uint(a.x) - oxu), fs),
+                           __fmul_rn((float)(int32_t)(__float_as_uint(a.y) - oyu), fs),
+                           __fmul_rn((float)(int32_t)(__float_as_uint(a.z) - ozu), fs), 0.f);
+    };
     const float kEdge = 4e-7f;
-    const float rc2_lo = p.rcut2 * (1.f - 2.f * kEdge), rc2_hi = p.rcut2 * (1.f + 2.f * kEdge);
+    // plain: cut-edge band decided in double; fixed: the float cut
+    const float rc2_lo = FIXED ? p.rcut2 : p.rcut2 * (1.f - 2.f * kEdge);
+    const float rc2_hi = FIXED ? p.rcut2 : p.rcut2 * (1.f + 2.f * kEdge);
     const double rcut2_d = (double)p.rcut * (double)p.rcut;
     bool staged = false;
     uint32_t npairs = 0;
@@ -274,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         const float xf = __fadd_rz(xt, 8388608.0f);
         const uint32_t ti = (uint32_t)(__float_as_int(xf) - 0x4B000000);
         const float frac = xt - (xf - 8388608.0f);
-        const bool edge = fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f);
+        const bool edge = !FIXED && fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f);
         const bool fast = r2 <= rc2_lo && !edge && r >= hmin;
         const float fac = fast ? rinv * rinv * rinv * tab[min(ti, (uint32_t)kNTab - 1u)] : 0.f;
         ax = __fmaf_rn(dx, fac, ax);
@@ -294,7 +319,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         int ti = __float_as_int(xf) - 0x4B000000;
         const float frac = xt - (xf - 8388608.0f);
         float fac = rinv * rinv * rinv;
-        if (fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f) || r2 > rc2_lo) {
+        if (!FIXED && (fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f) || r2 > rc2_lo)) {
             // decided in double as the reference's CPU path computes it
             const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
             ok = ok && dd <= rcut2_d;
@@ -321,10 +346,22 @@ __global__ void __launch_bounds__(kThreads, 4)
     for (uint32_t round = 0; round < rounds; ++round) {
         const uint32_t t = round * kWarps + warp;
         const bool active = t < nt;  // warp-uniform
-        const float4 pt = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-        tx = pt.x - ox;
-        ty = pt.y - oy;
-        tz = pt.z - oz;
+        const float4 praw = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        // pt: absolute float coordinates for the culling (fixed point rounded
+        // to float: the culling margin covers it); tx..tz: origin-relative
+        float4 pt = praw;
+        if (FIXED) {
+            pt = make_float4((float)__float_as_uint(praw.x) * fs, (float)__float_as_uint(praw.y) * fs,
+                             (float)__float_as_uint(praw.z) * fs, 0.f);
+            const float4 tr = rel(praw);
+            tx = tr.x;
+            ty = tr.y;
+            tz = tr.z;
+        } else {
+            tx = pt.x - ox;
+            ty = pt.y - oy;
+            tz = pt.z - oz;
+        }
         float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
@@ -341,8 +378,13 @@ __global__ void __launch_bounds__(kThreads, 4)
                         const float4 a0 = spos[r.gsrc + (s0 - r.soff)];
                         float4 a1 = make_float4(0.f, 0.f, 0.f, 0.f);
                         if (s1 < hi) a1 = spos[r.gsrc + (s1 - r.soff)];
-                        src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
-                        if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
+                        if (FIXED) {
+                            src[s0 - c0] = rel(a0);
+                            if (s1 < hi) src[s1 - c0] = rel(a1);
+                        } else {
+                            src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
+                            if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
+                        }
                     }
                 }
                 __syncthreads();
@@ -425,14 +467,38 @@ __global__ void __launch_bounds__(kThreads, 4)
             }
         }
         if (!active) continue;
-        ax += bx;
-        ay += by;
-        az += bz;
+        if (FIXED) {
+            // compensated: two-sum of the lanes' partial sums, errors carried
+            float ex, ey, ez;
+            two_sum(ax, bx, ax, ex);
+            two_sum(ay, by, ay, ey);
+            two_sum(az, bz, az, ez);
 #pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            ax += __shfl_xor_sync(kFull, ax, off);
-            ay += __shfl_xor_sync(kFull, ay, off);
-            az += __shfl_xor_sync(kFull, az, off);
+            for (int off = 16; off > 0; off >>= 1) {
+                float e;
+                const float ox_ = __shfl_xor_sync(kFull, ax, off), oex = __shfl_xor_sync(kFull, ex, off);
+                two_sum(ax, ox_, ax, e);
+                ex = __fadd_rn(ex, __fadd_rn(oex, e));
+                const float oy_ = __shfl_xor_sync(kFull, ay, off), oey = __shfl_xor_sync(kFull, ey, off);
+                two_sum(ay, oy_, ay, e);
+                ey = __fadd_rn(ey, __fadd_rn(oey, e));
+                const float oz_ = __shfl_xor_sync(kFull, az, off), oez = __shfl_xor_sync(kFull, ez, off);
+                two_sum(az, oz_, az, e);
+                ez = __fadd_rn(ez, __fadd_rn(oez, e));
+            }
+            ax = __fadd_rn(ax, ex);
+            ay = __fadd_rn(ay, ey);
+            az = __fadd_rn(az, ez);
+        } else {
+            ax += bx;
+            ay += by;
+            az += bz;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                ax += __shfl_xor_sync(kFull, ax, off);
+                ay += __shfl_xor_sync(kFull, ay, off);
+                az += __shfl_xor_sync(kFull, az, off);
+            }
         }
         if (lane == 0) {
             const uint32_t i = t_begin + t;
@@ -480,8 +546,11 @@ bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
     // segment length: a power of two dividing G, with the S + 2R z-cells of a
     // column at most G (so a column's z range wraps at most once)
     int S = kMaxSeg;
-    while (S > 1 && (p.grid % S || p.grid < S + 2 * R)) S >>= 1;
-    if (p.grid < S + 2 * R) return false;
+    // fixed point also needs every staged source within G/2 cells of the
+    // segment corner (the int32 difference is the periodic image)
+    auto bad = [&](int s) { return p.grid % s || p.grid < s + 2 * R || (p.fixed && 2 * (s + R) >= p.grid); };
+    while (S > 1 && bad(S)) S >>= 1;
+    if (bad(S)) return false;
     cs->R = R;
     cs->S = S;
     cs->margin = (float)margin;
@@ -500,7 +569,7 @@ bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
 
 }  // namespace
 
-template <CellFormat FMT, bool KICK>
+template <CellFormat FMT, bool KICK, bool FIXED>
 void launch_fmt_kick(unsigned blocks, cudaStream_t stream, const ShortRangeParams &p,
                      const ColumnSet &cs, const float4 *sorted_pos, const uint32_t *perm,
                      const uint32_t *cell_a, const uint32_t *cell_b, const float *table,
@@ -508,18 +577,18 @@ void launch_fmt_kick(unsigned blocks, cudaStream_t stream, const ShortRangeParam
     const size_t sm = smem_bytes(cs.ncols, cs.S + 2 * cs.R);
     static const size_t sm_max = smem_bytes(kMaxCols, kMaxSeg + 2 * kMaxR);
     static bool attr = [] {
-        cudaFuncSetAttribute(k_shortrange<FMT, KICK, true>,
+        cudaFuncSetAttribute(k_shortrange<FMT, KICK, true, FIXED>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange<FMT, KICK, false>,
+        cudaFuncSetAttribute(k_shortrange<FMT, KICK, false, FIXED>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
         return true;
     }();
     (void)attr;
     if (counter)
-        k_shortrange<FMT, KICK, true><<<blocks, kThreads, sm, stream>>>(
+        k_shortrange<FMT, KICK, true, FIXED><<<blocks, kThreads, sm, stream>>>(
             p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
     else
-        k_shortrange<FMT, KICK, false><<<blocks, kThreads, sm, stream>>>(
+        k_shortrange<FMT, KICK, false, FIXED><<<blocks, kThreads, sm, stream>>>(
             p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
 }
 
@@ -538,16 +607,25 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
     const int G = p.grid;
     const unsigned blocks = (unsigned)G * G * (G / cs.S);
     const bool kick_on = kick.vel != nullptr;
-    if (fmt == kCellOffsets) {
+    if (p.fixed && fmt != kCellOffsets) {
+        set_error("short range: fixed-point positions need the engine's cell-offset format");
+        return CUCO_ERR_UNSUPPORTED;
+    }
+    if (p.fixed) {
         if (kick_on)
-            launch_fmt_kick<kCellOffsets, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, true, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellOffsets, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, false, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+    } else if (fmt == kCellOffsets) {
+        if (kick_on)
+            launch_fmt_kick<kCellOffsets, true, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+        else
+            launch_fmt_kick<kCellOffsets, false, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     } else {
         if (kick_on)
-            launch_fmt_kick<kCellStartEnd, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellStartEnd, true, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellStartEnd, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellStartEnd, false, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     }
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;

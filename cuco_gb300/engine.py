@@ -139,6 +139,19 @@ class Box:
         check(self.lib.cuco_box_set_state(self.h, ptr(pos), ptr(v) if v is not None else None, 0),
               "cuco_box_set_state")
 
+    def set_state_fixed(self, pos_u32: np.ndarray, vel: np.ndarray | None = None):
+        """Fixed-point boxes: positions as uint32 (units of boxsize / 2^32)."""
+        pos = np.ascontiguousarray(pos_u32, dtype=np.uint32)
+        assert pos.shape == (self.n, 3)
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float32)
+        check(self.lib.cuco_box_set_state_fixed(self.h, ptr(pos), ptr(v) if v is not None else None, 0),
+              "cuco_box_set_state_fixed")
+
+    def get_state_fixed(self) -> np.ndarray:
+        out = np.empty((self.n, 3), dtype=np.uint32)
+        check(self.lib.cuco_box_get_state_fixed(self.h, ptr(out), 0), "cuco_box_get_state_fixed")
+        return out
+
     def set_state_device(self, pos_ptr: int, vel_ptr: int | None):
         check(self.lib.cuco_box_set_state(self.h, ctypes.c_void_p(pos_ptr),
                                           ctypes.c_void_p(vel_ptr) if vel_ptr else None, 1),

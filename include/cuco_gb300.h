@@ -212,6 +212,12 @@ cuco_status_t cuco_box_set_state(cuco_box_t *box, const float *pos, const float 
                                  int on_device);
 cuco_status_t cuco_box_get_state(cuco_box_t *box, float *pos, float *vel, float *acc_pp,
                                  float *acc_pm, int on_device);
+/* CUCO_MODE_FIXED boxes only: positions as uint32 x,y,z per particle in units
+ * of boxsize / 2^32 (exact; cuco_box_set_state converts floats by rounding to
+ * that grid, cuco_box_get_state rounds back to float). */
+cuco_status_t cuco_box_set_state_fixed(cuco_box_t *box, const uint32_t *pos, const float *vel,
+                                       int on_device);
+cuco_status_t cuco_box_get_state_fixed(cuco_box_t *box, uint32_t *pos, int on_device);
 /* Spline softening length h (changes with time when softening is physical). */
 cuco_status_t cuco_box_set_softening(cuco_box_t *box, float h);
 
