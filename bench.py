@@ -50,12 +50,29 @@ NSTEPS_RUN = 200
 SEED = 12345
 SOFT_FRAC = 0.025
 WORKLOAD = "plain-128^3-L256-M256-G64-z49to0-200steps"
+MODE = 0  # 0 plain (float32 positions, the reference's arithmetic), 1 fixed point
+
+# --workload presets: (n_side, box Mpc/h, mesh, cell grid, mode, name).  The
+# default is the plain method at mid size; the others are the precision form
+# (uint32 fixed-point positions) at the same size and both forms at 512^3.
+PRESETS = {
+    "plain-128": (128, 256.0, 256, 64, 0, "plain-128^3-L256-M256-G64-z49to0-200steps"),
+    "precision-128": (128, 256.0, 256, 64, 1, "precision-128^3-L256-M256-G64-z49to0-200steps"),
+    "plain-512": (512, 1000.0, 1024, 256, 0, "plain-512^3-L1000-M1024-G256-z49to0-200steps"),
+    "precision-512": (512, 1000.0, 1024, 256, 1, "precision-512^3-L1000-M1024-G256-z49to0-200steps"),
+}
+
+
+def apply_preset(name):
+    global N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD
+    N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD = PRESETS[name]
 
 
 def workload_config():
     return {"workload": WORKLOAD, "particles": N_SIDE ** 3, "box_mpc_h": BOX_MPC, "pm_grid": PM_GRID,
             "cell_grid": CELL_GRID, "z_init": Z_INIT, "log_a_steps": NSTEPS_RUN, "seed": SEED,
-            "softening": f"{SOFT_FRAC} mean spacing", "l2": "working set > L2 (no flush)"}
+            "softening": f"{SOFT_FRAC} mean spacing", "l2": "working set > L2 (no flush)",
+            "positions": "uint32 fixed point (L/2^32)" if MODE else "float32"}
 
 
 class ClockSampler:
@@ -232,7 +249,7 @@ def run_gpu_arm(args, world, rank, local):
     a, drift, kick = schedule(ic)
     vel0 = ic.canonical_velocity()
     box = Box(BoxConfig(n=ic.n, pm_grid=PM_GRID, cell_grid=CELL_GRID, boxsize=ic.boxsize,
-                        mass=ic.mass, G=ics.G_INTERNAL, softening=soft, device=local))
+                        mass=ic.mass, G=ics.G_INTERNAL, softening=soft, device=local, mode=MODE))
     K, W = args.steps, args.warmup
     box.set_state(ic.pos, vel0)
     for s in range(W):
@@ -272,7 +289,7 @@ def run_gpu_arm(args, world, rank, local):
     line = {
         "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": K, "warmup": W, "ms_per_step": 1e3 * t_total / K, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32" if MODE else "f32", "data": "synthetic",
         "config": workload_config(),
         "roofline": {"bound": "fp32", "kernel": "k_shortrange", "achieved": achieved,
                      "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
@@ -285,8 +302,10 @@ def run_gpu_arm(args, world, rank, local):
         "gpu_launches": launches,
     }
     box.close()
-    if args.e2e_steps:
+    if args.e2e_steps and MODE == 0:
         line["e2e"] = run_e2e(min(args.e2e_steps, K), ic, soft, local)
+    elif MODE:
+        line["e2e"] = {"value": None, "reason": "the drop-in C ABI is the plain form only"}
     if rank == 0 and not args.no_cpu:
         try:
             v, kind, sample, info = cpu_sample_rate(os.cpu_count() or 1)
@@ -378,7 +397,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS))
     args = ap.parse_args()
+    apply_preset(args.workload)
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
     if args.impl == "reference":
