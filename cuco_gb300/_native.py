@@ -137,6 +137,17 @@ SIGNATURES = {
     "cuco_box_launches_per_step": (_I, [_P]),
     "cuco_box_pair_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), _I]),
     "cuco_box_timer": (_I, [_P, _I, ctypes.POINTER(ctypes.c_float)]),
+    "cuco_ensemble_create": (_I, [ctypes.POINTER(CucoConfig), _I, ctypes.POINTER(_P)]),
+    "cuco_ensemble_destroy": (_I, [_P]),
+    "cuco_ensemble_cell_grid": (_I, [_P, _I, _P, _P, _P]),
+    "cuco_ensemble_set_state": (_I, [_P, _I, _P, _P]),
+    "cuco_ensemble_get_state": (_I, [_P, _I, _P, _P, _P, _P]),
+    "cuco_ensemble_forces": (_I, [_P]),
+    "cuco_ensemble_step": (_I, [_P, _P, _P, _P]),
+    "cuco_ensemble_sync": (_I, [_P]),
+    "cuco_ensemble_timer": (_I, [_P, _I, ctypes.POINTER(ctypes.c_float)]),
+    "cuco_ensemble_count_pairs": (_I, [_P, _I, _P]),
+    "cuco_ensemble_launches_per_step": (_I, [_P]),
     "cuco_pinned_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "cuco_pinned_free": (_I, [_P]),
     "cuco_fp32_peak": (_I, [_I, ctypes.POINTER(_D)]),

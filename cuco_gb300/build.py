@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcuco_gb300.so")
-SOURCES = ["sort.cu", "shortrange.cu", "pm.cu", "engine.cu", "capi_gpu.cu", "dropin.cu",
+SOURCES = ["sort.cu", "shortrange.cu", "pm.cu", "engine.cu", "capi_gpu.cu", "dropin.cu", "ensemble.cu",
            "sort_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr",

@@ -83,6 +83,7 @@ struct ShortRangeParams {
     uint32_t n;
     bool fixed;      // positions are 32-bit fixed point (bit patterns in the float4s)
     float fscale;    // L / 2^32
+    uint32_t cell_base;  // first cell of this box in a multi-box cell array (0 otherwise)
 };
 
 // Which cell-bound format the kernel reads.
@@ -103,6 +104,18 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
                                 float4 *acc_out, const KickArgs &kick, cudaStream_t stream,
                                 unsigned long long *pair_counter = nullptr);
 
+// Many boxes in one launch (the batched form).  A box's descriptor holds its
+// parameters and neighbour-column set; shortrange_desc_fill writes one (in
+// host memory, shortrange_desc_bytes() long) and returns the box's segment
+// count and shared memory.  kicks[b] = (kick_pp, kick_pm) of box b.
+size_t shortrange_desc_bytes();
+cuco_status_t shortrange_desc_fill(const ShortRangeParams &p, void *desc, uint32_t *segments, size_t *smem);
+cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, const uint32_t *seg_base,
+                                      int nbox, uint32_t segments, size_t smem, bool fixed,
+                                      const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
+                                      const float *table, float4 *acc_out, const KickArgs &kick,
+                                      cudaStream_t stream, unsigned long long *pair_counter);
+
 // ------------------------------------------------------------------- PM
 
 struct PMPlan {
@@ -118,6 +131,8 @@ struct PMPlan {
     float2 *twiddle;    // M: exp(-2 pi i t / M)
 };
 
+// Meshes the FFT supports: even, 8..1024, no prime factor above 5.
+bool pm_mesh_supported(int M);
 cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, float mass,
                              double G, bool fixed = false);
 void pm_plan_destroy(PMPlan *plan);
@@ -126,11 +141,65 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
                         cudaStream_t stream, cudaEvent_t *ev_deposit_done,
                         cudaEvent_t *ev_fft_done, int *launches);
 
+// Many boxes' meshes in one launch per PM phase (the batched form).
+struct PMBoxDesc {
+    int M, P, B;         // mesh; z-pass row pairs and axis-pass columns per CTA
+    float to_slab_fac, mass, fd_fac;
+    float *rho;          // this box's M^3 real grid (density, then potential)
+    float2 *spec;        // its M*M*(M/2+1) half spectrum
+    const float *green1d;
+    const float2 *twiddle;
+};
+struct PMMulti {
+    int nbox;
+    bool fixed;
+    const PMBoxDesc *boxes;   // device
+    const uint32_t *pbeg;     // device, nbox+1: each box's first particle
+    const uint2 *map_z;       // device: (box, block) per CTA of the z passes
+    const uint2 *map_axis;    // device: (box, block) per CTA of the y/x passes
+    uint32_t nz_blocks, naxis_blocks;
+    size_t smz, sma;          // dynamic shared memory of the z and axis passes
+    float *rho_all;           // all boxes' real grids, contiguous (one memset)
+    size_t rho_all_count;
+};
+int pm_batch_z(int M);
+int pm_batch_axis(int M);
+size_t pm_smem_z(int M, int P);
+size_t pm_smem_axis(int M, int B);
+void pm_tables(int M, float boxsize, float asmth, float *green1d, float2 *twiddle);
+float pm_fd_fac(int M, float boxsize, double G);
+// PM accelerations of n positions laid out box after box (pbeg), into acc.
+cuco_status_t pm_forces_multi(const PMMulti &m, const float4 *pos, uint32_t n, float4 *acc,
+                              cudaStream_t stream, int *launches);
+
+// Index of the box whose range [pbeg[b], pbeg[b+1]) holds i (pbeg[0] = 0).
+__device__ __forceinline__ int find_box(const uint32_t *__restrict__ pbeg, int nbox, uint32_t i) {
+    int lo = 0, hi = nbox;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&pbeg[mid]) <= i)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
 // ------------------------------------------------------------ integrator
 
 cuco_status_t launch_drift_keys(float4 *pos, const float4 *vel, double drift, float boxsize,
                                 bool do_drift, uint32_t *keys, uint32_t n, float gridfac, int G,
                                 cudaStream_t stream);
+
+// Fixed-point positions (uint32 per axis, units of L / 2^32, bit patterns in
+// the float4 slots) from and to float triplets; float triplets <-> float4.
+cuco_status_t to_fixed(const float *a, float4 *b, uint32_t n, float boxsize, cudaStream_t stream);
+cuco_status_t from_fixed(const float4 *b, float *a, uint32_t n, float boxsize, cudaStream_t stream);
+cuco_status_t pack3to4(const float *a, float4 *b, uint32_t n, cudaStream_t stream);
+cuco_status_t unpack4to3(const float4 *b, float *a, uint32_t n, cudaStream_t stream);
+
+// The reference's erfc split table T[i] (gravlist.cpp:56-67), FP64 -> float.
+void shortrange_table(float *t);
 
 // Host FP64 cosmological integrals.
 double cosmo_integral(double a0, double a1, double omega0, double omega_lambda, double hubble,

@@ -1,0 +1,660 @@
+// Batched form: many independent boxes advanced together, one launch per
+// phase.  No counterpart in the reference, which runs one box per process.
+//
+// Layout.  All boxes' particles are concatenated (box b owns [pbeg[b],
+// pbeg[b+1])), and so are their cells: a particle's key is the box's first
+// cell (cell_base) plus its cell in the box.  One stable radix sort of those
+// keys therefore sorts every box at once and keeps each box's particles in
+// its own range; one reorder builds every box's cell offsets.  Each PM phase
+// is one launch over all boxes' meshes (a per-CTA (box, block) map), and the
+// short range is one launch over all boxes' segments (a segment prefix
+// table).  The per-step factors of every box (drift, kicks) sit in a small
+// device array refreshed from pinned host memory at the start of the step, so
+// a whole step is one CUDA graph.
+//
+// Autotuning.  A box's short-range cell grid G (cell_grid = 0) and its FFT
+// batching (columns per CTA) are chosen by timing candidates on a scratch box
+// of the same particle count and mesh with uniform positions; results are
+// cached per (n, M, mode), since R = ceil(rcut / w) depends only on G / M.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cuco {
+
+namespace {
+
+struct DriftBox {
+    uint32_t G, cell_base;
+    float boxsize, gridfac;
+};
+
+struct StepFactors {
+    float units_per_time;  // fixed point: drift * 2^32 / L; plain: the drift factor
+    float pad;
+    double kick_pp, kick_pm;
+};
+
+__global__ void k_drift_keys_multi(float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                                   uint32_t *__restrict__ keys, uint32_t n, const uint32_t *__restrict__ pbeg,
+                                   int nbox, const DriftBox *__restrict__ boxes,
+                                   const StepFactors *__restrict__ f, int do_drift, int fixed) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = find_box(pbeg, nbox, i);
+    const DriftBox d = boxes[b];
+    const float4 p = pos[i];
+    uint32_t k[3];
+    if (fixed) {
+        // the precision form's drift: one rounding to the 2^-32 L grid, then a
+        // modular add (exact periodic wrap); key floor(x * G / 2^32)
+        uint32_t c[3] = {__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z)};
+        if (do_drift) {
+            const float4 v = vel[i];
+            const float vv[3] = {v.x, v.y, v.z};
+            const float upt = f[b].units_per_time;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) c[a] += (uint32_t)__float2ll_rn(vv[a] * upt);
+            pos[i] = make_float4(__uint_as_float(c[0]), __uint_as_float(c[1]), __uint_as_float(c[2]), p.w);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) k[a] = (uint32_t)(((uint64_t)c[a] * d.G) >> 32);
+    } else {
+        // the plain form's drift and wrap (predict.c:19,34-38) and key rule
+        // (gravlist_kernel.cu:108-113), as the single-box engine does them
+        float c[3] = {p.x, p.y, p.z};
+        if (do_drift) {
+            const float4 v = vel[i];
+            const float vv[3] = {v.x, v.y, v.z};
+            const float dt = f[b].units_per_time;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                float x = __fmaf_rn(vv[a], dt, c[a]);
+                for (int it = 0; it < 8 && x < 0.f; ++it) x = __fadd_rn(x, d.boxsize);
+                for (int it = 0; it < 8 && x >= d.boxsize; ++it) x = __fsub_rn(x, d.boxsize);
+                c[a] = x;
+            }
+            pos[i] = make_float4(c[0], c[1], c[2], p.w);
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            int v = (int)__fmul_rn(d.gridfac, c[a]);
+            v = v < 0 ? 0 : v;
+            k[a] = (uint32_t)(v >= (int)d.G ? d.G - 1 : v);
+        }
+    }
+    keys[i] = d.cell_base + (k[0] * d.G + k[1]) * d.G + k[2];
+}
+
+int key_bits(uint64_t ncells) {
+    int b = 1;
+    while ((1ull << b) < ncells) ++b;
+    return b;
+}
+
+template <typename T>
+cuco_status_t dalloc(T **p, size_t count) {
+    cudaError_t e = cudaMalloc(p, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        return CUCO_ERR_NOMEM;
+    }
+    return CUCO_OK;
+}
+
+ShortRangeParams sr_params(const cuco_config_t &c, uint32_t n, uint32_t cell_base) {
+    ShortRangeParams p{};
+    p.boxsize = c.boxsize;
+    p.gridfac = (float)c.cell_grid / c.boxsize;
+    p.cellw = c.boxsize / c.cell_grid;
+    p.rcut = c.rcut;
+    p.rcut2 = c.rcut * c.rcut;
+    p.asmthfac_d = 0.5 / (double)c.asmth * (kNTab / 3.0);
+    p.asmthfac = (float)p.asmthfac_d;
+    p.mass = c.mass;
+    p.G = (float)c.G;
+    p.h = c.softening;
+    p.hinv = (float)(1.0 / (double)c.softening);
+    p.h3inv = p.hinv * p.hinv * p.hinv;
+    p.grid = c.cell_grid;
+    p.n = n;
+    p.fixed = c.mode == CUCO_MODE_FIXED;
+    p.fscale = ldexpf(c.boxsize, -32);
+    p.cell_base = cell_base;
+    return p;
+}
+
+// ------------------------------------------------------------ autotuner
+
+struct Tuned {
+    int cell_grid, P, B;
+};
+
+std::mutex g_tune_mu;
+std::map<std::tuple<int64_t, int, int>, Tuned> g_tune_cache;
+
+// Shortest measured short-range time among the admissible cell grids.
+int tune_cell_grid(const cuco_config_t &c0, cudaStream_t stream) {
+    std::vector<int> cand;
+    for (int div : {2, 3, 4, 5, 6, 8}) {
+        const int G = std::max(8, c0.pm_grid / div);
+        if (std::find(cand.begin(), cand.end(), G) == cand.end()) cand.push_back(G);
+    }
+    const uint32_t n = (uint32_t)c0.n;
+    std::vector<float> pos(3 * (size_t)n);
+    uint64_t s = 0x9E3779B97F4A7C15ull ^ (uint64_t)n;
+    for (auto &x : pos) {  // seeded uniform positions (xorshift)
+        s ^= s << 13, s ^= s >> 7, s ^= s << 17;
+        x = (float)((double)(s >> 11) * (1.0 / 9007199254740992.0) * c0.boxsize);
+        if (x >= c0.boxsize) x = 0.f;
+    }
+    int best = -1;
+    float best_ms = 1e30f;
+    for (int G : cand) {
+        cuco_config_t c = c0;
+        c.cell_grid = G;
+        cuco_box_t *b = nullptr;
+        if (cuco_box_create(&c, &b) != CUCO_OK) continue;
+        float ms = 1e30f;
+        if (cuco_box_set_state(b, pos.data(), nullptr, 0) == CUCO_OK && cuco_box_enable_timing(b, 1) == CUCO_OK) {
+            bool ok = cuco_box_forces(b, 0, 1) == CUCO_OK;  // warm-up
+            for (int r = 0; ok && r < 2; ++r) {
+                float t[8];
+                ok = cuco_box_forces(b, 0, 1) == CUCO_OK && cuco_box_timings(b, t) == CUCO_OK;
+                if (ok) ms = std::min(ms, t[6]);
+            }
+        }
+        cuco_box_destroy(b);
+        if (ms < best_ms) best_ms = ms, best = G;
+    }
+    (void)stream;
+    return best;
+}
+
+// FFT batching (columns per CTA) by timing one-box multi launches.
+void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out, int *B_out) {
+    *P_out = pm_batch_z(M);
+    *B_out = pm_batch_axis(M);
+    const size_t Mh = M / 2 + 1;
+    float *rho = nullptr, *green = nullptr;
+    float2 *spec = nullptr, *tw = nullptr;
+    PMBoxDesc *dd = nullptr;
+    uint32_t *pbeg = nullptr;
+    uint2 *mz = nullptr, *ma = nullptr;
+    bool ok = dalloc(&rho, (size_t)M * M * M) == CUCO_OK && dalloc(&spec, (size_t)M * M * Mh) == CUCO_OK &&
+              dalloc(&green, Mh) == CUCO_OK && dalloc(&tw, (size_t)M) == CUCO_OK && dalloc(&dd, 1) == CUCO_OK &&
+              dalloc(&pbeg, 2) == CUCO_OK && dalloc(&mz, (size_t)M * M) == CUCO_OK &&
+              dalloc(&ma, (size_t)M * Mh) == CUCO_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ok) {
+        std::vector<float> g(Mh);
+        std::vector<float2> t(M);
+        pm_tables(M, boxsize, asmth, g.data(), t.data());
+        cudaMemcpy(green, g.data(), sizeof(float) * Mh, cudaMemcpyHostToDevice);
+        cudaMemcpy(tw, t.data(), sizeof(float2) * M, cudaMemcpyHostToDevice);
+        cudaMemset(rho, 0, sizeof(float) * (size_t)M * M * M);
+        const uint32_t pb[2] = {0, 0};
+        cudaMemcpy(pbeg, pb, sizeof pb, cudaMemcpyHostToDevice);
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 1e30f;
+        for (int P : {1, 2, 4, 8, 16}) {
+            if (P > M / 2 || (M * M / 2) % P || pm_smem_z(M, P) > 200 * 1024) continue;
+            for (int B : {4, 8, 16}) {
+                if (pm_smem_axis(M, B) > 200 * 1024) continue;
+                PMBoxDesc d{M, P, B, 1.f, 0.f, 0.f, rho, spec, green, tw};
+                cudaMemcpy(dd, &d, sizeof d, cudaMemcpyHostToDevice);
+                const uint32_t nz = (uint32_t)(M * M / (2 * P)), nbx = (uint32_t)((Mh + B - 1) / B),
+                               na = nbx * M;
+                std::vector<uint2> vz(nz), va(na);
+                for (uint32_t k = 0; k < nz; ++k) vz[k] = make_uint2(0, k);
+                for (uint32_t k = 0; k < na; ++k) va[k] = make_uint2(0, k);
+                cudaMemcpy(mz, vz.data(), sizeof(uint2) * nz, cudaMemcpyHostToDevice);
+                cudaMemcpy(ma, va.data(), sizeof(uint2) * na, cudaMemcpyHostToDevice);
+                PMMulti m{1, false, dd, pbeg, mz, ma, nz, na, pm_smem_z(M, P), pm_smem_axis(M, B), rho,
+                          (size_t)M * M * M};
+                if (pm_forces_multi(m, nullptr, 0, nullptr, stream, nullptr) != CUCO_OK) continue;  // warm-up
+                cudaEventRecord(e0, stream);
+                for (int r = 0; r < 3; ++r) pm_forces_multi(m, nullptr, 0, nullptr, stream, nullptr);
+                cudaEventRecord(e1, stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess) continue;
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) best = ms, *P_out = P, *B_out = B;
+            }
+        }
+    }
+    cudaGetLastError();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(rho), cudaFree(spec), cudaFree(green), cudaFree(tw), cudaFree(dd), cudaFree(pbeg), cudaFree(mz),
+        cudaFree(ma);
+}
+
+}  // namespace
+}  // namespace cuco
+
+using namespace cuco;
+
+struct cuco_ensemble {
+    int nbox = 0;
+    int device = 0;
+    bool fixed = false;
+    cudaStream_t stream = nullptr;
+    std::vector<cuco_config_t> cfg;
+    std::vector<uint32_t> pbeg;  // host copy, nbox+1
+    std::vector<int> P, B;
+    uint32_t n = 0;
+    uint64_t ncells = 0;
+    int key_bits = 0;
+    // particles, concatenated
+    float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr, *spos = nullptr,
+           *acc_pm_s = nullptr;
+    uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr, *hist = nullptr,
+             *cell_off = nullptr, *sorted_perm = nullptr;
+    float *stage3 = nullptr;
+    // meshes, concatenated
+    float *rho = nullptr, *green = nullptr, *table = nullptr;
+    float2 *spec = nullptr, *tw = nullptr;
+    // descriptors
+    uint32_t *d_pbeg = nullptr, *d_segbase = nullptr;
+    DriftBox *d_drift = nullptr;
+    PMBoxDesc *d_pm = nullptr;
+    uint2 *d_mapz = nullptr, *d_mapa = nullptr;
+    void *d_sr = nullptr;
+    double2 *d_kicks = nullptr;
+    StepFactors *d_factors = nullptr, *h_factors = nullptr;  // h_factors: pinned
+    double2 *h_kicks = nullptr;                               // pinned
+    PMMulti pm{};
+    uint32_t segments = 0;
+    size_t sr_smem = 0;
+    unsigned long long *pair_counter = nullptr;
+    bool count_pairs = false;
+    bool has_state = false;
+    int launches = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+namespace {
+
+// One force pass (and kicks when kick != 0), enqueued on e->stream.
+cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
+    e->launches = 0;
+    if (e->n) {
+        k_drift_keys_multi<<<(e->n + 255) / 256, 256, 0, e->stream>>>(e->pos, e->vel, e->keys, e->n, e->d_pbeg,
+                                                                     e->nbox, e->d_drift, e->d_factors, do_drift,
+                                                                     e->fixed ? 1 : 0);
+        CUCO_TRY_CUDA(cudaGetLastError());
+        e->launches++;
+    }
+    bool in_alt = false;
+    CUCO_TRY(sort_pairs(e->keys, e->perm, nullptr, e->keys_alt, e->perm_alt, e->hist, e->n, e->key_bits, 8,
+                        e->stream, &in_alt, &e->launches));
+    const uint32_t *skeys = in_alt ? e->keys_alt : e->keys;
+    e->sorted_perm = in_alt ? e->perm_alt : e->perm;
+    CUCO_TRY(launch_reorder_offsets(e->cell_off, e->spos, skeys, e->sorted_perm, e->pos, e->n, (uint32_t)e->ncells,
+                                    e->stream));
+    e->launches++;
+    CUCO_TRY(pm_forces_multi(e->pm, e->spos, e->n, e->acc_pm_s, e->stream, &e->launches));
+    KickArgs k{};
+    k.vel = kick ? e->vel : nullptr;
+    k.acc_pm_s = e->acc_pm_s;
+    k.acc_pm_out = e->acc_pm;
+    CUCO_TRY(launch_shortrange_multi(e->d_sr, e->d_kicks, e->d_segbase, e->nbox, e->segments, e->sr_smem, e->fixed,
+                                     e->spos, e->sorted_perm, e->cell_off, e->table, e->acc_pp, k, e->stream,
+                                     e->count_pairs ? e->pair_counter : nullptr));
+    e->launches++;
+    return CUCO_OK;
+}
+
+cuco_status_t upload_factors(cuco_ensemble *e) {
+    CUCO_TRY_CUDA(cudaMemcpyAsync(e->d_factors, e->h_factors, sizeof(StepFactors) * e->nbox,
+                                  cudaMemcpyHostToDevice, e->stream));
+    CUCO_TRY_CUDA(cudaMemcpyAsync(e->d_kicks, e->h_kicks, sizeof(double2) * e->nbox, cudaMemcpyHostToDevice,
+                                  e->stream));
+    return CUCO_OK;
+}
+
+void drop_graph(cuco_ensemble *e) {
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->exec = nullptr;
+    e->graph = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_ensemble_t **out) {
+    if (!boxes || nbox <= 0 || !out) {
+        set_error("cuco_ensemble_create: need at least one box");
+        return CUCO_ERR_INVALID;
+    }
+    for (int b = 0; b < nbox; ++b) {
+        const cuco_config_t &c = boxes[b];
+        if (c.mode != boxes[0].mode || c.device != boxes[0].device) {
+            set_error("cuco_ensemble_create: all boxes share one mode and one device");
+            return CUCO_ERR_INVALID;
+        }
+        if (c.n < 0 || !(c.boxsize > 0) || !(c.rcut > 0) || !(c.asmth > 0) || !(c.softening > 0) ||
+            c.cell_grid < 0 || c.cell_grid > 1024) {
+            set_error("cuco_ensemble_create: invalid box configuration");
+            return CUCO_ERR_INVALID;
+        }
+        if (!pm_mesh_supported(c.pm_grid)) {
+            set_error("cuco_ensemble_create: a mesh is not even, in [8, 1024] and 5-smooth");
+            return CUCO_ERR_UNSUPPORTED;
+        }
+    }
+    CUCO_TRY_CUDA(cudaSetDevice(boxes[0].device));
+    cuco_ensemble *e = new cuco_ensemble();
+    e->nbox = nbox;
+    e->device = boxes[0].device;
+    e->fixed = boxes[0].mode == CUCO_MODE_FIXED;
+    e->cfg.assign(boxes, boxes + nbox);
+    auto fail = [&](cuco_status_t s) {
+        cuco_ensemble_destroy(e);
+        return s;
+    };
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        delete e;
+        return CUCO_ERR_CUDA;
+    }
+    // autotune: cell grid and FFT batching per (n, M, mode)
+    e->P.resize(nbox);
+    e->B.resize(nbox);
+    for (int b = 0; b < nbox; ++b) {
+        cuco_config_t &c = e->cfg[b];
+        const auto key = std::make_tuple(c.n, c.pm_grid, (int)c.mode);
+        Tuned t{};
+        bool cached;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(key);
+            cached = it != g_tune_cache.end();
+            if (cached) t = it->second;
+        }
+        if (!cached) {
+            t.cell_grid = tune_cell_grid(c, e->stream);
+            tune_fft(c.pm_grid, c.boxsize, c.asmth, e->stream, &t.P, &t.B);
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tune_cache[key] = t;
+        }
+        if (c.cell_grid <= 0) {
+            if (t.cell_grid <= 0) {
+                set_error("cuco_ensemble_create: no admissible cell grid for a box");
+                return fail(CUCO_ERR_UNSUPPORTED);
+            }
+            c.cell_grid = t.cell_grid;
+        }
+        e->P[b] = t.P;
+        e->B[b] = t.B;
+    }
+    // sizes and offsets
+    e->pbeg.assign(nbox + 1, 0);
+    std::vector<uint64_t> cbase(nbox + 1, 0), mbase(nbox + 1, 0), sbase(nbox + 1, 0), gbase(nbox + 1, 0),
+        tbase(nbox + 1, 0);
+    for (int b = 0; b < nbox; ++b) {
+        const cuco_config_t &c = e->cfg[b];
+        const uint64_t M = c.pm_grid, G = c.cell_grid;
+        e->pbeg[b + 1] = e->pbeg[b] + (uint32_t)c.n;
+        cbase[b + 1] = cbase[b] + G * G * G;
+        mbase[b + 1] = mbase[b] + M * M * M;
+        sbase[b + 1] = sbase[b] + M * M * (M / 2 + 1);
+        gbase[b + 1] = gbase[b] + (M / 2 + 1);
+        tbase[b + 1] = tbase[b] + M;
+    }
+    if (cbase[nbox] >= 0xffffffffull || e->pbeg[nbox] > 0xfffffff0u) {
+        set_error("cuco_ensemble_create: more than 2^32 cells or particles in total");
+        return fail(CUCO_ERR_UNSUPPORTED);
+    }
+    e->n = e->pbeg[nbox];
+    e->ncells = cbase[nbox];
+    e->key_bits = key_bits(e->ncells);
+    const size_t n = e->n;
+    size_t maxn = 0;
+    for (int b = 0; b < nbox; ++b) maxn = std::max(maxn, (size_t)e->cfg[b].n);
+    cuco_status_t s;
+    if ((s = dalloc(&e->pos, n)) || (s = dalloc(&e->vel, n)) || (s = dalloc(&e->acc_pp, n)) ||
+        (s = dalloc(&e->acc_pm, n)) || (s = dalloc(&e->spos, n)) || (s = dalloc(&e->acc_pm_s, n)) ||
+        (s = dalloc(&e->keys, n)) || (s = dalloc(&e->perm, n)) || (s = dalloc(&e->keys_alt, n)) ||
+        (s = dalloc(&e->perm_alt, n)) || (s = dalloc(&e->hist, sort_hist_entries(e->n, e->key_bits, 8))) ||
+        (s = dalloc(&e->cell_off, e->ncells + 1)) || (s = dalloc(&e->stage3, 3 * maxn)) ||
+        (s = dalloc(&e->rho, mbase[nbox])) || (s = dalloc(&e->spec, sbase[nbox])) ||
+        (s = dalloc(&e->green, gbase[nbox])) || (s = dalloc(&e->tw, tbase[nbox])) ||
+        (s = dalloc(&e->table, kNTab)) || (s = dalloc(&e->d_pbeg, nbox + 1)) ||
+        (s = dalloc(&e->d_segbase, nbox + 1)) || (s = dalloc(&e->d_drift, nbox)) || (s = dalloc(&e->d_pm, nbox)) ||
+        (s = dalloc(&e->d_kicks, nbox)) || (s = dalloc(&e->d_factors, nbox)) ||
+        (s = dalloc(&e->pair_counter, 1)))
+        return fail(s);
+    if (cudaMalloc(&e->d_sr, shortrange_desc_bytes() * nbox) != cudaSuccess ||
+        cudaMallocHost(&e->h_factors, sizeof(StepFactors) * nbox) != cudaSuccess ||
+        cudaMallocHost(&e->h_kicks, sizeof(double2) * nbox) != cudaSuccess) {
+        set_error("cuco_ensemble_create: allocation failed");
+        return fail(CUCO_ERR_NOMEM);
+    }
+    memset(e->h_factors, 0, sizeof(StepFactors) * nbox);
+    memset(e->h_kicks, 0, sizeof(double2) * nbox);
+    // tables and descriptors
+    std::vector<float> tab(kNTab);
+    shortrange_table(tab.data());
+    std::vector<DriftBox> drift(nbox);
+    std::vector<PMBoxDesc> pmd(nbox);
+    std::vector<char> srd(shortrange_desc_bytes() * nbox);
+    std::vector<uint32_t> segbase(nbox + 1, 0);
+    std::vector<uint2> mapz, mapa;
+    size_t smz = 0, sma = 0;
+    for (int b = 0; b < nbox; ++b) {
+        const cuco_config_t &c = e->cfg[b];
+        const int M = c.pm_grid, Mh = M / 2 + 1;
+        drift[b] = DriftBox{(uint32_t)c.cell_grid, (uint32_t)cbase[b], c.boxsize, (float)c.cell_grid / c.boxsize};
+        std::vector<float> g(Mh);
+        std::vector<float2> t(M);
+        pm_tables(M, c.boxsize, c.asmth, g.data(), t.data());
+        if (cudaMemcpy(e->green + gbase[b], g.data(), sizeof(float) * Mh, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(e->tw + tbase[b], t.data(), sizeof(float2) * M, cudaMemcpyHostToDevice) != cudaSuccess) {
+            set_error("cuco_ensemble_create: table upload failed");
+            return fail(CUCO_ERR_CUDA);
+        }
+        pmd[b] = PMBoxDesc{M, e->P[b], e->B[b], (float)M / c.boxsize, c.mass, pm_fd_fac(M, c.boxsize, c.G),
+                           e->rho + mbase[b], e->spec + sbase[b], e->green + gbase[b], e->tw + tbase[b]};
+        const uint32_t nz = (uint32_t)(M * M / (2 * e->P[b]));
+        for (uint32_t k = 0; k < nz; ++k) mapz.push_back(make_uint2(b, k));
+        const uint32_t na = (uint32_t)((Mh + e->B[b] - 1) / e->B[b]) * M;
+        for (uint32_t k = 0; k < na; ++k) mapa.push_back(make_uint2(b, k));
+        smz = std::max(smz, pm_smem_z(M, e->P[b]));
+        sma = std::max(sma, pm_smem_axis(M, e->B[b]));
+        uint32_t nseg = 0;
+        size_t sm = 0;
+        if ((s = shortrange_desc_fill(sr_params(c, (uint32_t)c.n, (uint32_t)cbase[b]),
+                                      srd.data() + b * shortrange_desc_bytes(), &nseg, &sm)))
+            return fail(s);
+        segbase[b + 1] = segbase[b] + nseg;
+        e->sr_smem = std::max(e->sr_smem, sm);
+    }
+    e->segments = segbase[nbox];
+    if ((s = dalloc(&e->d_mapz, mapz.size())) || (s = dalloc(&e->d_mapa, mapa.size()))) return fail(s);
+    if (cudaMemcpy(e->table, tab.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_pbeg, e->pbeg.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_segbase, segbase.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_drift, drift.data(), sizeof(DriftBox) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_pm, pmd.data(), sizeof(PMBoxDesc) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_sr, srd.data(), srd.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_mapz, mapz.data(), sizeof(uint2) * mapz.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_mapa, mapa.data(), sizeof(uint2) * mapa.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(e->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(e->vel, 0, sizeof(float4) * (n ? n : 1)) != cudaSuccess ||
+        cudaMemset(e->pos, 0, sizeof(float4) * (n ? n : 1)) != cudaSuccess) {
+        set_error("cuco_ensemble_create: descriptor upload failed");
+        return fail(CUCO_ERR_CUDA);
+    }
+    e->pm = PMMulti{nbox, e->fixed, e->d_pm, e->d_pbeg, e->d_mapz, e->d_mapa, (uint32_t)mapz.size(),
+                    (uint32_t)mapa.size(), smz, sma, e->rho, (size_t)mbase[nbox]};
+    cudaEventCreate(&e->t0);
+    cudaEventCreate(&e->t1);
+    *out = e;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
+    if (!e) return CUCO_OK;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    drop_graph(e);
+    for (void *p : {(void *)e->pos, (void *)e->vel, (void *)e->acc_pp, (void *)e->acc_pm, (void *)e->spos,
+                    (void *)e->acc_pm_s, (void *)e->keys, (void *)e->perm, (void *)e->keys_alt, (void *)e->perm_alt,
+                    (void *)e->hist, (void *)e->cell_off, (void *)e->stage3, (void *)e->rho, (void *)e->spec,
+                    (void *)e->green, (void *)e->tw, (void *)e->table, (void *)e->d_pbeg, (void *)e->d_segbase,
+                    (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, e->d_sr,
+                    (void *)e->d_kicks, (void *)e->d_factors, (void *)e->pair_counter})
+        cudaFree(p);
+    if (e->h_factors) cudaFreeHost(e->h_factors);
+    if (e->h_kicks) cudaFreeHost(e->h_kicks);
+    if (e->t0) cudaEventDestroy(e->t0);
+    if (e->t1) cudaEventDestroy(e->t1);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_cell_grid(cuco_ensemble_t *e, int box, int *cell_grid, int *fft_p, int *fft_b) {
+    if (!e || box < 0 || box >= e->nbox) {
+        set_error("cuco_ensemble_cell_grid: no such box");
+        return CUCO_ERR_INVALID;
+    }
+    if (cell_grid) *cell_grid = e->cfg[box].cell_grid;
+    if (fft_p) *fft_p = e->P[box];
+    if (fft_b) *fft_b = e->B[box];
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_set_state(cuco_ensemble_t *e, int box, const float *pos, const float *vel) {
+    if (!e || box < 0 || box >= e->nbox || !pos) {
+        set_error("cuco_ensemble_set_state: invalid argument");
+        return CUCO_ERR_INVALID;
+    }
+    const uint32_t b0 = e->pbeg[box], nb = e->pbeg[box + 1] - b0;
+    const size_t bytes = sizeof(float) * 3 * nb;
+    CUCO_TRY_CUDA(cudaMemcpyAsync(e->stage3, pos, bytes, cudaMemcpyHostToDevice, e->stream));
+    if (e->fixed)
+        CUCO_TRY(to_fixed(e->stage3, e->pos + b0, nb, e->cfg[box].boxsize, e->stream));
+    else
+        CUCO_TRY(pack3to4(e->stage3, e->pos + b0, nb, e->stream));
+    if (vel) {
+        CUCO_TRY_CUDA(cudaMemcpyAsync(e->stage3, vel, bytes, cudaMemcpyHostToDevice, e->stream));
+        CUCO_TRY(pack3to4(e->stage3, e->vel + b0, nb, e->stream));
+    }
+    CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    e->has_state = true;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_get_state(cuco_ensemble_t *e, int box, float *pos, float *vel, float *acc_pp,
+                                      float *acc_pm) {
+    if (!e || box < 0 || box >= e->nbox) {
+        set_error("cuco_ensemble_get_state: invalid argument");
+        return CUCO_ERR_INVALID;
+    }
+    const uint32_t b0 = e->pbeg[box], nb = e->pbeg[box + 1] - b0;
+    float *dst[4] = {pos, vel, acc_pp, acc_pm};
+    float4 *src[4] = {e->pos, e->vel, e->acc_pp, e->acc_pm};
+    for (int k = 0; k < 4; ++k) {
+        if (!dst[k]) continue;
+        if (k == 0 && e->fixed)
+            CUCO_TRY(from_fixed(src[k] + b0, e->stage3, nb, e->cfg[box].boxsize, e->stream));
+        else
+            CUCO_TRY(unpack4to3(src[k] + b0, e->stage3, nb, e->stream));
+        CUCO_TRY_CUDA(cudaMemcpyAsync(dst[k], e->stage3, sizeof(float) * 3 * nb, cudaMemcpyDeviceToHost, e->stream));
+        CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    }
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_forces(cuco_ensemble_t *e) {
+    if (!e || !e->has_state) {
+        set_error("cuco_ensemble_forces: no state uploaded");
+        return CUCO_ERR_STATE;
+    }
+    CUCO_TRY(ensemble_pass(e, 0, false));
+    CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_step(cuco_ensemble_t *e, const double *drift, const double *kick_pp,
+                                 const double *kick_pm) {
+    if (!e || !e->has_state || !drift || !kick_pp || !kick_pm) {
+        set_error("cuco_ensemble_step: no state uploaded or null factors");
+        return CUCO_ERR_STATE;
+    }
+    // the previous replay may still read the pinned factors
+    if (e->exec) CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    for (int b = 0; b < e->nbox; ++b) {
+        const double L = e->cfg[b].boxsize;
+        e->h_factors[b].units_per_time = (float)(e->fixed ? drift[b] * 4294967296.0 / L : drift[b]);
+        e->h_kicks[b] = make_double2(kick_pp[b], kick_pm[b]);
+    }
+    if (!e->exec) {
+        // first step: run once outside capture (one-time kernel attributes),
+        // then capture the step as a graph for the following ones
+        CUCO_TRY(upload_factors(e));
+        CUCO_TRY(ensemble_pass(e, 1, true));
+        CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+        CUCO_TRY_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        cuco_status_t s1 = upload_factors(e);
+        cuco_status_t s2 = s1 == CUCO_OK ? ensemble_pass(e, 1, true) : s1;
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
+        if (s2 != CUCO_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s2;
+        }
+        CUCO_TRY_CUDA(ce);
+        e->graph = g;
+        CUCO_TRY_CUDA(cudaGraphInstantiate(&e->exec, e->graph, 0));
+        return CUCO_OK;
+    }
+    CUCO_TRY_CUDA(cudaGraphLaunch(e->exec, e->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_sync(cuco_ensemble_t *e) {
+    if (!e) return CUCO_ERR_INVALID;
+    CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_timer(cuco_ensemble_t *e, int op, float *ms) {
+    if (!e) return CUCO_ERR_INVALID;
+    if (op == 0) {
+        CUCO_TRY_CUDA(cudaEventRecord(e->t0, e->stream));
+    } else {
+        CUCO_TRY_CUDA(cudaEventRecord(e->t1, e->stream));
+        CUCO_TRY_CUDA(cudaEventSynchronize(e->t1));
+        CUCO_TRY_CUDA(cudaEventElapsedTime(ms, e->t0, e->t1));
+    }
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_count_pairs(cuco_ensemble_t *e, int enable, uint64_t *pairs) {
+    if (!e) return CUCO_ERR_INVALID;
+    CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    if (pairs) CUCO_TRY_CUDA(cudaMemcpy(pairs, e->pair_counter, sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    CUCO_TRY_CUDA(cudaMemset(e->pair_counter, 0, sizeof(unsigned long long)));
+    if ((bool)enable != e->count_pairs) drop_graph(e);  // the captured launch differs
+    e->count_pairs = enable != 0;
+    return CUCO_OK;
+}
+
+int cuco_ensemble_launches_per_step(cuco_ensemble_t *e) { return e ? e->launches : 0; }
+
+}  // extern "C"

@@ -20,8 +20,8 @@
 //                  (pm_periodic.c:272-309), fused: the three force grids the
 //                  reference builds are never materialised.
 // All transforms are unnormalised with cuFFT's sign conventions; each 1D
-// transform is a shared-memory Stockham radix-4 (one radix-2 stage when
-// log2 M is odd) over a batch of columns, twiddles from an FP64-built table.
+// transform is a shared-memory Stockham FFT over a batch of columns with
+// radix-4/2/3/5 stages (M = 2^a 3^b 5^c), twiddles from an FP64-built table.
 // The Green's function factorises: smth(k) = -g(kx) g(ky) g(kz) / k^2 with
 // g(k) = exp(-k^2 (2 pi asmth / L)^2) / sinc(pi k / M)^4, built in FP64.
 #include <cmath>
@@ -40,56 +40,77 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// Stage radix for the remaining length: 4, 2, 3 or 5 (M = 2^a 3^b 5^c).
+__device__ __forceinline__ int stage_radix(int rem) {
+    return (rem & 3) == 0 ? 4 : (rem & 1) == 0 ? 2 : rem % 3 == 0 ? 3 : 5;
+}
+
 // Transform B columns of length M held in x[m*pitch + b]; returns the buffer
-// holding the result.  sign = -1: forward (e^{-i}), +1: inverse.
+// holding the result.  sign = -1: forward (e^{-i}), +1: inverse.  Stockham
+// autosort: stage with radix r over Ns already-combined points reads
+// x[j + p*M/r] (p < r), twiddles it by w^{p k M/(Ns r)} (k = j mod Ns), and
+// writes the r-point DFT to y[(j/Ns) Ns r + k + q Ns].
 __device__ float2 *fft_columns(float2 *x, float2 *y, const float2 *tw, int M, int B, int pitch,
                                int sign) {
     int Ns = 1;
     float2 *in = x, *out = y;
     while (Ns < M) {
-        const int r = ((M / Ns) & 3) == 0 ? 4 : 2;
+        const int r = stage_radix(M / Ns);
         const int nb = M / r;
         const int step = M / (Ns * r);
         for (int e = threadIdx.x; e < nb * B; e += blockDim.x) {
             const int b = e % B, j = e / B;
             const int k = j % Ns;
             const int dst = (j / Ns) * Ns * r + k;
-            if (r == 4) {
-                float2 v0 = in[j * pitch + b];
-                float2 v1 = in[(j + nb) * pitch + b];
-                float2 v2 = in[(j + 2 * nb) * pitch + b];
-                float2 v3 = in[(j + 3 * nb) * pitch + b];
-                if (k) {
-                    float2 w1 = tw[k * step], w2 = tw[2 * k * step], w3 = tw[3 * k * step];
-                    if (sign > 0) {
-                        w1.y = -w1.y;
-                        w2.y = -w2.y;
-                        w3.y = -w3.y;
-                    }
-                    v1 = cmul(v1, w1);
-                    v2 = cmul(v2, w2);
-                    v3 = cmul(v3, w3);
+            float2 v[5];
+            for (int q = 0; q < r; ++q) v[q] = in[(j + q * nb) * pitch + b];
+            if (k) {
+                for (int q = 1; q < r; ++q) {
+                    float2 w = tw[q * k * step];
+                    if (sign > 0) w.y = -w.y;
+                    v[q] = cmul(v[q], w);
                 }
-                float2 a0 = make_float2(v0.x + v2.x, v0.y + v2.y);
-                float2 a1 = make_float2(v0.x - v2.x, v0.y - v2.y);
-                float2 a2 = make_float2(v1.x + v3.x, v1.y + v3.y);
-                float2 d = make_float2(v1.x - v3.x, v1.y - v3.y);
+            }
+            if (r == 4) {
+                const float2 a0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
+                const float2 a1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
+                const float2 a2 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
+                const float2 d = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
                 // (v1 - v3) * (sign * i)
-                float2 a3 = sign < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+                const float2 a3 = sign < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
                 out[dst * pitch + b] = make_float2(a0.x + a2.x, a0.y + a2.y);
                 out[(dst + Ns) * pitch + b] = make_float2(a1.x + a3.x, a1.y + a3.y);
                 out[(dst + 2 * Ns) * pitch + b] = make_float2(a0.x - a2.x, a0.y - a2.y);
                 out[(dst + 3 * Ns) * pitch + b] = make_float2(a1.x - a3.x, a1.y - a3.y);
+            } else if (r == 2) {
+                out[dst * pitch + b] = make_float2(v[0].x + v[1].x, v[0].y + v[1].y);
+                out[(dst + Ns) * pitch + b] = make_float2(v[0].x - v[1].x, v[0].y - v[1].y);
+            } else if (r == 3) {
+                // y1,2 = v0 - (v1+v2)/2 +- i s (v1-v2), s = sign sqrt(3)/2
+                const float s3 = sign * 0.866025403784438647f;
+                const float2 t = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
+                const float2 d = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
+                const float2 m = make_float2(v[0].x - 0.5f * t.x, v[0].y - 0.5f * t.y);
+                out[dst * pitch + b] = make_float2(v[0].x + t.x, v[0].y + t.y);
+                out[(dst + Ns) * pitch + b] = make_float2(m.x - s3 * d.y, m.y + s3 * d.x);
+                out[(dst + 2 * Ns) * pitch + b] = make_float2(m.x + s3 * d.y, m.y - s3 * d.x);
             } else {
-                float2 v0 = in[j * pitch + b];
-                float2 v1 = in[(j + nb) * pitch + b];
-                if (k) {
-                    float2 w1 = tw[k * step];
-                    if (sign > 0) w1.y = -w1.y;
-                    v1 = cmul(v1, w1);
-                }
-                out[dst * pitch + b] = make_float2(v0.x + v1.x, v0.y + v1.y);
-                out[(dst + Ns) * pitch + b] = make_float2(v0.x - v1.x, v0.y - v1.y);
+                // five-point DFT by the conjugate pairs (1,4), (2,3)
+                const float c1 = 0.309016994374947424f, c2 = -0.809016994374947424f;
+                const float s1 = sign * 0.951056516295153572f, s2 = sign * 0.587785252292473129f;
+                const float2 a1 = make_float2(v[1].x + v[4].x, v[1].y + v[4].y);
+                const float2 b1 = make_float2(v[1].x - v[4].x, v[1].y - v[4].y);
+                const float2 a2 = make_float2(v[2].x + v[3].x, v[2].y + v[3].y);
+                const float2 b2 = make_float2(v[2].x - v[3].x, v[2].y - v[3].y);
+                const float2 t1 = make_float2(v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y);
+                const float2 t2 = make_float2(v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y);
+                const float2 u1 = make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+                const float2 u2 = make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+                out[dst * pitch + b] = make_float2(v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y);
+                out[(dst + Ns) * pitch + b] = make_float2(t1.x - u1.y, t1.y + u1.x);      // t1 + i u1
+                out[(dst + 2 * Ns) * pitch + b] = make_float2(t2.x - u2.y, t2.y + u2.x);  // t2 + i u2
+                out[(dst + 3 * Ns) * pitch + b] = make_float2(t2.x + u2.y, t2.y - u2.x);  // t2 - i u2
+                out[(dst + 4 * Ns) * pitch + b] = make_float2(t1.x + u1.y, t1.y - u1.x);  // t1 - i u1
             }
         }
         __syncthreads();
@@ -106,14 +127,13 @@ __device__ __forceinline__ void load_twiddles(float2 *tw_s, const float2 *tw, in
 }
 
 // rows r0 .. r0+2P-1 of the M^3 real grid (row = x*M + y) -> spectrum rows
-__global__ void __launch_bounds__(kFFTThreads)
-    k_fft_z_r2c(const float *__restrict__ rho, float2 *__restrict__ spec, const float2 *tw, int M,
-                int P) {
+__device__ __forceinline__ void fft_z_r2c(const float *__restrict__ rho, float2 *__restrict__ spec,
+                                          const float2 *tw, int M, int P, int blk) {
     extern __shared__ float2 sm[];
     const int pitch = P + 1;
     float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
     const int Mh = M / 2 + 1;
-    const size_t r0 = (size_t)blockIdx.x * 2 * P;
+    const size_t r0 = (size_t)blk * 2 * P;
     load_twiddles(tw_s, tw, M);
     // kLoadBatch loads in flight per thread before their shared-memory stores
     for (int e0 = threadIdx.x; e0 < 2 * P * M; e0 += kLoadBatch * blockDim.x) {
@@ -149,14 +169,13 @@ __global__ void __launch_bounds__(kFFTThreads)
     }
 }
 
-__global__ void __launch_bounds__(kFFTThreads)
-    k_fft_z_c2r(const float2 *__restrict__ spec, float *__restrict__ out, const float2 *tw, int M,
-                int P) {
+__device__ __forceinline__ void fft_z_c2r(const float2 *__restrict__ spec, float *__restrict__ out,
+                                          const float2 *tw, int M, int P, int blk) {
     extern __shared__ float2 sm[];
     const int pitch = P + 1;
     float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
     const int Mh = M / 2 + 1;
-    const size_t r0 = (size_t)blockIdx.x * 2 * P;
+    const size_t r0 = (size_t)blk * 2 * P;
     load_twiddles(tw_s, tw, M);
     // rows into y as h[row*Mh + k]
     for (int e0 = threadIdx.x; e0 < 2 * P * Mh; e0 += kLoadBatch * blockDim.x) {
@@ -200,17 +219,18 @@ __global__ void __launch_bounds__(kFFTThreads)
     }
 }
 
-// axis 1: y transform for fixed x = blockIdx.y; axis 0: x transform for fixed
-// y = blockIdx.y, with the Green's multiply and inverse transform when green != 0.
-__global__ void __launch_bounds__(kFFTThreads)
-    k_fft_axis(float2 *__restrict__ spec, const float2 *tw, const float *__restrict__ green1d,
-               int M, int B, int axis, int sign, int green) {
+// axis 1: y transform for fixed x = by; axis 0: x transform for fixed y = by,
+// with the Green's multiply and inverse transform when green != 0; columns
+// kz0 = bx * B ...
+__device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2 *tw,
+                                         const float *__restrict__ green1d, int M, int B, int axis,
+                                         int sign, int green, int bx, int by) {
     extern __shared__ float2 sm[];
     const int pitch = B;
     float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
     const int Mh = M / 2 + 1;
-    const int o = blockIdx.y;
-    const int kz0 = blockIdx.x * B;
+    const int o = by;
+    const int kz0 = bx * B;
     const int nb = min(B, Mh - kz0);
     const size_t sm_stride = axis == 1 ? (size_t)Mh : (size_t)M * Mh;
     const size_t base = axis == 1 ? (size_t)o * M * Mh : (size_t)o * Mh;
@@ -257,6 +277,46 @@ __global__ void __launch_bounds__(kFFTThreads)
     }
 }
 
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_z_r2c(const float *__restrict__ rho, float2 *__restrict__ spec, const float2 *tw, int M, int P) {
+    fft_z_r2c(rho, spec, tw, M, P, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_z_c2r(const float2 *__restrict__ spec, float *__restrict__ out, const float2 *tw, int M, int P) {
+    fft_z_c2r(spec, out, tw, M, P, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_axis(float2 *__restrict__ spec, const float2 *tw, const float *__restrict__ green1d, int M, int B,
+               int axis, int sign, int green) {
+    fft_axis(spec, tw, green1d, M, B, axis, sign, green, blockIdx.x, blockIdx.y);
+}
+
+// Many boxes in one launch: map[blockIdx.x] = (box, the box's own block index).
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_z_r2c_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
+    const uint2 m = map[blockIdx.x];
+    const PMBoxDesc &d = boxes[m.x];
+    fft_z_r2c(d.rho, d.spec, d.twiddle, d.M, d.P, m.y);
+}
+
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_z_c2r_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
+    const uint2 m = map[blockIdx.x];
+    const PMBoxDesc &d = boxes[m.x];
+    fft_z_c2r(d.spec, d.rho, d.twiddle, d.M, d.P, m.y);
+}
+
+__global__ void __launch_bounds__(kFFTThreads)
+    k_fft_axis_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map, int axis, int sign,
+                     int green) {
+    const uint2 m = map[blockIdx.x];
+    const PMBoxDesc &d = boxes[m.x];
+    const int nbx = (d.M / 2 + 1 + d.B - 1) / d.B;
+    fft_axis(d.spec, d.twiddle, d.green1d, d.M, d.B, axis, sign, green, m.y % nbx, m.y / nbx);
+}
+
 __device__ __forceinline__ void cic_axis(float to_slab_fac, float p, int M, int *s, int *ss,
                                          float *d) {
     float t = __fmul_rn(to_slab_fac, p);  // pm_periodic.c:99 in float
@@ -293,11 +353,8 @@ __device__ __forceinline__ void cic_point(const float4 &p, float to_slab_fac, in
 }
 
 template <bool FIXED>
-__global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__restrict__ rho,
-                          int M, float to_slab_fac, float mass) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 p = pos[i];
+__device__ __forceinline__ void deposit_one(float4 p, float *__restrict__ rho, int M, float to_slab_fac,
+                                            float mass) {
     int s[3][2];
     float d[3];
     cic_point<FIXED>(p, to_slab_fac, M, s, d);
@@ -318,11 +375,8 @@ __global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__r
 __device__ __forceinline__ int wrapi(int a, int M) { return a < 0 ? a + M : (a >= M ? a - M : a); }
 
 template <bool FIXED>
-__global__ void k_interp(const float4 *__restrict__ pos, uint32_t n, const float *__restrict__ phi,
-                         int M, float to_slab_fac, float fac, float4 *__restrict__ acc) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 p = pos[i];
+__device__ __forceinline__ float4 interp_one(float4 p, const float *__restrict__ phi, int M, float to_slab_fac,
+                                             float fac) {
     int s[3][2];
     float d[3];
     cic_point<FIXED>(p, to_slab_fac, M, s, d);
@@ -353,7 +407,39 @@ __global__ void k_interp(const float4 *__restrict__ pos, uint32_t n, const float
                 }
         out[dim] = a;
     }
-    acc[i] = make_float4(out[0], out[1], out[2], 0.f);
+    return make_float4(out[0], out[1], out[2], 0.f);
+}
+
+template <bool FIXED>
+__global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__restrict__ rho,
+                          int M, float to_slab_fac, float mass) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) deposit_one<FIXED>(pos[i], rho, M, to_slab_fac, mass);
+}
+
+template <bool FIXED>
+__global__ void k_interp(const float4 *__restrict__ pos, uint32_t n, const float *__restrict__ phi,
+                         int M, float to_slab_fac, float fac, float4 *__restrict__ acc) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) acc[i] = interp_one<FIXED>(pos[i], phi, M, to_slab_fac, fac);
+}
+
+template <bool FIXED>
+__global__ void k_deposit_multi(const float4 *__restrict__ pos, uint32_t n, const PMBoxDesc *__restrict__ boxes,
+                                const uint32_t *__restrict__ pbeg, int nbox) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PMBoxDesc &d = boxes[find_box(pbeg, nbox, i)];
+    deposit_one<FIXED>(pos[i], d.rho, d.M, d.to_slab_fac, d.mass);
+}
+
+template <bool FIXED>
+__global__ void k_interp_multi(const float4 *__restrict__ pos, uint32_t n, const PMBoxDesc *__restrict__ boxes,
+                               const uint32_t *__restrict__ pbeg, int nbox, float4 *__restrict__ acc) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PMBoxDesc &d = boxes[find_box(pbeg, nbox, i)];
+    acc[i] = interp_one<FIXED>(pos[i], d.rho, d.M, d.to_slab_fac, d.fd_fac);
 }
 
 int fft_batch_z(int M) {
@@ -375,10 +461,80 @@ int fft_batch_axis(int M) {
 
 }  // namespace
 
+int pm_batch_z(int M) { return fft_batch_z(M); }
+int pm_batch_axis(int M) { return fft_batch_axis(M); }
+
+void pm_tables(int M, float boxsize, float asmth, float *green1d, float2 *twiddle) {
+    const size_t Mh = M / 2 + 1;
+    double asmth2 = (2 * M_PI) * (double)asmth / (double)boxsize;
+    asmth2 *= asmth2;
+    for (size_t k = 0; k < Mh; ++k) {
+        double e = exp(-(double)(k * k) * asmth2);
+        double f = 1.0;
+        if (k) {
+            f = (M_PI * (double)k) / M;
+            f = sin(f) / f;
+        }
+        green1d[k] = (float)(e / (f * f * f * f));
+    }
+    for (int t = 0; t < M; ++t)
+        twiddle[t] = make_float2((float)cos(2 * M_PI * t / M), (float)-sin(2 * M_PI * t / M));
+}
+
+float pm_fd_fac(int M, float boxsize, double G) {
+    double fac = G / (M_PI * (double)boxsize);
+    fac *= (double)(1.0f / (2.0f * boxsize / (float)M));
+    return (float)fac;
+}
+
+size_t pm_smem_z(int M, int P) { return sizeof(float2) * (2 * (size_t)M * (P + 1) + M); }
+size_t pm_smem_axis(int M, int B) { return sizeof(float2) * (2 * (size_t)M * B + M); }
+
+cuco_status_t pm_forces_multi(const PMMulti &m, const float4 *pos, uint32_t n, float4 *acc,
+                              cudaStream_t stream, int *launches) {
+    static bool attr = [] {
+        const int mx = 227 * 1024;
+        cudaFuncSetAttribute(k_fft_z_r2c_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(k_fft_z_c2r_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        cudaFuncSetAttribute(k_fft_axis_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        return true;
+    }();
+    (void)attr;
+    CUCO_TRY_CUDA(cudaMemsetAsync(m.rho_all, 0, sizeof(float) * m.rho_all_count, stream));
+    if (n) {
+        if (m.fixed)
+            k_deposit_multi<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox);
+        else
+            k_deposit_multi<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox);
+    }
+    k_fft_z_r2c_multi<<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
+    k_fft_axis_multi<<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, 1, -1, 0);
+    k_fft_axis_multi<<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, 0, -1, 1);
+    k_fft_axis_multi<<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, 1, +1, 0);
+    k_fft_z_c2r_multi<<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
+    if (n) {
+        if (m.fixed)
+            k_interp_multi<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox, acc);
+        else
+            k_interp_multi<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox, acc);
+    }
+    CUCO_TRY_CUDA(cudaGetLastError());
+    if (launches) *launches += 7;
+    return CUCO_OK;
+}
+
+bool pm_mesh_supported(int M) {
+    if (M < 8 || M > 1024 || (M & 1)) return false;
+    int r = M;
+    for (int f : {2, 3, 5})
+        while (r % f == 0) r /= f;
+    return r == 1;
+}
+
 cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, float mass,
                              double G, bool fixed) {
-    if (M < 8 || M > 1024 || (M & (M - 1))) {
-        set_error("PM mesh size must be a power of two in [8, 1024]");
+    if (!pm_mesh_supported(M)) {
+        set_error("PM mesh size must be even, in [8, 1024], with no prime factor above 5");
         return CUCO_ERR_UNSUPPORTED;
     }
     plan->M = M;

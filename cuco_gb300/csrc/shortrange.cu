@@ -39,6 +39,8 @@
 // L < 2^23) and dx exact for ~97% of pairs; pairs whose r^2 lies within
 // 4e-7 of rcut^2 or whose asmthfac*r lies within 4e-7 (relative) of a bin edge
 // are decided in double as gravlist.cpp:298-320 does.
+#include <cstring>
+
 #include "common.cuh"
 
 namespace cuco {
@@ -60,6 +62,12 @@ struct ColumnSet {
     float margin;  // culling slack for the float cell assignment (length units)
     signed char dx[kMaxCols];
     signed char dy[kMaxCols];
+};
+
+// One box of a multi-box launch.
+struct SRBoxDesc {
+    ShortRangeParams p;
+    ColumnSet cs;
 };
 
 struct Run {
@@ -116,13 +124,14 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
+// The kernel body for one segment `seg` of one box (p, cs); kick_pp/kick_pm
+// are that box's kick factors.
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
-__global__ void __launch_bounds__(kThreads, 4)
-    k_shortrange(ShortRangeParams p, ColumnSet cs, const float4 *__restrict__ spos,
-                 const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
-                 const uint32_t *__restrict__ cb, const float *__restrict__ table_g,
-                 float4 *__restrict__ acc_out, KickArgs kick,
-                 unsigned long long *__restrict__ pair_counter) {
+__device__ __forceinline__ void shortrange_segment(
+    const ShortRangeParams &p, const ColumnSet &cs, const int seg, const double kick_pp, const double kick_pm,
+    const float4 *__restrict__ spos, const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
+    const uint32_t *__restrict__ cb, const float *__restrict__ table_g, float4 *__restrict__ acc_out,
+    const KickArgs &kick, unsigned long long *__restrict__ pair_counter) {
     extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
     __shared__ uint32_t s_wdelta[kWarps][32];
@@ -140,7 +149,6 @@ __global__ void __launch_bounds__(kThreads, 4)
     uint32_t *coltot = reinterpret_cast<uint32_t *>(runs + 2 * ncols);
 
     const int segs = G / S;
-    const int seg = blockIdx.x;
     const int ix = seg / (G * segs);
     const int iy = (seg / segs) % G;
     const int iz0 = (seg % segs) * S;
@@ -155,7 +163,7 @@ __global__ void __launch_bounds__(kThreads, 4)
         int cy = cyu < 0 ? cyu + G : (cyu >= G ? cyu - G : cyu);
         int cz = czu < 0 ? czu + G : (czu >= G ? czu - G : czu);
         uint32_t st, cn;
-        cell_range<FMT>(ca, cb, ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
+        cell_range<FMT>(ca, cb, p.cell_base + ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
         cst[e] = st;
         ccn[e] = cn;
     }
@@ -188,8 +196,8 @@ __global__ void __launch_bounds__(kThreads, 4)
     // per column: staged offsets of its z-cells, runs of consecutive cells with one shift
     for (int col = tid; col < ncols; col += kThreads) {
         int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
-        const float x0 = cxu * p.cellw, y0 = cyu * p.cellw;
-        cgeo[col] = make_float4(x0, x0 + p.cellw, y0, y0 + p.cellw);
+        const float x0 = __fmul_rn((float)cxu, p.cellw), y0 = __fmul_rn((float)cyu, p.cellw);
+        cgeo[col] = make_float4(x0, __fadd_rn(x0, p.cellw), y0, __fadd_rn(y0, p.cellw));
         float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
         float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
         uint32_t acc = 0;
@@ -328,10 +336,11 @@ __global__ void __launch_bounds__(kThreads, 4)
         if (r < hh) {
             const float u = r * hinv;
             if (u < 0.5f)
-                fac = h3inv * (10.66667f + u * u * (32.0f * u - 38.4f));
+                fac = __fmul_rn(h3inv, __fmaf_rn(__fmul_rn(u, u), __fmaf_rn(32.0f, u, -38.4f), 10.66667f));
             else
-                fac = h3inv * (21.33333f - 48.0f * u + 38.4f * u * u - 10.66667f * u * u * u -
-                               0.06667f / (u * u * u));
+                fac = __fmul_rn(h3inv, __fsub_rn(__fmaf_rn(u, __fmaf_rn(u, __fmaf_rn(-10.66667f, u, 38.4f), -48.0f),
+                                                           21.33333f),
+                                                 __fdiv_rn(0.06667f, __fmul_rn(__fmul_rn(u, u), u))));
         }
         fac = ok ? fac * tab[min(ti, kNTab - 1)] : 0.f;
         ax = __fmaf_rn(dx, fac, ax);
@@ -351,8 +360,9 @@ __global__ void __launch_bounds__(kThreads, 4)
         // to float: the culling margin covers it); tx..tz: origin-relative
         float4 pt = praw;
         if (FIXED) {
-            pt = make_float4((float)__float_as_uint(praw.x) * fs, (float)__float_as_uint(praw.y) * fs,
-                             (float)__float_as_uint(praw.z) * fs, 0.f);
+            pt = make_float4(__fmul_rn((float)__float_as_uint(praw.x), fs),
+                             __fmul_rn((float)__float_as_uint(praw.y), fs),
+                             __fmul_rn((float)__float_as_uint(praw.z), fs), 0.f);
             const float4 tr = rel(praw);
             tx = tr.x;
             ty = tr.y;
@@ -398,11 +408,14 @@ __global__ void __launch_bounds__(kThreads, 4)
                     const float4 g = cgeo[col];
                     const float ddx = fmaxf(fmaxf(g.x - pt.x, pt.x - g.y), 0.f);
                     const float ddy = fmaxf(fmaxf(g.z - pt.y, pt.y - g.w), 0.f);
-                    const float q = rc2m - (ddx * ddx + ddy * ddy);
+                    // explicit roundings: the candidate set (hence the lane each
+                    // candidate lands on) must not depend on how the compiler
+                    // contracts this expression in a given instantiation
+                    const float q = __fsub_rn(rc2m, __fmaf_rn(ddy, ddy, __fmul_rn(ddx, ddx)));
                     if (q >= 0.f) {
                         // half-height of the cut disc over this column (an
                         // approximate square root: the margin covers it)
-                        const float hz = q * rsqrtf(fmaxf(q, 1e-30f));
+                        const float hz = __fmul_rn(q, rsqrtf(fmaxf(q, 1e-30f)));
                         const int zlo = max(__float2int_rd(__fmaf_rn(pt.z - hz, winv, -zbase)), 0);
                         const int zhi = min(__float2int_rd(__fmaf_rn(pt.z + hz, winv, -zbase)), nz - 1);
                         if (zlo <= zhi) {
@@ -515,7 +528,7 @@ __global__ void __launch_bounds__(kThreads, 4)
                 float4 v = kick.vel[o];
                 // vel += GravAccel*dt; vel += GravPM*dt (timestep.c:57-58,88), in
                 // float (the reference rounds each product to float first)
-                const float kp = (float)kick.kick_pp, km = (float)kick.kick_pm;
+                const float kp = (float)kick_pp, km = (float)kick_pm;
                 v.x += __fmul_rn(a.x, kp);
                 v.y += __fmul_rn(a.y, kp);
                 v.z += __fmul_rn(a.z, kp);
@@ -533,6 +546,35 @@ __global__ void __launch_bounds__(kThreads, 4)
         for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
         if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
     }
+}
+
+template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
+__global__ void __launch_bounds__(kThreads, 4)
+    k_shortrange(const __grid_constant__ ShortRangeParams p, const __grid_constant__ ColumnSet cs,
+                 const float4 *__restrict__ spos, const uint32_t *__restrict__ perm,
+                 const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
+                 const float *__restrict__ table_g, float4 *__restrict__ acc_out,
+                 const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
+    shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, blockIdx.x, kick.kick_pp, kick.kick_pm, spos, perm, ca,
+                                                cb, table_g, acc_out, kick, pair_counter);
+}
+
+// Many boxes in one launch: segments numbered box after box (seg_base, nbox+1
+// entries); particles, cells (p.cell_base) and outputs are the concatenated
+// arrays of all boxes.
+template <bool KICK, bool COUNT, bool FIXED>
+__global__ void __launch_bounds__(kThreads, 4)
+    k_shortrange_multi(const SRBoxDesc *__restrict__ boxes, const double2 *__restrict__ kicks,
+                       const uint32_t *__restrict__ seg_base, int nbox, const float4 *__restrict__ spos,
+                       const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cell_off,
+                       const float *__restrict__ table_g, float4 *__restrict__ acc_out,
+                       const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
+    const int b = find_box(seg_base, nbox, blockIdx.x);
+    const SRBoxDesc &d = boxes[b];
+    const double2 k = KICK ? kicks[b] : make_double2(0.0, 0.0);
+    shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, d.cs, (int)(blockIdx.x - seg_base[b]), k.x, k.y,
+                                                         spos, perm, cell_off, nullptr, table_g, acc_out, kick,
+                                                         pair_counter);
 }
 
 // Neighbour columns (dx, dy) whose xy cell distance is within rcut (+margin).
@@ -627,6 +669,65 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
         else
             launch_fmt_kick<kCellStartEnd, false, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     }
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
+
+size_t shortrange_desc_bytes() { return sizeof(SRBoxDesc); }
+
+cuco_status_t shortrange_desc_fill(const ShortRangeParams &p, void *desc, uint32_t *segments, size_t *smem) {
+    SRBoxDesc d{};
+    d.p = p;
+    if (!build_columns(p, &d.cs)) {
+        set_error("short range: cell grid does not fit rcut (need rcut <= 8 cell widths, "
+                  "rcut < L/2 and at least S+2R cells per dimension)");
+        return CUCO_ERR_UNSUPPORTED;
+    }
+    memcpy(desc, &d, sizeof d);
+    *segments = (uint32_t)p.grid * p.grid * (p.grid / d.cs.S);
+    *smem = smem_bytes(d.cs.ncols, d.cs.S + 2 * d.cs.R);
+    return CUCO_OK;
+}
+
+cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, const uint32_t *seg_base,
+                                      int nbox, uint32_t segments, size_t smem, bool fixed,
+                                      const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
+                                      const float *table, float4 *acc_out, const KickArgs &kick,
+                                      cudaStream_t stream, unsigned long long *pair_counter) {
+    static const size_t sm_max = smem_bytes(kMaxCols, kMaxSeg + 2 * kMaxR);
+    static bool attr = [] {
+        cudaFuncSetAttribute(k_shortrange_multi<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        cudaFuncSetAttribute(k_shortrange_multi<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+        return true;
+    }();
+    (void)attr;
+    if (!segments) return CUCO_OK;
+    const SRBoxDesc *d = static_cast<const SRBoxDesc *>(descs);
+    const bool kick_on = kick.vel != nullptr;
+#define CUCO_SR_MULTI(K, C, F)                                                                              \
+    k_shortrange_multi<K, C, F><<<segments, kThreads, smem, stream>>>(d, kicks, seg_base, nbox, sorted_pos, \
+                                                                     perm, cell_off, table, acc_out, kick,   \
+                                                                     pair_counter)
+    if (fixed) {
+        if (kick_on) {
+            if (pair_counter) CUCO_SR_MULTI(true, true, true); else CUCO_SR_MULTI(true, false, true);
+        } else {
+            if (pair_counter) CUCO_SR_MULTI(false, true, true); else CUCO_SR_MULTI(false, false, true);
+        }
+    } else {
+        if (kick_on) {
+            if (pair_counter) CUCO_SR_MULTI(true, true, false); else CUCO_SR_MULTI(true, false, false);
+        } else {
+            if (pair_counter) CUCO_SR_MULTI(false, true, false); else CUCO_SR_MULTI(false, false, false);
+        }
+    }
+#undef CUCO_SR_MULTI
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
 }

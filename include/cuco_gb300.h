@@ -267,6 +267,39 @@ cuco_status_t cuco_box_timer(cuco_box_t *box, int op, float *ms);
 cuco_status_t cuco_pinned_alloc(size_t bytes, void **ptr);
 cuco_status_t cuco_pinned_free(void *ptr);
 
+/* ---- Batched form (no counterpart in the reference) ---------------------
+ * Many independent boxes advanced together: every phase of a step (drift and
+ * keys, sort, reorder, each PM pass, short range and kick) is one launch over
+ * all boxes, and cuco_ensemble_step replays the whole step as one CUDA graph.
+ * Each box is described by a cuco_config_t (all boxes share mode and device;
+ * meshes even, 8..1024, no prime factor above 5).  cell_grid = 0 lets the
+ * autotuner pick the box's short-range cell grid by timing candidates on a
+ * scratch box of the same size; FFT batching is always tuned.  Tuning results
+ * are cached per (n, pm_grid, mode) for the life of the process. */
+typedef struct cuco_ensemble cuco_ensemble_t;
+cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_ensemble_t **ensemble);
+cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *ensemble);
+/* the cell grid and FFT batching (z-pass row pairs, axis-pass columns per CTA) in use */
+cuco_status_t cuco_ensemble_cell_grid(cuco_ensemble_t *ensemble, int box, int *cell_grid, int *fft_p,
+                                      int *fft_b);
+/* host float triplets, as cuco_box_set_state / cuco_box_get_state */
+cuco_status_t cuco_ensemble_set_state(cuco_ensemble_t *ensemble, int box, const float *pos, const float *vel);
+cuco_status_t cuco_ensemble_get_state(cuco_ensemble_t *ensemble, int box, float *pos, float *vel,
+                                      float *acc_pp, float *acc_pm);
+/* forces at the current positions (synchronous) */
+cuco_status_t cuco_ensemble_forces(cuco_ensemble_t *ensemble);
+/* one step of every box: drift[b], kick_pp[b], kick_pm[b] as cuco_box_step
+ * (asynchronous; the first call also captures the graph) */
+cuco_status_t cuco_ensemble_step(cuco_ensemble_t *ensemble, const double *drift, const double *kick_pp,
+                                 const double *kick_pm);
+cuco_status_t cuco_ensemble_sync(cuco_ensemble_t *ensemble);
+/* op 0: mark a start on the ensemble's stream; op 1: ms since the mark */
+cuco_status_t cuco_ensemble_timer(cuco_ensemble_t *ensemble, int op, float *ms);
+/* returns (and resets) the in-range pairs counted so far; enable turns the
+ * in-kernel count on or off for the following passes */
+cuco_status_t cuco_ensemble_count_pairs(cuco_ensemble_t *ensemble, int enable, uint64_t *pairs);
+int cuco_ensemble_launches_per_step(cuco_ensemble_t *ensemble);
+
 /* Stable sort of (keys, values) by the low key_bits bits, in place, that
  * allocates no device memory (no counterpart in the reference).  For callers
  * that must not allocate where they sort: cudaMalloc/cudaFree can synchronize

@@ -296,9 +296,26 @@ typedef struct {
     double re, im;
 } dcpx;
 
-/* In-place radix-2 transform of n (a power of two) points `stride` apart. */
+/* In-place transform of n points `stride` apart: radix-2 for a power of two,
+ * else the DFT by its definition, X_k = sum_j a_j w^(j k mod n) (the meshes
+ * the reference supports are powers of two; the others serve the engine's
+ * batched form, whose meshes are 2 x the particle grid). */
 static void fft_line(dcpx *a, int n, int64_t stride, int sign, dcpx *buf, const dcpx *tw) {
     for (int i = 0; i < n; ++i) buf[i] = a[i * stride];
+    if (n & (n - 1)) {
+        for (int k = 0; k < n; ++k) {
+            double re = 0, im = 0;
+            for (int j = 0; j < n; ++j) {
+                dcpx w = tw[(int)(((int64_t)j * k) % n)];
+                if (sign > 0) w.im = -w.im;
+                re += buf[j].re * w.re - buf[j].im * w.im;
+                im += buf[j].re * w.im + buf[j].im * w.re;
+            }
+            a[k * stride].re = re;
+            a[k * stride].im = im;
+        }
+        return;
+    }
     for (int i = 1, j = 0; i < n; ++i) {
         int bit = n >> 1;
         for (; j & bit; bit >>= 1) j ^= bit;

@@ -1,0 +1,113 @@
+"""The batched form (cuco_ensemble_*): many boxes in one launch per phase.
+
+Each box of an ensemble must get the forces it gets alone: the short range
+runs the same per-segment code on the same cell-ordered sources, so it is
+compared bit for bit with a single box of the same cell grid; the PM deposit
+uses float atomics, whose order differs between launches, so PM is compared
+at 1e-5 rms.  Meshes that are not powers of two (2 x the particle grid, as
+the batched workload has them) are checked against the oracle, whose FFT
+falls back to the DFT by definition for them.  Steps replayed from the
+captured graph must track single boxes stepped alone.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cuco_gb300 import Box, BoxConfig, fixed_step_schedule, ics
+from cuco_gb300.engine import MODE_FIXED
+from cuco_gb300.ensemble import Ensemble
+from conftest import rms_rel
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [(16, 32, 60.0, 1), (20, 40, 120.0, 2), (24, 48, 200.0, 3), (18, 36, 90.0, 4)]
+
+
+def soft(L, n_side):
+    return float(np.float32(2.8 * np.float32(0.025 * L * 1000.0 / n_side)))
+
+
+def make(specs, mode, cell_grid=None):
+    ics_, cfgs = [], []
+    for n_side, M, L, seed in specs:
+        ic = ics.zeldovich(n_side, L, 49.0, seed)
+        ics_.append(ic)
+        cfgs.append(BoxConfig(n=ic.n, pm_grid=M, boxsize=ic.boxsize, mass=ic.mass, G=ics.G_INTERNAL,
+                              softening=soft(L, n_side), mode=mode, cell_grid=cell_grid))
+    return ics_, cfgs
+
+
+def test_ensemble_forces_match_single_boxes():
+    ics_, cfgs = make(SPECS, MODE_FIXED)
+    ens = Ensemble(cfgs)
+    for b, ic in enumerate(ics_):
+        ens.set_state(b, ic.pos)
+    ens.forces()
+    for b, (ic, c) in enumerate(zip(ics_, cfgs)):
+        G, P, B = ens.plan(b)
+        assert G >= 8 and P >= 1 and B >= 1
+        _, _, app, apm = ens.get_state(b)
+        c1 = BoxConfig(**{**c.__dict__, "cell_grid": G})
+        box = Box(c1)
+        box.set_state(ic.pos)
+        box.forces()
+        _, _, app1, apm1 = box.get_state()
+        box.close()
+        assert np.array_equal(app, app1), f"box {b}: short range differs from the box alone"
+        assert rms_rel(apm, apm1) < 1e-5
+    ens.close()
+
+
+def test_ensemble_mixed_radix_meshes_vs_oracle(port):
+    specs = [(24, 48, 100.0, 5), (30, 60, 150.0, 6), (20, 40, 80.0, 7)]
+    ics_, cfgs = make(specs, 0)
+    ens = Ensemble(cfgs)
+    for b, ic in enumerate(ics_):
+        ens.set_state(b, ic.pos)
+    ens.forces()
+    for b, (ic, c) in enumerate(zip(ics_, cfgs)):
+        _, _, app, apm = ens.get_state(b)
+        p = oracle.reference_params(ic.boxsize, ic.mass, ics.G_INTERNAL, c.pm_grid, c.softening)
+        e_pp = rms_rel(app, port.pp(ic.pos, p, c.pm_grid // 2, 8))
+        e_pm = rms_rel(apm, port.pm(ic.pos, p, c.pm_grid, 8))
+        print(f"M={c.pm_grid}: pp {e_pp:.2e} pm {e_pm:.2e}")
+        assert e_pp < 1e-4 and e_pm < 1e-4
+    ens.close()
+
+
+def test_single_box_mixed_radix_pm_vs_oracle(port):
+    ic = ics.zeldovich(30, 100.0, 49.0, 9)
+    for M in (60, 90):
+        box = Box(BoxConfig(n=ic.n, pm_grid=M, boxsize=ic.boxsize, mass=ic.mass, G=ics.G_INTERNAL,
+                            softening=soft(100.0, 30), cell_grid=M // 4))
+        box.set_state(ic.pos)
+        box.forces(pm=True, pp=False)
+        apm = box.get_state()[3]
+        box.close()
+        p = oracle.reference_params(ic.boxsize, ic.mass, ics.G_INTERNAL, M, soft(100.0, 30))
+        assert rms_rel(apm, port.pm(ic.pos, p, M, 8)) < 1e-4
+
+
+def test_ensemble_graph_steps_track_single_boxes():
+    ics_, cfgs = make(SPECS, MODE_FIXED)
+    ens = Ensemble(cfgs)
+    for b, ic in enumerate(ics_):
+        ens.set_state(b, ic.pos, ic.canonical_velocity())
+    a, drift, kick = fixed_step_schedule(ics_[0].a, 0.05, 4)
+    for s in range(5):  # the first call captures the graph, the rest replay it
+        ens.step(drift[s], kick[s])
+    ens.sync()
+    for b, (ic, c) in enumerate(zip(ics_, cfgs)):
+        pos, vel, _, _ = ens.get_state(b)
+        box = Box(BoxConfig(**{**c.__dict__, "cell_grid": ens.plan(b)[0]}))
+        box.set_state(ic.pos, ic.canonical_velocity())
+        for s in range(5):
+            box.step(drift[s], kick[s])
+        pos1, vel1, _, _ = box.get_state()
+        box.close()
+        v0 = ic.canonical_velocity()
+        assert rms_rel(vel - v0, vel1 - v0) < 1e-4
+        dx = np.abs(pos - pos1)
+        dx = np.minimum(dx, ic.boxsize - dx)
+        assert dx.max() < 1e-5 * ic.boxsize
+    ens.close()
