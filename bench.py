@@ -63,6 +63,118 @@ PRESETS = {
 }
 
 
+BATCHED = "batched-64"
+
+
+def smooth5(n):
+    for f in (2, 3, 5):
+        while n % f == 0:
+            n //= f
+    return n == 1
+
+
+def batched_specs(nbox=64, seed=2024):
+    """Boxes of the batched workload: particle grid log-uniform over 16..96 per
+    side (rounded to the nearest integer with no prime factor above 5, so the
+    2x mesh suits the FFT), L uniform in 50..400 Mpc/h, seeds base+i."""
+    rng = np.random.default_rng(seed)
+    smooth = [k for k in range(16, 97) if smooth5(k)]
+    out = []
+    for i in range(nbox):
+        x = math.exp(rng.uniform(math.log(16), math.log(96)))
+        n_side = min(smooth, key=lambda k: abs(k - x))
+        out.append((n_side, 2 * n_side, float(rng.uniform(50.0, 400.0)), seed + 1 + i))
+    return out
+
+
+def run_batched(args, world, rank, local):
+    """Many boxes per launch (fixed-point form) against the same boxes stepped
+    one at a time on the plain path."""
+    from cuco_gb300 import Box, BoxConfig, ics
+    from cuco_gb300.engine import MODE_FIXED
+    from cuco_gb300.ensemble import Ensemble
+    specs = batched_specs()
+    ic_list, cfgs, sched = [], [], None
+    for n_side, M, L, seed in specs:
+        ic = ics.zeldovich(n_side, L, Z_INIT, seed)
+        ic_list.append(ic)
+        cfgs.append(BoxConfig(n=ic.n, pm_grid=M, boxsize=ic.boxsize, mass=ic.mass, G=ics.G_INTERNAL,
+                              softening=float(np.float32(2.8 * np.float32(SOFT_FRAC * ic.boxsize / n_side))),
+                              mode=MODE_FIXED, device=local))
+        if sched is None:
+            sched = schedule(ic)
+    a, drift, kick = sched
+    ntot = sum(ic.n for ic in ic_list)
+    K, W = args.steps, args.warmup
+    t0 = time.perf_counter()
+    ens = Ensemble(cfgs)
+    setup_s = time.perf_counter() - t0
+
+    def reset():
+        for b, ic in enumerate(ic_list):
+            ens.set_state(b, ic.pos, ic.canonical_velocity())
+
+    reset()
+    for s in range(W):
+        ens.step(drift[s], kick[s])
+    ens.sync()
+    reset()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    dist_barrier(world)
+    ens.sync()
+    ens.timer_start()
+    for s in range(K):
+        ens.step(drift[s], kick[s])
+    ms = ens.timer_stop()
+    ens.sync()
+    dist_barrier(world)
+    clk = clocks.stop()
+    t_total = dist_max(ms / 1e3, world)
+    value = world * ntot * K / t_total
+    launches = ens.launches()
+    plans = [ens.plan(b) for b in range(len(cfgs))]
+    ens.close()
+    # the same boxes, one at a time, plain path (default cell grid M/4)
+    Kb = min(K, args.baseline_steps)
+    t_plain = 0.0
+    lib = None
+    for ic, c in zip(ic_list, cfgs):
+        box = Box(BoxConfig(**{**c.__dict__, "mode": 0, "cell_grid": None}))
+        box.set_state(ic.pos, ic.canonical_velocity())
+        for s in range(W):
+            box.step(drift[s], kick[s])
+        box.set_state(ic.pos, ic.canonical_velocity())
+        box.sync()
+        lib = box.lib
+        lib.cuco_box_timer(box.h, 0, None)
+        for s in range(Kb):
+            box.step(drift[s], kick[s])
+        m = ctypes.c_float()
+        lib.cuco_box_timer(box.h, 1, ctypes.byref(m))
+        t_plain += m.value / 1e3
+        box.close()
+    plain_rate = ntot * Kb / t_plain
+    sizes = [sp[0] for sp in specs]
+    line = {
+        "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
+        "steps": K, "warmup": W, "ms_per_step": 1e3 * t_total / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic",
+        "config": {"workload": "batched-64boxes-N16to96-M2N-L50to400-z49", "boxes": len(specs),
+                   "particles": ntot, "n_side_min": min(sizes), "n_side_max": max(sizes),
+                   "positions": "uint32 fixed point (L/2^32)", "timed_steps": "steps 0..K-1 from z=49",
+                   "graph": "one CUDA graph per step, one launch per phase over all boxes"},
+        "one_at_a_time_plain": {"value": plain_rate, "unit": "particle-updates/s", "steps": Kb,
+                                "ratio": value / plain_rate},
+        "autotuned_plans": {"cell_grid": [p[0] for p in plans], "fft_rows_per_cta": [p[1] for p in plans],
+                            "fft_cols_per_cta": [p[2] for p in plans]},
+        "setup_s": setup_s, "clocks": clk, "gpu_launches": launches * K,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def apply_preset(name):
     global N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD
     N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD = PRESETS[name]
@@ -397,8 +509,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS))
+    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS) + [BATCHED])
+    ap.add_argument("--baseline-steps", type=int, default=20)
     args = ap.parse_args()
+    if args.workload == BATCHED:
+        args.warmup = max(args.warmup, 3)
+        world, rank, local = dist_setup()
+        run_batched(args, world, rank, local)
+        return
     apply_preset(args.workload)
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
