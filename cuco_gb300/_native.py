@@ -148,6 +148,8 @@ SIGNATURES = {
     "cuco_ensemble_timer": (_I, [_P, _I, ctypes.POINTER(ctypes.c_float)]),
     "cuco_ensemble_count_pairs": (_I, [_P, _I, _P]),
     "cuco_ensemble_launches_per_step": (_I, [_P]),
+    "cuco_ensemble_copy_state": (_I, [_P, _I, _P, _I]),
+    "cuco_ensemble_footprint": (_I, [ctypes.POINTER(CucoConfig), _I, _P]),
     "cuco_pinned_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "cuco_pinned_free": (_I, [_P]),
     "cuco_fp32_peak": (_I, [_I, ctypes.POINTER(_D)]),

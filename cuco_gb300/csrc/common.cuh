@@ -125,7 +125,8 @@ struct PMPlan {
     float to_slab_fac;  // M / L in float (pm_periodic.c:42)
     float mass;
     float fd_fac;       // G/(pi L) * M/(2L) (pm_periodic.c:85-86)
-    float *rho;         // M^3 real grid (density, then potential)
+    float *rho;         // M^3 real grid: the potential
+    unsigned long long *rho64;  // M^3 deposited mass in units of m / 2^32
     float2 *spec;       // M*M*(M/2+1) complex grid
     float *green1d;     // M/2+1: exp(-k^2 a) / sinc(pi k/M)^4
     float2 *twiddle;    // M: exp(-2 pi i t / M)
@@ -145,7 +146,9 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
 struct PMBoxDesc {
     int M, P, B;         // mesh; z-pass row pairs and axis-pass columns per CTA
     float to_slab_fac, mass, fd_fac;
-    float *rho;          // this box's M^3 real grid (density, then potential)
+    float *rho;          // this box's M^3 real grid (the potential)
+    unsigned long long *rho64;  // its deposited mass, units of m / 2^32
+    float mscale;        // m / 2^32
     float2 *spec;        // its M*M*(M/2+1) half spectrum
     const float *green1d;
     const float2 *twiddle;
@@ -159,7 +162,7 @@ struct PMMulti {
     const uint2 *map_axis;    // device: (box, block) per CTA of the y/x passes
     uint32_t nz_blocks, naxis_blocks;
     size_t smz, sma;          // dynamic shared memory of the z and axis passes
-    float *rho_all;           // all boxes' real grids, contiguous (one memset)
+    unsigned long long *rho64_all;  // all boxes' deposit grids, contiguous (one memset)
     size_t rho_all_count;
 };
 int pm_batch_z(int M);

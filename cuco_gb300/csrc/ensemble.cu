@@ -109,6 +109,33 @@ cuco_status_t dalloc(T **p, size_t count) {
     return CUCO_OK;
 }
 
+// Ensemble arrays come from the device's stream-ordered pool, which keeps
+// freed memory for reuse (release threshold raised once per device): a
+// serving loop rebuilds its ensemble whenever jobs join or leave, and must not
+// pay cudaMalloc/cudaFree each time.
+void pool_keep_memory(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    std::lock_guard<std::mutex> lk(mu);
+    if (device < 0 || device >= 64 || done[device]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done[device] = true;
+}
+
+template <typename T>
+cuco_status_t palloc(T **p, size_t count, cudaStream_t s) {
+    cudaError_t e = cudaMallocAsync((void **)p, sizeof(T) * (count ? count : 1), s);
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+        return CUCO_ERR_NOMEM;
+    }
+    return CUCO_OK;
+}
+
 ShortRangeParams sr_params(const cuco_config_t &c, uint32_t n, uint32_t cell_base) {
     ShortRangeParams p{};
     p.boxsize = c.boxsize;
@@ -184,11 +211,13 @@ void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out
     *B_out = pm_batch_axis(M);
     const size_t Mh = M / 2 + 1;
     float *rho = nullptr, *green = nullptr;
+    unsigned long long *rho64 = nullptr;
     float2 *spec = nullptr, *tw = nullptr;
     PMBoxDesc *dd = nullptr;
     uint32_t *pbeg = nullptr;
     uint2 *mz = nullptr, *ma = nullptr;
-    bool ok = dalloc(&rho, (size_t)M * M * M) == CUCO_OK && dalloc(&spec, (size_t)M * M * Mh) == CUCO_OK &&
+    bool ok = dalloc(&rho, (size_t)M * M * M) == CUCO_OK && dalloc(&rho64, (size_t)M * M * M) == CUCO_OK &&
+              dalloc(&spec, (size_t)M * M * Mh) == CUCO_OK &&
               dalloc(&green, Mh) == CUCO_OK && dalloc(&tw, (size_t)M) == CUCO_OK && dalloc(&dd, 1) == CUCO_OK &&
               dalloc(&pbeg, 2) == CUCO_OK && dalloc(&mz, (size_t)M * M) == CUCO_OK &&
               dalloc(&ma, (size_t)M * Mh) == CUCO_OK;
@@ -209,7 +238,7 @@ void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out
             if (P > M / 2 || (M * M / 2) % P || pm_smem_z(M, P) > 200 * 1024) continue;
             for (int B : {4, 8, 16}) {
                 if (pm_smem_axis(M, B) > 200 * 1024) continue;
-                PMBoxDesc d{M, P, B, 1.f, 0.f, 0.f, rho, spec, green, tw};
+                PMBoxDesc d{M, P, B, 1.f, 0.f, 0.f, rho, rho64, 1.f, spec, green, tw};
                 cudaMemcpy(dd, &d, sizeof d, cudaMemcpyHostToDevice);
                 const uint32_t nz = (uint32_t)(M * M / (2 * P)), nbx = (uint32_t)((Mh + B - 1) / B),
                                na = nbx * M;
@@ -218,7 +247,7 @@ void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out
                 for (uint32_t k = 0; k < na; ++k) va[k] = make_uint2(0, k);
                 cudaMemcpy(mz, vz.data(), sizeof(uint2) * nz, cudaMemcpyHostToDevice);
                 cudaMemcpy(ma, va.data(), sizeof(uint2) * na, cudaMemcpyHostToDevice);
-                PMMulti m{1, false, dd, pbeg, mz, ma, nz, na, pm_smem_z(M, P), pm_smem_axis(M, B), rho,
+                PMMulti m{1, false, dd, pbeg, mz, ma, nz, na, pm_smem_z(M, P), pm_smem_axis(M, B), rho64,
                           (size_t)M * M * M};
                 if (pm_forces_multi(m, nullptr, 0, nullptr, stream, nullptr) != CUCO_OK) continue;  // warm-up
                 cudaEventRecord(e0, stream);
@@ -234,7 +263,7 @@ void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out
     cudaGetLastError();
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    cudaFree(rho), cudaFree(spec), cudaFree(green), cudaFree(tw), cudaFree(dd), cudaFree(pbeg), cudaFree(mz),
+    cudaFree(rho), cudaFree(rho64), cudaFree(spec), cudaFree(green), cudaFree(tw), cudaFree(dd), cudaFree(pbeg), cudaFree(mz),
         cudaFree(ma);
 }
 
@@ -262,6 +291,7 @@ struct cuco_ensemble {
     float *stage3 = nullptr;
     // meshes, concatenated
     float *rho = nullptr, *green = nullptr, *table = nullptr;
+    unsigned long long *rho64 = nullptr;
     float2 *spec = nullptr, *tw = nullptr;
     // descriptors
     uint32_t *d_pbeg = nullptr, *d_segbase = nullptr;
@@ -426,19 +456,23 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
     size_t maxn = 0;
     for (int b = 0; b < nbox; ++b) maxn = std::max(maxn, (size_t)e->cfg[b].n);
     cuco_status_t s;
-    if ((s = dalloc(&e->pos, n)) || (s = dalloc(&e->vel, n)) || (s = dalloc(&e->acc_pp, n)) ||
-        (s = dalloc(&e->acc_pm, n)) || (s = dalloc(&e->spos, n)) || (s = dalloc(&e->acc_pm_s, n)) ||
-        (s = dalloc(&e->keys, n)) || (s = dalloc(&e->perm, n)) || (s = dalloc(&e->keys_alt, n)) ||
-        (s = dalloc(&e->perm_alt, n)) || (s = dalloc(&e->hist, sort_hist_entries(e->n, e->key_bits, 8))) ||
-        (s = dalloc(&e->cell_off, e->ncells + 1)) || (s = dalloc(&e->stage3, 3 * maxn)) ||
-        (s = dalloc(&e->rho, mbase[nbox])) || (s = dalloc(&e->spec, sbase[nbox])) ||
-        (s = dalloc(&e->green, gbase[nbox])) || (s = dalloc(&e->tw, tbase[nbox])) ||
-        (s = dalloc(&e->table, kNTab)) || (s = dalloc(&e->d_pbeg, nbox + 1)) ||
-        (s = dalloc(&e->d_segbase, nbox + 1)) || (s = dalloc(&e->d_drift, nbox)) || (s = dalloc(&e->d_pm, nbox)) ||
-        (s = dalloc(&e->d_kicks, nbox)) || (s = dalloc(&e->d_factors, nbox)) ||
-        (s = dalloc(&e->pair_counter, 1)))
+    pool_keep_memory(e->device);
+    cudaStream_t st = e->stream;
+    if ((s = palloc(&e->pos, n, st)) || (s = palloc(&e->vel, n, st)) || (s = palloc(&e->acc_pp, n, st)) ||
+        (s = palloc(&e->acc_pm, n, st)) || (s = palloc(&e->spos, n, st)) || (s = palloc(&e->acc_pm_s, n, st)) ||
+        (s = palloc(&e->keys, n, st)) || (s = palloc(&e->perm, n, st)) || (s = palloc(&e->keys_alt, n, st)) ||
+        (s = palloc(&e->perm_alt, n, st)) || (s = palloc(&e->hist, sort_hist_entries(e->n, e->key_bits, 8), st)) ||
+        (s = palloc(&e->cell_off, e->ncells + 1, st)) || (s = palloc(&e->stage3, 3 * maxn, st)) ||
+        (s = palloc(&e->rho, mbase[nbox], st)) || (s = palloc(&e->rho64, mbase[nbox], st)) ||
+        (s = palloc(&e->spec, sbase[nbox], st)) ||
+        (s = palloc(&e->green, gbase[nbox], st)) || (s = palloc(&e->tw, tbase[nbox], st)) ||
+        (s = palloc(&e->table, kNTab, st)) || (s = palloc(&e->d_pbeg, nbox + 1, st)) ||
+        (s = palloc(&e->d_segbase, nbox + 1, st)) || (s = palloc(&e->d_drift, nbox, st)) ||
+        (s = palloc(&e->d_pm, nbox, st)) || (s = palloc(&e->d_kicks, nbox, st)) ||
+        (s = palloc(&e->d_factors, nbox, st)) || (s = palloc(&e->pair_counter, 1, st)) ||
+        (s = palloc((char **)&e->d_sr, shortrange_desc_bytes() * nbox, st)))
         return fail(s);
-    if (cudaMalloc(&e->d_sr, shortrange_desc_bytes() * nbox) != cudaSuccess ||
+    if (cudaStreamSynchronize(st) != cudaSuccess ||
         cudaMallocHost(&e->h_factors, sizeof(StepFactors) * nbox) != cudaSuccess ||
         cudaMallocHost(&e->h_kicks, sizeof(double2) * nbox) != cudaSuccess) {
         set_error("cuco_ensemble_create: allocation failed");
@@ -468,7 +502,8 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
             return fail(CUCO_ERR_CUDA);
         }
         pmd[b] = PMBoxDesc{M, e->P[b], e->B[b], (float)M / c.boxsize, c.mass, pm_fd_fac(M, c.boxsize, c.G),
-                           e->rho + mbase[b], e->spec + sbase[b], e->green + gbase[b], e->tw + tbase[b]};
+                           e->rho + mbase[b], e->rho64 + mbase[b], ldexpf(c.mass, -32), e->spec + sbase[b],
+                           e->green + gbase[b], e->tw + tbase[b]};
         const uint32_t nz = (uint32_t)(M * M / (2 * e->P[b]));
         for (uint32_t k = 0; k < nz; ++k) mapz.push_back(make_uint2(b, k));
         const uint32_t na = (uint32_t)((Mh + e->B[b] - 1) / e->B[b]) * M;
@@ -484,7 +519,11 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
         e->sr_smem = std::max(e->sr_smem, sm);
     }
     e->segments = segbase[nbox];
-    if ((s = dalloc(&e->d_mapz, mapz.size())) || (s = dalloc(&e->d_mapa, mapa.size()))) return fail(s);
+    if ((s = palloc(&e->d_mapz, mapz.size(), st)) || (s = palloc(&e->d_mapa, mapa.size(), st))) return fail(s);
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error("cuco_ensemble_create: allocation failed");
+        return fail(CUCO_ERR_NOMEM);
+    }
     if (cudaMemcpy(e->table, tab.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_pbeg, e->pbeg.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_segbase, segbase.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -500,7 +539,7 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
         return fail(CUCO_ERR_CUDA);
     }
     e->pm = PMMulti{nbox, e->fixed, e->d_pm, e->d_pbeg, e->d_mapz, e->d_mapa, (uint32_t)mapz.size(),
-                    (uint32_t)mapa.size(), smz, sma, e->rho, (size_t)mbase[nbox]};
+                    (uint32_t)mapa.size(), smz, sma, e->rho64, (size_t)mbase[nbox]};
     cudaEventCreate(&e->t0);
     cudaEventCreate(&e->t1);
     *out = e;
@@ -513,11 +552,13 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
     drop_graph(e);
     for (void *p : {(void *)e->pos, (void *)e->vel, (void *)e->acc_pp, (void *)e->acc_pm, (void *)e->spos,
                     (void *)e->acc_pm_s, (void *)e->keys, (void *)e->perm, (void *)e->keys_alt, (void *)e->perm_alt,
-                    (void *)e->hist, (void *)e->cell_off, (void *)e->stage3, (void *)e->rho, (void *)e->spec,
+                    (void *)e->hist, (void *)e->cell_off, (void *)e->stage3, (void *)e->rho, (void *)e->rho64,
+                    (void *)e->spec,
                     (void *)e->green, (void *)e->tw, (void *)e->table, (void *)e->d_pbeg, (void *)e->d_segbase,
                     (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, e->d_sr,
                     (void *)e->d_kicks, (void *)e->d_factors, (void *)e->pair_counter})
-        cudaFree(p);
+        if (p && e->stream) cudaFreeAsync(p, e->stream);
+    if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->h_factors) cudaFreeHost(e->h_factors);
     if (e->h_kicks) cudaFreeHost(e->h_kicks);
     if (e->t0) cudaEventDestroy(e->t0);
@@ -656,5 +697,44 @@ cuco_status_t cuco_ensemble_count_pairs(cuco_ensemble_t *e, int enable, uint64_t
 }
 
 int cuco_ensemble_launches_per_step(cuco_ensemble_t *e) { return e ? e->launches : 0; }
+
+cuco_status_t cuco_ensemble_copy_state(cuco_ensemble_t *dst, int dst_box, cuco_ensemble_t *src, int src_box) {
+    if (!dst || !src || dst_box < 0 || dst_box >= dst->nbox || src_box < 0 || src_box >= src->nbox ||
+        dst->cfg[dst_box].n != src->cfg[src_box].n || dst->fixed != src->fixed ||
+        dst->cfg[dst_box].boxsize != src->cfg[src_box].boxsize) {
+        set_error("cuco_ensemble_copy_state: boxes differ in size, box length or mode");
+        return CUCO_ERR_INVALID;
+    }
+    CUCO_TRY_CUDA(cudaStreamSynchronize(src->stream));
+    const size_t nb = src->cfg[src_box].n;
+    const uint32_t s0 = src->pbeg[src_box], d0 = dst->pbeg[dst_box];
+    CUCO_TRY_CUDA(cudaMemcpyAsync(dst->pos + d0, src->pos + s0, sizeof(float4) * nb, cudaMemcpyDeviceToDevice,
+                                  dst->stream));
+    CUCO_TRY_CUDA(cudaMemcpyAsync(dst->vel + d0, src->vel + s0, sizeof(float4) * nb, cudaMemcpyDeviceToDevice,
+                                  dst->stream));
+    CUCO_TRY_CUDA(cudaStreamSynchronize(dst->stream));
+    dst->has_state = true;
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_footprint(const cuco_config_t *boxes, int nbox, uint64_t *bytes) {
+    if (!boxes || nbox < 0 || !bytes) {
+        set_error("cuco_ensemble_footprint: invalid argument");
+        return CUCO_ERR_INVALID;
+    }
+    uint64_t b = 0, maxn = 0;
+    for (int k = 0; k < nbox; ++k) {
+        const uint64_t n = (uint64_t)boxes[k].n, M = (uint64_t)boxes[k].pm_grid;
+        const uint64_t G = boxes[k].cell_grid > 0 ? (uint64_t)boxes[k].cell_grid : M / 2;  // the largest tuned grid
+        b += n * (6 * sizeof(float4) + 4 * sizeof(uint32_t));    // state, sorted copies, keys
+        b += 4 * (G * G * G + 1);                                // cell offsets
+        b += 12 * M * M * M + 8 * M * M * (M / 2 + 1);           // deposit + real grid + half spectrum
+        b += 12 * (M / 2 + 1) + 8 * M + 2048 + 16 * (M * M);    // tables, descriptors, CTA maps
+        maxn = std::max(maxn, n);
+    }
+    b += 12 * maxn + 4 * (uint64_t)kNTab;
+    *bytes = b;
+    return CUCO_OK;
+}
 
 }  // extern "C"

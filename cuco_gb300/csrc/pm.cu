@@ -3,10 +3,14 @@
 //
 // Reference: pmforce_periodic (pm_periodic.c:67-314), which deposits and
 // interpolates on the host and round-trips the grid through cuFFT.  Here:
-//   k_deposit      CIC mass assignment (pm_periodic.c:97-132) with float atomics
-//                  into an M^3 grid; the particles arrive cell-sorted, so a
-//                  warp's atomics hit a few neighbouring mesh cells.
-//   k_fft_z_r2c    real->complex along z.  Two real rows are packed as the real
+//   k_deposit      CIC mass assignment (pm_periodic.c:97-132): each weight as
+//                  the integer w * 2^32, added with 64-bit integer atomics into
+//                  an M^3 grid, so the grid is the same whatever order the
+//                  particles land in (float atomics are not associative); the
+//                  particles arrive cell-sorted, so a warp's atomics hit a few
+//                  neighbouring mesh cells.
+//   k_fft_z_r2c    real->complex along z; its load converts the integer sums to
+//                  mass (one rounding).  Two real rows are packed as the real
 //                  and imaginary parts of one complex row, transformed together
 //                  and separated (X1 = (Z + conj Z_-k)/2, X2 = (Z - conj Z_-k)/2i).
 //   k_fft_axis     complex transforms along y, and along x fused with the
@@ -127,8 +131,8 @@ __device__ __forceinline__ void load_twiddles(float2 *tw_s, const float2 *tw, in
 }
 
 // rows r0 .. r0+2P-1 of the M^3 real grid (row = x*M + y) -> spectrum rows
-__device__ __forceinline__ void fft_z_r2c(const float *__restrict__ rho, float2 *__restrict__ spec,
-                                          const float2 *tw, int M, int P, int blk) {
+__device__ __forceinline__ void fft_z_r2c(const unsigned long long *__restrict__ rho64, float mscale,
+                                          float2 *__restrict__ spec, const float2 *tw, int M, int P, int blk) {
     extern __shared__ float2 sm[];
     const int pitch = P + 1;
     float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
@@ -141,7 +145,8 @@ __device__ __forceinline__ void fft_z_r2c(const float *__restrict__ rho, float2 
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             int e = e0 + u * blockDim.x;
-            v[u] = e < 2 * P * M ? rho[r0 * M + e] : 0.f;
+            // the deposit's exact integer sums, rounded once to float
+            v[u] = e < 2 * P * M ? __fmul_rn(__ull2float_rn(rho64[r0 * M + e]), mscale) : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
@@ -278,8 +283,9 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
 }
 
 __global__ void __launch_bounds__(kFFTThreads)
-    k_fft_z_r2c(const float *__restrict__ rho, float2 *__restrict__ spec, const float2 *tw, int M, int P) {
-    fft_z_r2c(rho, spec, tw, M, P, blockIdx.x);
+    k_fft_z_r2c(const unsigned long long *__restrict__ rho64, float mscale, float2 *__restrict__ spec,
+                const float2 *tw, int M, int P) {
+    fft_z_r2c(rho64, mscale, spec, tw, M, P, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(kFFTThreads)
@@ -298,7 +304,7 @@ __global__ void __launch_bounds__(kFFTThreads)
     k_fft_z_r2c_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
-    fft_z_r2c(d.rho, d.spec, d.twiddle, d.M, d.P, m.y);
+    fft_z_r2c(d.rho64, d.mscale, d.spec, d.twiddle, d.M, d.P, m.y);
 }
 
 __global__ void __launch_bounds__(kFFTThreads)
@@ -352,24 +358,31 @@ __device__ __forceinline__ void cic_point(const float4 &p, float to_slab_fac, in
     }
 }
 
+// CIC weight w in [0, 1] as the integer w * 2^32 (rounded once): integer
+// atomics are associative, so the deposited grid does not depend on the order
+// in which particles land, and it is the exact sum of the rounded weights.
+__device__ __forceinline__ void deposit_w(unsigned long long *a, float w) {
+    atomicAdd(a, __float2ull_rn(__fmul_rn(w, 4294967296.0f)));
+}
+
 template <bool FIXED>
-__device__ __forceinline__ void deposit_one(float4 p, float *__restrict__ rho, int M, float to_slab_fac,
-                                            float mass) {
+__device__ __forceinline__ void deposit_one(float4 p, unsigned long long *__restrict__ rho64, int M,
+                                            float to_slab_fac) {
     int s[3][2];
     float d[3];
     cic_point<FIXED>(p, to_slab_fac, M, s, d);
     const int sx = s[0][0], sxx = s[0][1], sy = s[1][0], syy = s[1][1], sz = s[2][0], szz = s[2][1];
     const float dx = d[0], dy = d[1], dz = d[2];
     const size_t Mz = M, Myz = (size_t)M * M;
-    float m0 = mass * (1.f - dx), m1 = mass * dx;
-    atomicAdd(&rho[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz));
-    atomicAdd(&rho[sx * Myz + syy * Mz + sz], m0 * dy * (1.f - dz));
-    atomicAdd(&rho[sx * Myz + sy * Mz + szz], m0 * (1.f - dy) * dz);
-    atomicAdd(&rho[sx * Myz + syy * Mz + szz], m0 * dy * dz);
-    atomicAdd(&rho[sxx * Myz + sy * Mz + sz], m1 * (1.f - dy) * (1.f - dz));
-    atomicAdd(&rho[sxx * Myz + syy * Mz + sz], m1 * dy * (1.f - dz));
-    atomicAdd(&rho[sxx * Myz + sy * Mz + szz], m1 * (1.f - dy) * dz);
-    atomicAdd(&rho[sxx * Myz + syy * Mz + szz], m1 * dy * dz);
+    const float m0 = 1.f - dx, m1 = dx;
+    deposit_w(&rho64[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz));
+    deposit_w(&rho64[sx * Myz + syy * Mz + sz], m0 * dy * (1.f - dz));
+    deposit_w(&rho64[sx * Myz + sy * Mz + szz], m0 * (1.f - dy) * dz);
+    deposit_w(&rho64[sx * Myz + syy * Mz + szz], m0 * dy * dz);
+    deposit_w(&rho64[sxx * Myz + sy * Mz + sz], m1 * (1.f - dy) * (1.f - dz));
+    deposit_w(&rho64[sxx * Myz + syy * Mz + sz], m1 * dy * (1.f - dz));
+    deposit_w(&rho64[sxx * Myz + sy * Mz + szz], m1 * (1.f - dy) * dz);
+    deposit_w(&rho64[sxx * Myz + syy * Mz + szz], m1 * dy * dz);
 }
 
 __device__ __forceinline__ int wrapi(int a, int M) { return a < 0 ? a + M : (a >= M ? a - M : a); }
@@ -411,10 +424,10 @@ __device__ __forceinline__ float4 interp_one(float4 p, const float *__restrict__
 }
 
 template <bool FIXED>
-__global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, float *__restrict__ rho,
-                          int M, float to_slab_fac, float mass) {
+__global__ void k_deposit(const float4 *__restrict__ pos, uint32_t n, unsigned long long *__restrict__ rho64,
+                          int M, float to_slab_fac) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) deposit_one<FIXED>(pos[i], rho, M, to_slab_fac, mass);
+    if (i < n) deposit_one<FIXED>(pos[i], rho64, M, to_slab_fac);
 }
 
 template <bool FIXED>
@@ -430,7 +443,7 @@ __global__ void k_deposit_multi(const float4 *__restrict__ pos, uint32_t n, cons
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const PMBoxDesc &d = boxes[find_box(pbeg, nbox, i)];
-    deposit_one<FIXED>(pos[i], d.rho, d.M, d.to_slab_fac, d.mass);
+    deposit_one<FIXED>(pos[i], d.rho64, d.M, d.to_slab_fac);
 }
 
 template <bool FIXED>
@@ -500,7 +513,7 @@ cuco_status_t pm_forces_multi(const PMMulti &m, const float4 *pos, uint32_t n, f
         return true;
     }();
     (void)attr;
-    CUCO_TRY_CUDA(cudaMemsetAsync(m.rho_all, 0, sizeof(float) * m.rho_all_count, stream));
+    CUCO_TRY_CUDA(cudaMemsetAsync(m.rho64_all, 0, sizeof(unsigned long long) * m.rho_all_count, stream));
     if (n) {
         if (m.fixed)
             k_deposit_multi<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox);
@@ -547,6 +560,7 @@ cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, fl
     plan->fd_fac = (float)fac;
     const size_t Mh = M / 2 + 1;
     CUCO_TRY_CUDA(cudaMalloc(&plan->rho, sizeof(float) * (size_t)M * M * M));
+    CUCO_TRY_CUDA(cudaMalloc(&plan->rho64, sizeof(unsigned long long) * (size_t)M * M * M));
     CUCO_TRY_CUDA(cudaMalloc(&plan->spec, sizeof(float2) * (size_t)M * M * Mh));
     CUCO_TRY_CUDA(cudaMalloc(&plan->green1d, sizeof(float) * Mh));
     CUCO_TRY_CUDA(cudaMalloc(&plan->twiddle, sizeof(float2) * M));
@@ -577,6 +591,8 @@ cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, fl
 
 void pm_plan_destroy(PMPlan *plan) {
     cudaFree(plan->rho);
+    cudaFree(plan->rho64);
+    plan->rho64 = nullptr;
     cudaFree(plan->spec);
     cudaFree(plan->green1d);
     cudaFree(plan->twiddle);
@@ -591,17 +607,18 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
     const int P = fft_batch_z(M), B = fft_batch_axis(M);
     const size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
     const size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
-    CUCO_TRY_CUDA(cudaMemsetAsync(plan.rho, 0, sizeof(float) * (size_t)M * M * M, stream));
+    CUCO_TRY_CUDA(cudaMemsetAsync(plan.rho64, 0, sizeof(unsigned long long) * (size_t)M * M * M, stream));
     if (n) {
         if (plan.fixed)
-            k_deposit<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.mass);
+            k_deposit<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho64, M, plan.to_slab_fac);
         else
-            k_deposit<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.mass);
+            k_deposit<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho64, M, plan.to_slab_fac);
     }
     CUCO_TRY_CUDA(cudaGetLastError());
     if (ev_deposit_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_deposit_done, stream));
     const unsigned zblocks = (unsigned)((size_t)M * M / (2 * P));
-    k_fft_z_r2c<<<zblocks, kFFTThreads, smz, stream>>>(plan.rho, plan.spec, plan.twiddle, M, P);
+    k_fft_z_r2c<<<zblocks, kFFTThreads, smz, stream>>>(plan.rho64, ldexpf(plan.mass, -32), plan.spec,
+                                                       plan.twiddle, M, P);
     dim3 ag((Mh + B - 1) / B, M);
     k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, -1, 0);
     k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 0, -1, 1);

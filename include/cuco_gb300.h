@@ -299,6 +299,13 @@ cuco_status_t cuco_ensemble_timer(cuco_ensemble_t *ensemble, int op, float *ms);
  * in-kernel count on or off for the following passes */
 cuco_status_t cuco_ensemble_count_pairs(cuco_ensemble_t *ensemble, int enable, uint64_t *pairs);
 int cuco_ensemble_launches_per_step(cuco_ensemble_t *ensemble);
+/* the positions and velocities of src's box to dst's box (same n, box length
+ * and mode), device to device: how a serving loop carries a running job into
+ * a rebuilt ensemble */
+cuco_status_t cuco_ensemble_copy_state(cuco_ensemble_t *dst, int dst_box, cuco_ensemble_t *src, int src_box);
+/* device bytes an ensemble of these boxes holds (an upper bound: a box with
+ * cell_grid 0 is counted at the largest grid the autotuner may pick) */
+cuco_status_t cuco_ensemble_footprint(const cuco_config_t *boxes, int nbox, uint64_t *bytes);
 
 /* Stable sort of (keys, values) by the low key_bits bits, in place, that
  * allocates no device memory (no counterpart in the reference).  For callers
