@@ -175,6 +175,119 @@ def run_batched(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+SERVING = "serving"
+
+
+def serving_stream(njobs, rate=20.0, seed=5150):
+    """Poisson arrivals (exponential gaps, mean 1/rate s); per job: particle
+    grid log-uniform over 32..192 per side (nearest integer with no prime
+    factor above 5), mesh 2x, L uniform in 50..500 Mpc/h, 50..200 steps, own
+    seed."""
+    rng = np.random.default_rng(seed)
+    smooth = [k for k in range(32, 193) if smooth5(k)]
+    t, out = 0.0, []
+    for i in range(njobs):
+        t += float(rng.exponential(1.0 / rate))
+        x = math.exp(rng.uniform(math.log(32), math.log(192)))
+        n_side = min(smooth, key=lambda k: abs(k - x))
+        out.append({"id": i, "arrival": t, "n_side": n_side, "M": 2 * n_side, "L": float(rng.uniform(50.0, 500.0)),
+                    "steps": int(rng.integers(50, 201)), "seed": seed + 1 + i})
+    return out
+
+
+def _serving_ic(spec):
+    from cuco_gb300 import ics
+    ic = ics.zeldovich(spec["n_side"], spec["L"], Z_INIT, spec["seed"])
+    return ic.pos, ic.canonical_velocity(), ic.mass, ic.boxsize, ic.a
+
+
+def serving_jobs(stream, device=0):
+    """The stream's jobs with their initial conditions (the request payload),
+    made in a spawn process pool before the stream starts."""
+    import multiprocessing as mp
+    from cuco_gb300 import BoxConfig, ics
+    from cuco_gb300.engine import MODE_FIXED
+    from cuco_gb300.serve import Job
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        ic_data = pool.map(_serving_ic, stream)
+    jobs = []
+    for sp, (pos, vel, mass, boxsize, a0) in zip(stream, ic_data):
+        soft = float(np.float32(2.8 * np.float32(SOFT_FRAC * boxsize / sp["n_side"])))
+        cfg = BoxConfig(n=sp["n_side"] ** 3, pm_grid=sp["M"], boxsize=boxsize, mass=mass, G=ics.G_INTERNAL,
+                        softening=soft, mode=MODE_FIXED, device=device)
+        jobs.append(Job(sp["id"], cfg, pos, vel, a0, sp["steps"], arrival=sp["arrival"]))
+    return jobs
+
+
+def run_serving(args, world, rank, local):
+    """Continuous batching of a job stream under an HBM budget, against the
+    same jobs run one at a time on the plain path."""
+    from cuco_gb300 import Box, BoxConfig, fixed_step_schedule
+    from cuco_gb300.engine import MODE_FIXED
+    from cuco_gb300.ensemble import Ensemble
+    from cuco_gb300.serve import Server
+    stream = serving_stream(args.jobs)
+    jobs = serving_jobs(stream, local)
+    # autotune every size once (cached), outside the timed stream
+    sizes_seen = {}
+    for j in jobs:
+        sizes_seen.setdefault((j.config.n, j.config.pm_grid), j.config)
+    Ensemble(list(sizes_seen.values())).close()
+    srv = Server(int(args.hbm_budget_gb * 1e9), mode=MODE_FIXED, keep_results=False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    done = srv.run(jobs)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    lat = np.array([j.done - j.arrival for j in done])
+    updates = sum(j.config.n * (j.steps + 1) for j in done)
+    served_rate = updates / wall
+    # one at a time, plain path: a sample of the jobs run alone (their full
+    # runs), and a FIFO queue of all jobs at that rate with the same arrivals
+    sample = jobs[:: max(1, len(jobs) // args.baseline_jobs)][: args.baseline_jobs]
+    plain_t, plain_u = 0.0, 0
+    for j in sample:
+        box = Box(BoxConfig(**{**j.config.__dict__, "mode": 0, "cell_grid": None}))
+        box.set_state(j.pos, j.vel)
+        _, drift, kick = fixed_step_schedule(j.a_begin, 1.0, j.steps)
+        box.sync()
+        t = time.perf_counter()
+        for s in range(j.steps + 1):
+            box.step(drift[s], kick[s])
+        box.sync()
+        plain_t += time.perf_counter() - t
+        plain_u += j.config.n * (j.steps + 1)
+        box.close()
+    plain_rate = plain_u / plain_t
+    free, fifo = 0.0, []
+    for sp in stream:
+        free = max(free, sp["arrival"]) + sp["n_side"] ** 3 * (sp["steps"] + 1) / plain_rate
+        fifo.append(free - sp["arrival"])
+    fifo = np.array(fifo)
+    sizes = [sp["n_side"] for sp in stream]
+    line = {
+        "metric": "particle-updates/s", "value": served_rate, "unit": "particle-updates/s", "n_gpus": world,
+        "steps": int(sum(sp["steps"] + 1 for sp in stream)), "warmup": 0, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic",
+        "config": {"workload": f"serving-{len(stream)}jobs-poisson20-N32to192-M2N-L50to500-50to200steps",
+                   "jobs": len(stream), "arrival_rate_per_s": 20.0, "hbm_budget_gb": args.hbm_budget_gb,
+                   "n_side_min": min(sizes), "n_side_max": max(sizes),
+                   "positions": "uint32 fixed point (L/2^32)", "clock": "host wall time"},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "max": float(lat.max())},
+        "wall_s": wall, "particle_updates": updates, "max_concurrent_jobs": srv.peak_active,
+        "rebuilds": srv.rebuilds, "rebuild_s": srv.rebuild_s,
+        "one_at_a_time_plain": {"value": plain_rate, "unit": "particle-updates/s", "sample_jobs": len(sample),
+                                "fifo_latency_s": {"p50": float(np.percentile(fifo, 50)),
+                                                   "p99": float(np.percentile(fifo, 99))},
+                                "ratio": served_rate / plain_rate},
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def apply_preset(name):
     global N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD
     N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD = PRESETS[name]
@@ -509,9 +622,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS) + [BATCHED])
+    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS) + [BATCHED, SERVING])
     ap.add_argument("--baseline-steps", type=int, default=20)
+    ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")
+    ap.add_argument("--baseline-jobs", type=int, default=8, help="serving: jobs run alone on the plain path")
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
     args = ap.parse_args()
+    if args.workload == SERVING:
+        world, rank, local = dist_setup()
+        run_serving(args, world, rank, local)
+        return
     if args.workload == BATCHED:
         args.warmup = max(args.warmup, 3)
         world, rank, local = dist_setup()

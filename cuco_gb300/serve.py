@@ -10,9 +10,10 @@ running jobs plus the newcomer stay within the HBM budget (and the number of
 running jobs within max_active); finished jobs leave.  When the set of running
 jobs changes, the ensemble is rebuilt from the device's memory pool and the
 running jobs' positions and velocities are carried over device to device, so
-a job's trajectory does not depend on who else is running: its short-range
-force is bit-identical alone and in the mix, and its PM force differs only by
-the order of float atomics in the mass deposit.
+a job's trajectory does not depend on who else is running: every stage of a
+step is deterministic (stable sort, integer-atomic mass deposit, FFT,
+interpolation, a short range that visits candidates in a fixed order), and a
+job's result is bit-identical alone and in the mix.
 
 Time comes from a clock callable: wall time for measurements, a tick counter
 for tests.  A job's latency is its completion time minus its arrival time.
@@ -81,6 +82,8 @@ class Server:
         self.ens: Ensemble | None = None
         self.ticks = 0
         self.rebuilds = 0
+        self.rebuild_s = 0.0             # host time spent rebuilding ensembles
+        self.peak_active = 0             # most jobs running at once
         self.updates = 0                 # particle-updates done
 
     # -------------------------------------------------------------- intake
@@ -103,6 +106,7 @@ class Server:
 
     # ------------------------------------------------------------- rebuild
     def _rebuild(self, keep: list[Job], new: list[Job]):
+        t_host = time.perf_counter()
         now = self.clock()
         jobs = keep + new
         old, old_index = self.ens, {id(j): k for k, j in enumerate(self.active)}
@@ -119,6 +123,8 @@ class Server:
         self.ens = ens
         self.active = jobs
         self.rebuilds += 1
+        self.peak_active = max(self.peak_active, len(jobs))
+        self.rebuild_s += time.perf_counter() - t_host
 
     def _retire(self):
         """Collect finished jobs' results (their boxes stay in the ensemble,
