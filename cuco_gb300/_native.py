@@ -139,6 +139,7 @@ SIGNATURES = {
     "cuco_box_timer": (_I, [_P, _I, ctypes.POINTER(ctypes.c_float)]),
     "cuco_ensemble_create": (_I, [ctypes.POINTER(CucoConfig), _I, ctypes.POINTER(_P)]),
     "cuco_ensemble_destroy": (_I, [_P]),
+    "cuco_ensemble_reshape": (_I, [_P, ctypes.POINTER(CucoConfig), _I, _P]),
     "cuco_ensemble_cell_grid": (_I, [_P, _I, _P, _P, _P]),
     "cuco_ensemble_set_state": (_I, [_P, _I, _P, _P]),
     "cuco_ensemble_get_state": (_I, [_P, _I, _P, _P, _P, _P]),

@@ -298,7 +298,7 @@ struct cuco_ensemble {
     DriftBox *d_drift = nullptr;
     PMBoxDesc *d_pm = nullptr;
     uint2 *d_mapz = nullptr, *d_mapa = nullptr;
-    void *d_sr = nullptr;
+    char *d_sr = nullptr;
     double2 *d_kicks = nullptr;
     StepFactors *d_factors = nullptr, *h_factors = nullptr;  // h_factors: pinned
     double2 *h_kicks = nullptr;                               // pinned
@@ -312,6 +312,11 @@ struct cuco_ensemble {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    // capacities (elements) of the grow-only arrays
+    size_t cap_n = 0, cap_hist = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
+           cap_green = 0, cap_tw = 0, cap_table = 0, cap_pbeg = 0, cap_segbase = 0, cap_drift = 0, cap_pm = 0,
+           cap_kicks = 0, cap_factors = 0, cap_counter = 0, cap_sr = 0, cap_hfactors = 0, cap_hkicks = 0,
+           cap_mapz = 0, cap_mapa = 0;
 };
 
 namespace {
@@ -361,51 +366,67 @@ void drop_graph(cuco_ensemble *e) {
     e->graph = nullptr;
 }
 
-}  // namespace
-
-extern "C" {
-
-cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_ensemble_t **out) {
-    if (!boxes || nbox <= 0 || !out) {
-        set_error("cuco_ensemble_create: need at least one box");
-        return CUCO_ERR_INVALID;
-    }
+cuco_status_t validate_boxes(const cuco_config_t *boxes, int nbox, int mode, int device) {
     for (int b = 0; b < nbox; ++b) {
         const cuco_config_t &c = boxes[b];
-        if (c.mode != boxes[0].mode || c.device != boxes[0].device) {
-            set_error("cuco_ensemble_create: all boxes share one mode and one device");
+        if ((int)c.mode != mode || c.device != device) {
+            set_error("ensemble: all boxes share one mode and one device");
             return CUCO_ERR_INVALID;
         }
         if (c.n < 0 || !(c.boxsize > 0) || !(c.rcut > 0) || !(c.asmth > 0) || !(c.softening > 0) ||
             c.cell_grid < 0 || c.cell_grid > 1024) {
-            set_error("cuco_ensemble_create: invalid box configuration");
+            set_error("ensemble: invalid box configuration");
             return CUCO_ERR_INVALID;
         }
         if (!pm_mesh_supported(c.pm_grid)) {
-            set_error("cuco_ensemble_create: a mesh is not even, in [8, 1024] and 5-smooth");
+            set_error("ensemble: a mesh is not even, in [8, 1024] and 5-smooth");
             return CUCO_ERR_UNSUPPORTED;
         }
     }
-    CUCO_TRY_CUDA(cudaSetDevice(boxes[0].device));
-    cuco_ensemble *e = new cuco_ensemble();
-    e->nbox = nbox;
-    e->device = boxes[0].device;
-    e->fixed = boxes[0].mode == CUCO_MODE_FIXED;
-    e->cfg.assign(boxes, boxes + nbox);
-    auto fail = [&](cuco_status_t s) {
-        cuco_ensemble_destroy(e);
-        return s;
-    };
-    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        set_error("cudaStreamCreate failed");
-        delete e;
-        return CUCO_ERR_CUDA;
+    return CUCO_OK;
+}
+
+// Device array that only grows (25% headroom), reallocated without keeping
+// its contents; the stream-ordered pool makes the reallocation cheap.
+template <typename T>
+cuco_status_t grow(T *&p, size_t &cap, size_t need, cudaStream_t s) {
+    if (p && need <= cap) return CUCO_OK;
+    const size_t ncap = std::max(need ? need : 1, cap + cap / 4);
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    cap = 0;
+    CUCO_TRY(palloc(&p, ncap, s));
+    cap = ncap;
+    return CUCO_OK;
+}
+
+template <typename T>
+cuco_status_t grow_pinned(T *&p, size_t &cap, size_t need) {
+    if (p && need <= cap) return CUCO_OK;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    if (cudaMallocHost(&p, sizeof(T) * need) != cudaSuccess) {
+        set_error("ensemble: pinned allocation failed");
+        return CUCO_ERR_NOMEM;
     }
+    memset(p, 0, sizeof(T) * need);
+    cap = need;
+    return CUCO_OK;
+}
+
+// (Re)build the ensemble for a set of boxes: autotuned plans, offsets, array
+// capacities, descriptors and CTA maps.  carry[b] = the box of the previous
+// layout whose positions and velocities box b keeps (-1: set by the caller
+// afterwards); null when there is no previous layout to keep.
+cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int nbox, const int *carry) {
+    cudaStream_t st = e->stream;
+    drop_graph(e);
+    std::vector<cuco_config_t> cfg(boxes, boxes + nbox);
+    std::vector<int> P(nbox), B(nbox);
     // autotune: cell grid and FFT batching per (n, M, mode)
-    e->P.resize(nbox);
-    e->B.resize(nbox);
     for (int b = 0; b < nbox; ++b) {
-        cuco_config_t &c = e->cfg[b];
+        cuco_config_t &c = cfg[b];
         const auto key = std::make_tuple(c.n, c.pm_grid, (int)c.mode);
         Tuned t{};
         bool cached;
@@ -416,70 +437,116 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
             if (cached) t = it->second;
         }
         if (!cached) {
-            t.cell_grid = tune_cell_grid(c, e->stream);
-            tune_fft(c.pm_grid, c.boxsize, c.asmth, e->stream, &t.P, &t.B);
+            t.cell_grid = tune_cell_grid(c, st);
+            tune_fft(c.pm_grid, c.boxsize, c.asmth, st, &t.P, &t.B);
             std::lock_guard<std::mutex> lk(g_tune_mu);
             g_tune_cache[key] = t;
         }
         if (c.cell_grid <= 0) {
             if (t.cell_grid <= 0) {
-                set_error("cuco_ensemble_create: no admissible cell grid for a box");
-                return fail(CUCO_ERR_UNSUPPORTED);
+                set_error("ensemble: no admissible cell grid for a box");
+                return CUCO_ERR_UNSUPPORTED;
             }
             c.cell_grid = t.cell_grid;
         }
-        e->P[b] = t.P;
-        e->B[b] = t.B;
+        P[b] = t.P;
+        B[b] = t.B;
     }
     // sizes and offsets
-    e->pbeg.assign(nbox + 1, 0);
+    std::vector<uint32_t> pbeg(nbox + 1, 0);
     std::vector<uint64_t> cbase(nbox + 1, 0), mbase(nbox + 1, 0), sbase(nbox + 1, 0), gbase(nbox + 1, 0),
         tbase(nbox + 1, 0);
+    size_t maxn = 0;
     for (int b = 0; b < nbox; ++b) {
-        const cuco_config_t &c = e->cfg[b];
+        const cuco_config_t &c = cfg[b];
         const uint64_t M = c.pm_grid, G = c.cell_grid;
-        e->pbeg[b + 1] = e->pbeg[b] + (uint32_t)c.n;
+        pbeg[b + 1] = pbeg[b] + (uint32_t)c.n;
         cbase[b + 1] = cbase[b] + G * G * G;
         mbase[b + 1] = mbase[b] + M * M * M;
         sbase[b + 1] = sbase[b] + M * M * (M / 2 + 1);
         gbase[b + 1] = gbase[b] + (M / 2 + 1);
         tbase[b + 1] = tbase[b] + M;
+        maxn = std::max(maxn, (size_t)c.n);
     }
-    if (cbase[nbox] >= 0xffffffffull || e->pbeg[nbox] > 0xfffffff0u) {
-        set_error("cuco_ensemble_create: more than 2^32 cells or particles in total");
-        return fail(CUCO_ERR_UNSUPPORTED);
+    if (cbase[nbox] >= 0xffffffffull || (uint64_t)pbeg[nbox] > 0xfffffff0ull) {
+        set_error("ensemble: more than 2^32 cells or particles in total");
+        return CUCO_ERR_UNSUPPORTED;
     }
-    e->n = e->pbeg[nbox];
-    e->ncells = cbase[nbox];
-    e->key_bits = key_bits(e->ncells);
-    const size_t n = e->n;
-    size_t maxn = 0;
-    for (int b = 0; b < nbox; ++b) maxn = std::max(maxn, (size_t)e->cfg[b].n);
+    const size_t n = pbeg[nbox];
+    const uint64_t ncells = cbase[nbox];
+    const int kbits = key_bits(ncells);
     cuco_status_t s;
-    pool_keep_memory(e->device);
-    cudaStream_t st = e->stream;
-    if ((s = palloc(&e->pos, n, st)) || (s = palloc(&e->vel, n, st)) || (s = palloc(&e->acc_pp, n, st)) ||
-        (s = palloc(&e->acc_pm, n, st)) || (s = palloc(&e->spos, n, st)) || (s = palloc(&e->acc_pm_s, n, st)) ||
-        (s = palloc(&e->keys, n, st)) || (s = palloc(&e->perm, n, st)) || (s = palloc(&e->keys_alt, n, st)) ||
-        (s = palloc(&e->perm_alt, n, st)) || (s = palloc(&e->hist, sort_hist_entries(e->n, e->key_bits, 8), st)) ||
-        (s = palloc(&e->cell_off, e->ncells + 1, st)) || (s = palloc(&e->stage3, 3 * maxn, st)) ||
-        (s = palloc(&e->rho, mbase[nbox], st)) || (s = palloc(&e->rho64, mbase[nbox], st)) ||
-        (s = palloc(&e->spec, sbase[nbox], st)) ||
-        (s = palloc(&e->green, gbase[nbox], st)) || (s = palloc(&e->tw, tbase[nbox], st)) ||
-        (s = palloc(&e->table, kNTab, st)) || (s = palloc(&e->d_pbeg, nbox + 1, st)) ||
-        (s = palloc(&e->d_segbase, nbox + 1, st)) || (s = palloc(&e->d_drift, nbox, st)) ||
-        (s = palloc(&e->d_pm, nbox, st)) || (s = palloc(&e->d_kicks, nbox, st)) ||
-        (s = palloc(&e->d_factors, nbox, st)) || (s = palloc(&e->pair_counter, 1, st)) ||
-        (s = palloc((char **)&e->d_sr, shortrange_desc_bytes() * nbox, st)))
-        return fail(s);
-    if (cudaStreamSynchronize(st) != cudaSuccess ||
-        cudaMallocHost(&e->h_factors, sizeof(StepFactors) * nbox) != cudaSuccess ||
-        cudaMallocHost(&e->h_kicks, sizeof(double2) * nbox) != cudaSuccess) {
-        set_error("cuco_ensemble_create: allocation failed");
-        return fail(CUCO_ERR_NOMEM);
+    // particle state: carried boxes move to their new offsets device to device
+    if (carry && e->pos) {
+        if (n > e->cap_n) {
+            float4 *pos2 = nullptr, *vel2 = nullptr;
+            const size_t ncap = std::max(n, e->cap_n + e->cap_n / 4);
+            if ((s = palloc(&pos2, ncap, st)) || (s = palloc(&vel2, ncap, st))) {
+                if (pos2) cudaFreeAsync(pos2, st);
+                return s;
+            }
+            for (int b = 0; b < nbox; ++b)
+                if (carry[b] >= 0) {
+                    const size_t nb = cfg[b].n, o = e->pbeg[carry[b]];
+                    CUCO_TRY_CUDA(cudaMemcpyAsync(pos2 + pbeg[b], e->pos + o, sizeof(float4) * nb,
+                                                  cudaMemcpyDeviceToDevice, st));
+                    CUCO_TRY_CUDA(cudaMemcpyAsync(vel2 + pbeg[b], e->vel + o, sizeof(float4) * nb,
+                                                  cudaMemcpyDeviceToDevice, st));
+                }
+            cudaFreeAsync(e->pos, st);
+            cudaFreeAsync(e->vel, st);
+            e->pos = pos2;
+            e->vel = vel2;
+            size_t cap = e->cap_n;  // the other per-particle arrays follow
+            for (float4 **q : {&e->acc_pp, &e->acc_pm, &e->spos, &e->acc_pm_s}) {
+                size_t c2 = cap;
+                CUCO_TRY(grow(*q, c2, ncap, st));
+            }
+            for (uint32_t **q : {&e->keys, &e->perm, &e->keys_alt, &e->perm_alt}) {
+                size_t c2 = cap;
+                CUCO_TRY(grow(*q, c2, ncap, st));
+            }
+            e->cap_n = ncap;
+        } else {
+            // through the sorted-copy arrays (scratch between steps), then swap
+            for (int b = 0; b < nbox; ++b)
+                if (carry[b] >= 0) {
+                    const size_t nb = cfg[b].n, o = e->pbeg[carry[b]];
+                    CUCO_TRY_CUDA(cudaMemcpyAsync(e->spos + pbeg[b], e->pos + o, sizeof(float4) * nb,
+                                                  cudaMemcpyDeviceToDevice, st));
+                    CUCO_TRY_CUDA(cudaMemcpyAsync(e->acc_pm_s + pbeg[b], e->vel + o, sizeof(float4) * nb,
+                                                  cudaMemcpyDeviceToDevice, st));
+                }
+            std::swap(e->pos, e->spos);
+            std::swap(e->vel, e->acc_pm_s);
+        }
+    } else if (n > e->cap_n || !e->pos) {
+        const size_t ncap = std::max(n ? n : 1, e->cap_n + e->cap_n / 4);
+        for (float4 **q : {&e->pos, &e->vel, &e->acc_pp, &e->acc_pm, &e->spos, &e->acc_pm_s}) {
+            size_t c2 = e->cap_n;
+            CUCO_TRY(grow(*q, c2, ncap, st));
+        }
+        for (uint32_t **q : {&e->keys, &e->perm, &e->keys_alt, &e->perm_alt}) {
+            size_t c2 = e->cap_n;
+            CUCO_TRY(grow(*q, c2, ncap, st));
+        }
+        e->cap_n = ncap;
+        CUCO_TRY_CUDA(cudaMemsetAsync(e->pos, 0, sizeof(float4) * ncap, st));
+        CUCO_TRY_CUDA(cudaMemsetAsync(e->vel, 0, sizeof(float4) * ncap, st));
     }
-    memset(e->h_factors, 0, sizeof(StepFactors) * nbox);
-    memset(e->h_kicks, 0, sizeof(double2) * nbox);
+    const size_t nbc = (size_t)nbox + 1;
+    if ((s = grow(e->hist, e->cap_hist, sort_hist_entries((uint32_t)n, kbits, 8), st)) ||
+        (s = grow(e->cell_off, e->cap_cells, ncells + 1, st)) || (s = grow(e->stage3, e->cap_stage3, 3 * maxn, st)) ||
+        (s = grow(e->rho, e->cap_mesh, mbase[nbox], st)) ||
+        (s = grow(e->rho64, e->cap_mesh64, mbase[nbox], st)) || (s = grow(e->spec, e->cap_spec, sbase[nbox], st)) ||
+        (s = grow(e->green, e->cap_green, gbase[nbox], st)) || (s = grow(e->tw, e->cap_tw, tbase[nbox], st)) ||
+        (s = grow(e->table, e->cap_table, (size_t)kNTab, st)) || (s = grow(e->d_pbeg, e->cap_pbeg, nbc, st)) ||
+        (s = grow(e->d_segbase, e->cap_segbase, nbc, st)) || (s = grow(e->d_drift, e->cap_drift, nbc, st)) ||
+        (s = grow(e->d_pm, e->cap_pm, nbc, st)) || (s = grow(e->d_kicks, e->cap_kicks, nbc, st)) ||
+        (s = grow(e->d_factors, e->cap_factors, nbc, st)) || (s = grow(e->pair_counter, e->cap_counter, 1, st)) ||
+        (s = grow(e->d_sr, e->cap_sr, shortrange_desc_bytes() * nbc, st)) ||
+        (s = grow_pinned(e->h_factors, e->cap_hfactors, nbc)) || (s = grow_pinned(e->h_kicks, e->cap_hkicks, nbc)))
+        return s;
     // tables and descriptors
     std::vector<float> tab(kNTab);
     shortrange_table(tab.data());
@@ -488,62 +555,115 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
     std::vector<char> srd(shortrange_desc_bytes() * nbox);
     std::vector<uint32_t> segbase(nbox + 1, 0);
     std::vector<uint2> mapz, mapa;
-    size_t smz = 0, sma = 0;
+    std::vector<float> green(gbase[nbox]);
+    std::vector<float2> tw(tbase[nbox]);
+    size_t smz = 0, sma = 0, sr_smem = 0;
     for (int b = 0; b < nbox; ++b) {
-        const cuco_config_t &c = e->cfg[b];
+        const cuco_config_t &c = cfg[b];
         const int M = c.pm_grid, Mh = M / 2 + 1;
         drift[b] = DriftBox{(uint32_t)c.cell_grid, (uint32_t)cbase[b], c.boxsize, (float)c.cell_grid / c.boxsize};
-        std::vector<float> g(Mh);
-        std::vector<float2> t(M);
-        pm_tables(M, c.boxsize, c.asmth, g.data(), t.data());
-        if (cudaMemcpy(e->green + gbase[b], g.data(), sizeof(float) * Mh, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(e->tw + tbase[b], t.data(), sizeof(float2) * M, cudaMemcpyHostToDevice) != cudaSuccess) {
-            set_error("cuco_ensemble_create: table upload failed");
-            return fail(CUCO_ERR_CUDA);
-        }
-        pmd[b] = PMBoxDesc{M, e->P[b], e->B[b], (float)M / c.boxsize, c.mass, pm_fd_fac(M, c.boxsize, c.G),
+        pm_tables(M, c.boxsize, c.asmth, green.data() + gbase[b], tw.data() + tbase[b]);
+        pmd[b] = PMBoxDesc{M, P[b], B[b], (float)M / c.boxsize, c.mass, pm_fd_fac(M, c.boxsize, c.G),
                            e->rho + mbase[b], e->rho64 + mbase[b], ldexpf(c.mass, -32), e->spec + sbase[b],
                            e->green + gbase[b], e->tw + tbase[b]};
-        const uint32_t nz = (uint32_t)(M * M / (2 * e->P[b]));
+        const uint32_t nz = (uint32_t)(M * M / (2 * P[b]));
         for (uint32_t k = 0; k < nz; ++k) mapz.push_back(make_uint2(b, k));
-        const uint32_t na = (uint32_t)((Mh + e->B[b] - 1) / e->B[b]) * M;
+        const uint32_t na = (uint32_t)((Mh + B[b] - 1) / B[b]) * M;
         for (uint32_t k = 0; k < na; ++k) mapa.push_back(make_uint2(b, k));
-        smz = std::max(smz, pm_smem_z(M, e->P[b]));
-        sma = std::max(sma, pm_smem_axis(M, e->B[b]));
+        smz = std::max(smz, pm_smem_z(M, P[b]));
+        sma = std::max(sma, pm_smem_axis(M, B[b]));
         uint32_t nseg = 0;
         size_t sm = 0;
         if ((s = shortrange_desc_fill(sr_params(c, (uint32_t)c.n, (uint32_t)cbase[b]),
                                       srd.data() + b * shortrange_desc_bytes(), &nseg, &sm)))
-            return fail(s);
+            return s;
         segbase[b + 1] = segbase[b] + nseg;
-        e->sr_smem = std::max(e->sr_smem, sm);
+        sr_smem = std::max(sr_smem, sm);
     }
-    e->segments = segbase[nbox];
-    if ((s = palloc(&e->d_mapz, mapz.size(), st)) || (s = palloc(&e->d_mapa, mapa.size(), st))) return fail(s);
-    if (cudaStreamSynchronize(st) != cudaSuccess) {
-        set_error("cuco_ensemble_create: allocation failed");
-        return fail(CUCO_ERR_NOMEM);
-    }
-    if (cudaMemcpy(e->table, tab.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(e->d_pbeg, e->pbeg.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+    if ((s = grow(e->d_mapz, e->cap_mapz, mapz.size(), st)) || (s = grow(e->d_mapa, e->cap_mapa, mapa.size(), st)))
+        return s;
+    if (cudaStreamSynchronize(st) != cudaSuccess ||
+        cudaMemcpy(e->table, tab.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->green, green.data(), sizeof(float) * green.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->tw, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(e->d_pbeg, pbeg.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_segbase, segbase.data(), sizeof(uint32_t) * (nbox + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_drift, drift.data(), sizeof(DriftBox) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_pm, pmd.data(), sizeof(PMBoxDesc) * nbox, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_sr, srd.data(), srd.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_mapz, mapz.data(), sizeof(uint2) * mapz.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_mapa, mapa.data(), sizeof(uint2) * mapa.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(e->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMemset(e->vel, 0, sizeof(float4) * (n ? n : 1)) != cudaSuccess ||
-        cudaMemset(e->pos, 0, sizeof(float4) * (n ? n : 1)) != cudaSuccess) {
-        set_error("cuco_ensemble_create: descriptor upload failed");
-        return fail(CUCO_ERR_CUDA);
+        cudaMemset(e->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess) {
+        set_error("ensemble: descriptor upload failed");
+        return CUCO_ERR_CUDA;
     }
+    memset(e->h_factors, 0, sizeof(StepFactors) * nbox);
+    memset(e->h_kicks, 0, sizeof(double2) * nbox);
+    e->nbox = nbox;
+    e->cfg = cfg;
+    e->P = P;
+    e->B = B;
+    e->pbeg = pbeg;
+    e->n = (uint32_t)n;
+    e->ncells = ncells;
+    e->key_bits = kbits;
+    e->segments = segbase[nbox];
+    e->sr_smem = sr_smem;
     e->pm = PMMulti{nbox, e->fixed, e->d_pm, e->d_pbeg, e->d_mapz, e->d_mapa, (uint32_t)mapz.size(),
                     (uint32_t)mapa.size(), smz, sma, e->rho64, (size_t)mbase[nbox]};
+    e->has_state = e->has_state || carry != nullptr;
+    return CUCO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_ensemble_t **out) {
+    if (!boxes || nbox <= 0 || !out) {
+        set_error("cuco_ensemble_create: need at least one box");
+        return CUCO_ERR_INVALID;
+    }
+    CUCO_TRY(validate_boxes(boxes, nbox, boxes[0].mode, boxes[0].device));
+    CUCO_TRY_CUDA(cudaSetDevice(boxes[0].device));
+    cuco_ensemble *e = new cuco_ensemble();
+    e->device = boxes[0].device;
+    e->fixed = boxes[0].mode == CUCO_MODE_FIXED;
+    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        delete e;
+        return CUCO_ERR_CUDA;
+    }
     cudaEventCreate(&e->t0);
     cudaEventCreate(&e->t1);
+    pool_keep_memory(e->device);
+    cuco_status_t s = ensemble_layout(e, boxes, nbox, nullptr);
+    if (s != CUCO_OK) {
+        cuco_ensemble_destroy(e);
+        return s;
+    }
     *out = e;
     return CUCO_OK;
+}
+
+cuco_status_t cuco_ensemble_reshape(cuco_ensemble_t *e, const cuco_config_t *boxes, int nbox, const int *carry) {
+    if (!e || !boxes || nbox <= 0) {
+        set_error("cuco_ensemble_reshape: need at least one box");
+        return CUCO_ERR_INVALID;
+    }
+    CUCO_TRY(validate_boxes(boxes, nbox, e->fixed ? CUCO_MODE_FIXED : CUCO_MODE_PLAIN, e->device));
+    if (carry)
+        for (int b = 0; b < nbox; ++b) {
+            const int o = carry[b];
+            if (o < -1 || o >= e->nbox || (o >= 0 && (e->cfg[o].n != boxes[b].n ||
+                                                      e->cfg[o].boxsize != boxes[b].boxsize))) {
+                set_error("cuco_ensemble_reshape: a carried box differs in size or box length");
+                return CUCO_ERR_INVALID;
+            }
+        }
+    CUCO_TRY_CUDA(cudaSetDevice(e->device));
+    CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    return ensemble_layout(e, boxes, nbox, carry);
 }
 
 cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
@@ -555,7 +675,7 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
                     (void *)e->hist, (void *)e->cell_off, (void *)e->stage3, (void *)e->rho, (void *)e->rho64,
                     (void *)e->spec,
                     (void *)e->green, (void *)e->tw, (void *)e->table, (void *)e->d_pbeg, (void *)e->d_segbase,
-                    (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, e->d_sr,
+                    (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, (void *)e->d_sr,
                     (void *)e->d_kicks, (void *)e->d_factors, (void *)e->pair_counter})
         if (p && e->stream) cudaFreeAsync(p, e->stream);
     if (e->stream) cudaStreamSynchronize(e->stream);

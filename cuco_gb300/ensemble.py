@@ -17,19 +17,34 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
 
 
+def _configs(configs):
+    arr = (_native.CucoConfig * len(configs))()
+    for k, c in enumerate(configs):
+        arr[k] = c.to_c()
+        if c.cell_grid is None:
+            arr[k].cell_grid = 0  # autotune
+    return arr
+
+
 class Ensemble:
     def __init__(self, configs: list[BoxConfig]):
         self.lib = _native.load()
         self.cfgs = configs
-        arr = (_native.CucoConfig * len(configs))()
-        for k, c in enumerate(configs):
-            arr[k] = c.to_c()
-            if c.cell_grid is None:
-                arr[k].cell_grid = 0  # autotune
         self.nbox = len(configs)
         self.h = ctypes.c_void_p()
-        check(self.lib.cuco_ensemble_create(arr, self.nbox, ctypes.byref(self.h)), "cuco_ensemble_create")
+        check(self.lib.cuco_ensemble_create(_configs(configs), self.nbox, ctypes.byref(self.h)),
+              "cuco_ensemble_create")
         self.n = [c.n for c in configs]
+
+    def reshape(self, configs: list[BoxConfig], carry: list[int] | None = None):
+        """New set of boxes in the same device arrays; carry[b] = current box
+        whose state box b keeps, or -1 (then set it with set_state)."""
+        c = None if carry is None else np.ascontiguousarray(carry, dtype=np.int32)
+        check(self.lib.cuco_ensemble_reshape(self.h, _configs(configs), len(configs), _ptr(c)),
+              "cuco_ensemble_reshape")
+        self.cfgs = configs
+        self.nbox = len(configs)
+        self.n = [x.n for x in configs]
 
     def close(self):
         if self.h:

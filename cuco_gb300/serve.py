@@ -8,8 +8,9 @@ step of a batched ensemble (cuco_ensemble_*), every job on its own schedule.
 Jobs are admitted first-come first-served while the device bytes of the
 running jobs plus the newcomer stay within the HBM budget (and the number of
 running jobs within max_active); finished jobs leave.  When the set of running
-jobs changes, the ensemble is rebuilt from the device's memory pool and the
-running jobs' positions and velocities are carried over device to device, so
+jobs changes, the ensemble is re-laid out in its own device arrays (which
+only grow, so the resident footprint never doubles) and the running jobs'
+positions and velocities move device to device, so
 a job's trajectory does not depend on who else is running: every stage of a
 step is deterministic (stable sort, integer-atomic mass deposit, FFT,
 interpolation, a short range that visits candidates in a fixed order), and a
@@ -106,21 +107,23 @@ class Server:
 
     # ------------------------------------------------------------- rebuild
     def _rebuild(self, keep: list[Job], new: list[Job]):
+        """Re-lay the ensemble out for the running jobs in the same device
+        arrays (they only grow): kept jobs' state moves device to device, new
+        jobs' initial conditions are uploaded."""
         t_host = time.perf_counter()
         now = self.clock()
         jobs = keep + new
-        old, old_index = self.ens, {id(j): k for k, j in enumerate(self.active)}
-        ens = Ensemble([j.config for j in jobs]) if jobs else None
-        for k, j in enumerate(jobs):
-            if id(j) in old_index:
-                check(ens.lib.cuco_ensemble_copy_state(ens.h, k, old.h, old_index[id(j)]),
-                      "cuco_ensemble_copy_state")
+        if jobs:
+            old_index = {id(j): k for k, j in enumerate(self.active)}
+            carry = [old_index.get(id(j), -1) for j in jobs]
+            if self.ens is None:
+                self.ens = Ensemble([j.config for j in jobs])
             else:
-                ens.set_state(k, j.pos, j.vel)
-                j.admitted = now
-        if old is not None:
-            old.close()
-        self.ens = ens
+                self.ens.reshape([j.config for j in jobs], carry)
+            for k, j in enumerate(jobs):
+                if carry[k] < 0:
+                    self.ens.set_state(k, j.pos, j.vel)
+                    j.admitted = now
         self.active = jobs
         self.rebuilds += 1
         self.peak_active = max(self.peak_active, len(jobs))

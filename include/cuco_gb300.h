@@ -279,6 +279,15 @@ cuco_status_t cuco_pinned_free(void *ptr);
 typedef struct cuco_ensemble cuco_ensemble_t;
 cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_ensemble_t **ensemble);
 cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *ensemble);
+/* Re-lay the ensemble out for a new set of boxes (same mode and device),
+ * reusing its device arrays, which only grow: how a serving loop admits and
+ * retires jobs without reallocating.  carry[b] = the current box whose
+ * positions and velocities new box b keeps (same n and box length), or -1
+ * for a box whose state the caller then sets with cuco_ensemble_set_state;
+ * carry may be NULL when nothing is kept.  Synchronizes the ensemble's stream;
+ * the next step captures a new graph. */
+cuco_status_t cuco_ensemble_reshape(cuco_ensemble_t *ensemble, const cuco_config_t *boxes, int nbox,
+                                    const int *carry);
 /* the cell grid and FFT batching (z-pass row pairs, axis-pass columns per CTA) in use */
 cuco_status_t cuco_ensemble_cell_grid(cuco_ensemble_t *ensemble, int box, int *cell_grid, int *fft_p,
                                       int *fft_b);

@@ -107,3 +107,37 @@ def test_ensemble_graph_steps_track_single_boxes():
         box.close()
         assert np.array_equal(pos, pos1) and np.array_equal(vel, vel1), f"box {b} differs from the box alone"
     ens.close()
+
+
+def test_ensemble_reshape_carries_state():
+    """Boxes kept across a reshape (reordered, one dropped, one added, the
+    particle count growing past the arrays' capacity) continue exactly as
+    single boxes stepped alone."""
+    ics_, cfgs = make(SPECS, MODE_FIXED)
+    a, drift, kick = fixed_step_schedule(ics_[0].a, 0.05, 5)
+    ens = Ensemble(cfgs[:2])
+    for b in range(2):
+        ens.set_state(b, ics_[b].pos, ics_[b].canonical_velocity())
+    for s in range(3):
+        ens.step(drift[s], kick[s])
+    before = [ens.get_state(b)[:2] for b in range(2)]
+    # new layout: box 1 first, then the two new boxes (more particles than before); box 0 leaves
+    ens.reshape([cfgs[1], cfgs[2], cfgs[3]], [1, -1, -1])
+    pos, vel, _, _ = ens.get_state(0)
+    assert np.array_equal(pos, before[1][0]) and np.array_equal(vel, before[1][1])
+    for b, k in ((1, 2), (2, 3)):
+        ens.set_state(b, ics_[k].pos, ics_[k].canonical_velocity())
+    for s in range(3, 6):
+        ens.step(drift[s], [kick[s]] * 3)
+    ens.sync()
+    # box 1 ran steps 0..5, boxes 2 and 3 ran steps 3..5 from their ICs
+    for b, k, steps in ((0, 1, range(6)), (1, 2, range(3, 6)), (2, 3, range(3, 6))):
+        pos, vel, _, _ = ens.get_state(b)
+        box = Box(BoxConfig(**{**cfgs[k].__dict__, "cell_grid": ens.plan(b)[0]}))
+        box.set_state(ics_[k].pos, ics_[k].canonical_velocity())
+        for s in steps:
+            box.step(drift[s], kick[s])
+        pos1, vel1, _, _ = box.get_state()
+        box.close()
+        assert np.array_equal(pos, pos1) and np.array_equal(vel, vel1), f"box {b} differs after the reshape"
+    ens.close()
