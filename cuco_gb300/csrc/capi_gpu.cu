@@ -122,8 +122,23 @@ void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridP
     p.grid = G;
     p.n = numParticles;
     KickArgs k{};
+    // the work plan's scratch, grown on demand (like the reference's device
+    // arrays, held until exit)
+    static SRWork w{};
+    if (w.seg_cap < numCells || w.heavy_cap < shortrange_heavy_cap(numParticles)) {
+        cudaFree(w.heavy);
+        cudaFree(w.seg_nt);
+        cudaFree(w.ctl);
+        w = SRWork{};
+        const uint32_t hc = shortrange_heavy_cap(numParticles);
+        capi_check(cudaMalloc(&w.heavy, sizeof(uint2) * hc), "cudaForceEvaluateShortrange");
+        capi_check(cudaMalloc(&w.seg_nt, sizeof(uint32_t) * numCells), "cudaForceEvaluateShortrange");
+        capi_check(cudaMalloc(&w.ctl, 2 * sizeof(uint32_t)), "cudaForceEvaluateShortrange");
+        w.heavy_cap = hc;
+        w.seg_cap = numCells;
+    }
     capi_status(launch_shortrange(p, (const float4 *)sortedPos, gridParticleIndex, cellStart, cellEnd,
-                                  kCellStartEnd, s.table, (float4 *)gravAccel, k, 0),
+                                  kCellStartEnd, s.table, (float4 *)gravAccel, k, w, 0),
                 "cudaForceEvaluateShortrange");
 }
 

@@ -97,11 +97,24 @@ struct KickArgs {
     double kick_pp, kick_pm;
 };
 
+// Device scratch of a launch's work plan: each segment's target count, the
+// slices of segments denser than one unit, and two counters.  seg_cap must
+// cover the launch's segments (G^3 is always enough), heavy_cap
+// shortrange_heavy_cap(n).
+struct SRWork {
+    uint2 *heavy;
+    uint32_t heavy_cap;
+    uint32_t *seg_nt;
+    uint32_t seg_cap;
+    uint32_t *ctl;  // [0] dense slices listed, [1] next unit
+};
+uint32_t shortrange_heavy_cap(uint32_t n);
+
 // pair_counter: when non-null, the launch adds its in-range pair count to it.
 cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,
                                 const uint32_t *perm, const uint32_t *cell_a,
                                 const uint32_t *cell_b, CellFormat fmt, const float *table,
-                                float4 *acc_out, const KickArgs &kick, cudaStream_t stream,
+                                float4 *acc_out, const KickArgs &kick, const SRWork &work, cudaStream_t stream,
                                 unsigned long long *pair_counter = nullptr);
 
 // Many boxes in one launch (the batched form).  A box's descriptor holds its
@@ -114,7 +127,7 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
                                       int nbox, uint32_t segments, size_t smem, bool fixed,
                                       const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
                                       const float *table, float4 *acc_out, const KickArgs &kick,
-                                      cudaStream_t stream, unsigned long long *pair_counter);
+                                      const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter);
 
 // ------------------------------------------------------------------- PM
 

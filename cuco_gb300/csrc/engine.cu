@@ -304,6 +304,7 @@ struct cuco_box {
     int launches = 0;
     unsigned long long *pair_counter = nullptr;
     cudaEvent_t tstart = nullptr, tstop = nullptr;
+    SRWork work{};  // the short range's work-plan scratch
 };
 
 namespace {
@@ -378,9 +379,9 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
         k.acc_pm_s = pm ? b->acc_pm_s : nullptr;
         k.acc_pm_out = pm ? b->acc_pm : nullptr;
         CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, b->sorted_perm, b->cell_off,
-                                   nullptr, kCellOffsets, b->table, b->acc_pp, k, b->stream,
+                                   nullptr, kCellOffsets, b->table, b->acc_pp, k, b->work, b->stream,
                                    b->timing ? b->pair_counter : nullptr));
-        b->launches += 1;
+        b->launches += 2;  // work plan + persistent short range
     } else if (pm) {
         CUCO_TRY(scatter4(b->acc_pm_s, b->sorted_perm, b->acc_pm, b->n, b->stream));
         b->launches += 1;
@@ -463,8 +464,12 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         (s = alloc(&b->perm_alt, n)) ||
         (s = alloc(&b->hist, sort_hist_entries(b->n, b->key_bits, 8))) ||
         (s = alloc(&b->cell_off, (size_t)b->ncells + 1)) || (s = alloc(&b->table, kNTab)) ||
-        (s = alloc(&b->stage3, 3 * n)) || (s = alloc(&b->pair_counter, 1)))
+        (s = alloc(&b->stage3, 3 * n)) || (s = alloc(&b->pair_counter, 1)) ||
+        (s = alloc(&b->work.heavy, shortrange_heavy_cap(b->n))) || (s = alloc(&b->work.seg_nt, b->ncells)) ||
+        (s = alloc(&b->work.ctl, 2)))
         return fail(s);
+    b->work.heavy_cap = shortrange_heavy_cap(b->n);
+    b->work.seg_cap = b->ncells;  // G^3 covers every segment length
     cudaMemset(b->pair_counter, 0, sizeof(unsigned long long));
     std::vector<float> t(kNTab);
     shortrange_table(t.data());
@@ -503,6 +508,9 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     cudaFree(b->table);
     cudaFree(b->stage3);
     cudaFree(b->pair_counter);
+    cudaFree(b->work.heavy);
+    cudaFree(b->work.seg_nt);
+    cudaFree(b->work.ctl);
     if (b->tstart) cudaEventDestroy(b->tstart);
     if (b->tstop) cudaEventDestroy(b->tstop);
     if (b->pm.rho) pm_plan_destroy(&b->pm);

@@ -316,7 +316,10 @@ struct cuco_ensemble {
     size_t cap_n = 0, cap_hist = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
            cap_green = 0, cap_tw = 0, cap_table = 0, cap_pbeg = 0, cap_segbase = 0, cap_drift = 0, cap_pm = 0,
            cap_kicks = 0, cap_factors = 0, cap_counter = 0, cap_sr = 0, cap_hfactors = 0, cap_hkicks = 0,
-           cap_mapz = 0, cap_mapa = 0;
+           cap_mapz = 0, cap_mapa = 0, cap_heavy = 0, cap_segnt = 0, cap_ctl = 0;
+    // the short range's work-plan scratch
+    uint2 *sr_heavy = nullptr;
+    uint32_t *sr_segnt = nullptr, *sr_ctl = nullptr;
 };
 
 namespace {
@@ -344,10 +347,11 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
     k.vel = kick ? e->vel : nullptr;
     k.acc_pm_s = e->acc_pm_s;
     k.acc_pm_out = e->acc_pm;
+    SRWork w{e->sr_heavy, (uint32_t)e->cap_heavy, e->sr_segnt, (uint32_t)e->cap_segnt, e->sr_ctl};
     CUCO_TRY(launch_shortrange_multi(e->d_sr, e->d_kicks, e->d_segbase, e->nbox, e->segments, e->sr_smem, e->fixed,
-                                     e->spos, e->sorted_perm, e->cell_off, e->table, e->acc_pp, k, e->stream,
+                                     e->spos, e->sorted_perm, e->cell_off, e->table, e->acc_pp, k, w, e->stream,
                                      e->count_pairs ? e->pair_counter : nullptr));
-    e->launches++;
+    e->launches += 2;  // work plan + persistent short range
     return CUCO_OK;
 }
 
@@ -580,7 +584,9 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
         segbase[b + 1] = segbase[b] + nseg;
         sr_smem = std::max(sr_smem, sm);
     }
-    if ((s = grow(e->d_mapz, e->cap_mapz, mapz.size(), st)) || (s = grow(e->d_mapa, e->cap_mapa, mapa.size(), st)))
+    if ((s = grow(e->d_mapz, e->cap_mapz, mapz.size(), st)) || (s = grow(e->d_mapa, e->cap_mapa, mapa.size(), st)) ||
+        (s = grow(e->sr_heavy, e->cap_heavy, (size_t)shortrange_heavy_cap((uint32_t)n) + 16u * nbox, st)) ||
+        (s = grow(e->sr_segnt, e->cap_segnt, (size_t)segbase[nbox], st)) || (s = grow(e->sr_ctl, e->cap_ctl, 2, st)))
         return s;
     if (cudaStreamSynchronize(st) != cudaSuccess ||
         cudaMemcpy(e->table, tab.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -676,7 +682,8 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
                     (void *)e->spec,
                     (void *)e->green, (void *)e->tw, (void *)e->table, (void *)e->d_pbeg, (void *)e->d_segbase,
                     (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, (void *)e->d_sr,
-                    (void *)e->d_kicks, (void *)e->d_factors, (void *)e->pair_counter})
+                    (void *)e->d_kicks, (void *)e->d_factors, (void *)e->pair_counter, (void *)e->sr_heavy,
+                    (void *)e->sr_segnt, (void *)e->sr_ctl})
         if (p && e->stream) cudaFreeAsync(p, e->stream);
     if (e->stream) cudaStreamSynchronize(e->stream);
     if (e->h_factors) cudaFreeHost(e->h_factors);

@@ -39,6 +39,7 @@
 // L < 2^23) and dx exact for ~97% of pairs; pairs whose r^2 lies within
 // 4e-7 of rcut^2 or whose asmthfac*r lies within 4e-7 (relative) of a bin edge
 // are decided in double as gravlist.cpp:298-320 does.
+#include <algorithm>
 #include <cstring>
 
 #include "common.cuh"
@@ -53,6 +54,9 @@ constexpr int kMaxStage = 2048;  // staged sources per chunk (32 KB)
 constexpr int kMaxR = 8;         // neighbour reach in cells (the reference's G = PMGRID needs 6)
 constexpr int kMaxCols = (2 * kMaxR + 1) * (2 * kMaxR + 1);
 constexpr int kMaxSeg = 8;
+// A unit of work is at most kTMax targets: a segment with that many, or a
+// kTMax slice of a denser segment.
+constexpr int kTMax = 128;
 constexpr unsigned kFull = 0xffffffffu;
 
 struct ColumnSet {
@@ -124,17 +128,20 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
-// The kernel body for one segment `seg` of one box (p, cs); kick_pp/kick_pm
-// are that box's kick factors.
+// The body for one unit: the targets [slice_lo, slice_hi) (counted from the
+// segment's first target) of segment `seg` of one box (p, cs); kick_pp/kick_pm
+// are that box's kick factors.  A unit has at most kTMax targets.
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
 __device__ __forceinline__ void shortrange_segment(
-    const ShortRangeParams &p, const ColumnSet &cs, const int seg, const double kick_pp, const double kick_pm,
-    const float4 *__restrict__ spos, const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
-    const uint32_t *__restrict__ cb, const float *__restrict__ table_g, float4 *__restrict__ acc_out,
-    const KickArgs &kick, unsigned long long *__restrict__ pair_counter) {
+    const ShortRangeParams &p, const ColumnSet &cs, const int seg, const uint32_t slice_lo,
+    const uint32_t slice_hi, const double kick_pp, const double kick_pm, const float4 *__restrict__ spos,
+    const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
+    const float *__restrict__ table_g, float4 *__restrict__ acc_out, const KickArgs &kick,
+    unsigned long long *__restrict__ pair_counter) {
     extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
     __shared__ uint32_t s_wdelta[kWarps][32];
+    __shared__ float s_acc[6][kTMax];  // multi-chunk units: per-target sums (and FIXED error terms)
 
     const int G = p.grid;
     const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
@@ -187,8 +194,10 @@ __device__ __forceinline__ void shortrange_segment(
         s_tend = found ? te : tb;
     }
     __syncthreads();
-    const uint32_t t_begin = s_tbegin, t_end = s_tend;
-    if (t_begin == t_end) return;
+    const uint32_t t_seg = s_tbegin, t_seg_end = s_tend;
+    const uint32_t t_begin = t_seg + min(slice_lo, t_seg_end - t_seg);
+    const uint32_t t_end = t_seg + min(slice_hi, t_seg_end - t_seg);
+    if (t_begin >= t_end) return;
 
     for (int i = tid; i < kNTab; i += kThreads) tab[i] = table_g[i];
     if (tid == 0) src[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
@@ -277,7 +286,6 @@ __device__ __forceinline__ void shortrange_segment(
     const float rc2_lo = FIXED ? p.rcut2 : p.rcut2 * (1.f - 2.f * kEdge);
     const float rc2_hi = FIXED ? p.rcut2 : p.rcut2 * (1.f + 2.f * kEdge);
     const double rcut2_d = (double)p.rcut * (double)p.rcut;
-    bool staged = false;
     uint32_t npairs = 0;
     uint32_t *wdelta = s_wdelta[warp];
     const uint32_t lt_mask = (1u << lane) - 1u, le_mask = lt_mask | (1u << lane);
@@ -351,138 +359,98 @@ __device__ __forceinline__ void shortrange_segment(
 
     // One target per warp: lane k culls columns k, k+32, ...; the warp then
     // walks each non-empty column range with all lanes on consecutive sources.
+    // Chunk-major: each chunk of staged sources is staged once, and every
+    // target of the unit runs against it; with more than one chunk the
+    // targets' sums are carried in shared memory from chunk to chunk.
     const uint32_t rounds = (nt + kWarps - 1) / kWarps;
-    for (uint32_t round = 0; round < rounds; ++round) {
-        const uint32_t t = round * kWarps + warp;
-        const bool active = t < nt;  // warp-uniform
-        const float4 praw = active ? spos[t_begin + t] : make_float4(0.f, 0.f, 0.f, 0.f);
-        // pt: absolute float coordinates for the culling (fixed point rounded
-        // to float: the culling margin covers it); tx..tz: origin-relative
-        float4 pt = praw;
-        if (FIXED) {
-            pt = make_float4(__fmul_rn((float)__float_as_uint(praw.x), fs),
-                             __fmul_rn((float)__float_as_uint(praw.y), fs),
-                             __fmul_rn((float)__float_as_uint(praw.z), fs), 0.f);
-            const float4 tr = rel(praw);
-            tx = tr.x;
-            ty = tr.y;
-            tz = tr.z;
-        } else {
-            tx = pt.x - ox;
-            ty = pt.y - oy;
-            tz = pt.z - oz;
-        }
-        float ax = 0.f, ay = 0.f, az = 0.f, bx = 0.f, by = 0.f, bz = 0.f;
-        for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
-            const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
-            if (!(single_chunk && staged)) {
-                __syncthreads();
-                // stage [c0, c1): warp per run
-                for (int rr = warp; rr < ncols * 2; rr += kWarps) {
-                    const Run r = runs[rr];
-                    if (r.cnt == 0) continue;
-                    const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
-                    uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
-                    for (uint32_t s0 = lo + lane; s0 < hi; s0 += 64) {
-                        const uint32_t s1 = s0 + 32;
-                        const float4 a0 = spos[r.gsrc + (s0 - r.soff)];
-                        float4 a1 = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (s1 < hi) a1 = spos[r.gsrc + (s1 - r.soff)];
-                        if (FIXED) {
-                            src[s0 - c0] = rel(a0);
-                            if (s1 < hi) src[s1 - c0] = rel(a1);
-                        } else {
-                            src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
-                            if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
-                        }
+    const float mg = p.mass * p.G;
+
+    // The target's force from the sources of chunk [c0, c1), warp-reduced
+    // (lane 0 holds it); FIXED: compensated, with the error terms in e*.
+    auto target_chunk = [&](float4 pt, uint32_t c0, uint32_t c1, float &ax, float &ay, float &az, float &ex,
+                            float &ey, float &ez) {
+        float bx = 0.f, by = 0.f, bz = 0.f;
+        ax = ay = az = 0.f;
+        for (int cb = 0; cb < ncols; cb += 32) {
+            const int col = cb + lane;
+            uint32_t b = 0, e = 0;
+            if (col < ncols) {
+                const float4 g = cgeo[col];
+                const float ddx = fmaxf(fmaxf(g.x - pt.x, pt.x - g.y), 0.f);
+                const float ddy = fmaxf(fmaxf(g.z - pt.y, pt.y - g.w), 0.f);
+                // explicit roundings: the candidate set (hence the lane each
+                // candidate lands on) must not depend on how the compiler
+                // contracts this expression in a given instantiation
+                const float q = __fsub_rn(rc2m, __fmaf_rn(ddy, ddy, __fmul_rn(ddx, ddx)));
+                if (q >= 0.f) {
+                    // half-height of the cut disc over this column (an
+                    // approximate square root: the margin covers it)
+                    const float hz = __fmul_rn(q, rsqrtf(fmaxf(q, 1e-30f)));
+                    const int zlo = max(__float2int_rd(__fmaf_rn(pt.z - hz, winv, -zbase)), 0);
+                    const int zhi = min(__float2int_rd(__fmaf_rn(pt.z + hz, winv, -zbase)), nz - 1);
+                    if (zlo <= zhi) {
+                        b = max(coff[col * zst + zlo], c0);
+                        e = min(coff[col * zst + zhi + 1], c1);
                     }
                 }
-                __syncthreads();
-                staged = true;
             }
-            if (!active) continue;
-            for (int cb = 0; cb < ncols; cb += 32) {
-                const int col = cb + lane;
-                uint32_t b = 0, e = 0;
-                if (col < ncols) {
-                    const float4 g = cgeo[col];
-                    const float ddx = fmaxf(fmaxf(g.x - pt.x, pt.x - g.y), 0.f);
-                    const float ddy = fmaxf(fmaxf(g.z - pt.y, pt.y - g.w), 0.f);
-                    // explicit roundings: the candidate set (hence the lane each
-                    // candidate lands on) must not depend on how the compiler
-                    // contracts this expression in a given instantiation
-                    const float q = __fsub_rn(rc2m, __fmaf_rn(ddy, ddy, __fmul_rn(ddx, ddx)));
-                    if (q >= 0.f) {
-                        // half-height of the cut disc over this column (an
-                        // approximate square root: the margin covers it)
-                        const float hz = __fmul_rn(q, rsqrtf(fmaxf(q, 1e-30f)));
-                        const int zlo = max(__float2int_rd(__fmaf_rn(pt.z - hz, winv, -zbase)), 0);
-                        const int zhi = min(__float2int_rd(__fmaf_rn(pt.z + hz, winv, -zbase)), nz - 1);
-                        if (zlo <= zhi) {
-                            b = max(coff[col * zst + zlo], c0);
-                            e = min(coff[col * zst + zhi + 1], c1);
-                        }
-                    }
-                }
-                // The column ranges, concatenated, form one candidate list of
-                // length T; ps is this lane's column start in it.
-                const uint32_t len = b < e ? e - b : 0u;
-                uint32_t ps = len;
+            // The column ranges, concatenated, form one candidate list of
+            // length T; ps is this lane's column start in it.
+            const uint32_t len = b < e ? e - b : 0u;
+            uint32_t ps = len;
 #pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const uint32_t v = __shfl_up_sync(kFull, ps, off);
-                    if (lane >= off) ps += v;
-                }
-                const uint32_t T = __shfl_sync(kFull, ps, 31);
-                ps -= len;
-                if (T == 0) continue;
-                // the k-th non-empty column's shift from list to staged index
-                const uint32_t nonempty = __ballot_sync(kFull, len > 0);
-                if (len > 0) wdelta[__popc(nonempty & lt_mask)] = b - c0 - ps;
-                if (len == 0) ps = 0xffffffffu;  // marks no start
-                __syncwarp();
-                // Each window of 64 candidates: one bit per column start, so a
-                // lane's column is (columns started before the window) +
-                // (starts at or below its position) - 1.  Positions at or past
-                // T read the sentinel.  The rare-case law runs under a
-                // warp-uniform branch.
-                uint32_t before = 0, base = 0;
-                for (; base + 32u < T; base += 64) {
-                    const uint32_t r0 = ps - base, r1 = r0 - 32u;
-                    const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
-                    const uint32_t m1 = __reduce_or_sync(kFull, r1 < 32u ? 1u << r1 : 0u);
-                    const uint32_t n0 = before + __popc(m0);
-                    const uint32_t k0 = base + lane, k1 = k0 + 32;
-                    const uint32_t i0 = k0 + wdelta[before + __popc(m0 & le_mask) - 1];
-                    const uint32_t d1 = wdelta[n0 + __popc(m1 & le_mask) - 1];
-                    const uint32_t i1 = k1 < T ? k1 + d1 : (uint32_t)kMaxStage;
-                    const float4 s0 = src[i0], s1 = src[i1];
-                    const bool x0 = pair_fast(s0, ax, ay, az);
-                    const bool x1 = pair_fast(s1, bx, by, bz);
-                    if (__any_sync(kFull, x0 || x1)) {
-                        if (x0) pair_slow(s0, ax, ay, az);
-                        if (x1) pair_slow(s1, bx, by, bz);
-                    }
-                    before = n0 + __popc(m1);
-                }
-                if (base < T) {
-                    const uint32_t r0 = ps - base;
-                    const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
-                    const uint32_t k0 = base + lane;
-                    const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
-                    const float4 s0 = src[k0 < T ? k0 + d0 : (uint32_t)kMaxStage];
-                    const bool x0 = pair_fast(s0, ax, ay, az);
-                    if (__any_sync(kFull, x0)) {
-                        if (x0) pair_slow(s0, ax, ay, az);
-                    }
-                }
-                __syncwarp();
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t v = __shfl_up_sync(kFull, ps, off);
+                if (lane >= off) ps += v;
             }
+            const uint32_t T = __shfl_sync(kFull, ps, 31);
+            ps -= len;
+            if (T == 0) continue;
+            // the k-th non-empty column's shift from list to staged index
+            const uint32_t nonempty = __ballot_sync(kFull, len > 0);
+            if (len > 0) wdelta[__popc(nonempty & lt_mask)] = b - c0 - ps;
+            if (len == 0) ps = 0xffffffffu;  // marks no start
+            __syncwarp();
+            // Each window of 64 candidates: one bit per column start, so a
+            // lane's column is (columns started before the window) +
+            // (starts at or below its position) - 1.  Positions at or past
+            // T read the sentinel.  The rare-case law runs under a
+            // warp-uniform branch.
+            uint32_t before = 0, base = 0;
+            for (; base + 32u < T; base += 64) {
+                const uint32_t r0 = ps - base, r1 = r0 - 32u;
+                const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
+                const uint32_t m1 = __reduce_or_sync(kFull, r1 < 32u ? 1u << r1 : 0u);
+                const uint32_t n0 = before + __popc(m0);
+                const uint32_t k0 = base + lane, k1 = k0 + 32;
+                const uint32_t i0 = k0 + wdelta[before + __popc(m0 & le_mask) - 1];
+                const uint32_t d1 = wdelta[n0 + __popc(m1 & le_mask) - 1];
+                const uint32_t i1 = k1 < T ? k1 + d1 : (uint32_t)kMaxStage;
+                const float4 s0 = src[i0], s1 = src[i1];
+                const bool x0 = pair_fast(s0, ax, ay, az);
+                const bool x1 = pair_fast(s1, bx, by, bz);
+                if (__any_sync(kFull, x0 || x1)) {
+                    if (x0) pair_slow(s0, ax, ay, az);
+                    if (x1) pair_slow(s1, bx, by, bz);
+                }
+                before = n0 + __popc(m1);
+            }
+            if (base < T) {
+                const uint32_t r0 = ps - base;
+                const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
+                const uint32_t k0 = base + lane;
+                const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
+                const float4 s0 = src[k0 < T ? k0 + d0 : (uint32_t)kMaxStage];
+                const bool x0 = pair_fast(s0, ax, ay, az);
+                if (__any_sync(kFull, x0)) {
+                    if (x0) pair_slow(s0, ax, ay, az);
+                }
+            }
+            __syncwarp();
         }
-        if (!active) continue;
+        ex = ey = ez = 0.f;
         if (FIXED) {
             // compensated: two-sum of the lanes' partial sums, errors carried
-            float ex, ey, ez;
             two_sum(ax, bx, ax, ex);
             two_sum(ay, by, ay, ey);
             two_sum(az, bz, az, ez);
@@ -499,9 +467,6 @@ __device__ __forceinline__ void shortrange_segment(
                 two_sum(az, oz_, az, e);
                 ez = __fadd_rn(ez, __fadd_rn(oez, e));
             }
-            ax = __fadd_rn(ax, ex);
-            ay = __fadd_rn(ay, ey);
-            az = __fadd_rn(az, ez);
         } else {
             ax += bx;
             ay += by;
@@ -513,32 +478,137 @@ __device__ __forceinline__ void shortrange_segment(
                 az += __shfl_xor_sync(kFull, az, off);
             }
         }
-        if (lane == 0) {
-            const uint32_t i = t_begin + t;
-            const uint32_t o = perm[i];
-            const float mg = p.mass * p.G;
-            const float4 a = make_float4(ax * mg, ay * mg, az * mg, 0.f);
-            acc_out[o] = a;
-            float4 gpm = make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+
+    // the target's coordinates: pt absolute float (for the culling; fixed
+    // point rounded to float, which the culling margin covers), tx..tz
+    // origin-relative (for the pair law)
+    auto load_target = [&](uint32_t t) {
+        const float4 praw = spos[t_begin + t];
+        float4 pt = praw;
+        if (FIXED) {
+            pt = make_float4(__fmul_rn((float)__float_as_uint(praw.x), fs),
+                             __fmul_rn((float)__float_as_uint(praw.y), fs),
+                             __fmul_rn((float)__float_as_uint(praw.z), fs), 0.f);
+            const float4 tr = rel(praw);
+            tx = tr.x;
+            ty = tr.y;
+            tz = tr.z;
+        } else {
+            tx = pt.x - ox;
+            ty = pt.y - oy;
+            tz = pt.z - oz;
+        }
+        return pt;
+    };
+
+    // force (already scaled by m G) to original order, PM scatter and kick
+    auto epilogue = [&](uint32_t t, float4 a) {
+        const uint32_t i = t_begin + t;
+        const uint32_t o = perm[i];
+        acc_out[o] = a;
+        float4 gpm = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (kick.acc_pm_s) {
+            gpm = kick.acc_pm_s[i];
+            if (kick.acc_pm_out) kick.acc_pm_out[o] = gpm;
+        }
+        if (KICK) {
+            float4 v = kick.vel[o];
+            // vel += GravAccel*dt; vel += GravPM*dt (timestep.c:57-58,88), in
+            // float (the reference rounds each product to float first)
+            const float kp = (float)kick_pp, km = (float)kick_pm;
+            v.x += __fmul_rn(a.x, kp);
+            v.y += __fmul_rn(a.y, kp);
+            v.z += __fmul_rn(a.z, kp);
             if (kick.acc_pm_s) {
-                gpm = kick.acc_pm_s[i];
-                if (kick.acc_pm_out) kick.acc_pm_out[o] = gpm;
+                v.x = __fmaf_rn(gpm.x, km, v.x);
+                v.y = __fmaf_rn(gpm.y, km, v.y);
+                v.z = __fmaf_rn(gpm.z, km, v.z);
             }
-            if (KICK) {
-                float4 v = kick.vel[o];
-                // vel += GravAccel*dt; vel += GravPM*dt (timestep.c:57-58,88), in
-                // float (the reference rounds each product to float first)
-                const float kp = (float)kick_pp, km = (float)kick_pm;
-                v.x += __fmul_rn(a.x, kp);
-                v.y += __fmul_rn(a.y, kp);
-                v.z += __fmul_rn(a.z, kp);
-                if (kick.acc_pm_s) {
-                    v.x = __fmaf_rn(gpm.x, km, v.x);
-                    v.y = __fmaf_rn(gpm.y, km, v.y);
-                    v.z = __fmaf_rn(gpm.z, km, v.z);
+            kick.vel[o] = v;
+        }
+    };
+
+    // stage [c0, c1): warp per run
+    auto stage = [&](uint32_t c0, uint32_t c1) {
+        for (int rr = warp; rr < ncols * 2; rr += kWarps) {
+            const Run r = runs[rr];
+            if (r.cnt == 0) continue;
+            const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
+            uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
+            for (uint32_t s0 = lo + lane; s0 < hi; s0 += 64) {
+                const uint32_t s1 = s0 + 32;
+                const float4 a0 = spos[r.gsrc + (s0 - r.soff)];
+                float4 a1 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (s1 < hi) a1 = spos[r.gsrc + (s1 - r.soff)];
+                if (FIXED) {
+                    src[s0 - c0] = rel(a0);
+                    if (s1 < hi) src[s1 - c0] = rel(a1);
+                } else {
+                    src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
+                    if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
                 }
-                kick.vel[o] = v;
             }
+        }
+    };
+
+    if (single_chunk) {
+        stage(0, total);
+        __syncthreads();
+        for (uint32_t round = 0; round < rounds; ++round) {
+            const uint32_t t = round * kWarps + warp;
+            if (t >= nt) break;  // warp-uniform; no barrier follows
+            const float4 pt = load_target(t);
+            float ax, ay, az, ex, ey, ez;
+            target_chunk(pt, 0, total, ax, ay, az, ex, ey, ez);
+            if (FIXED) {
+                ax = __fadd_rn(ax, ex);
+                ay = __fadd_rn(ay, ey);
+                az = __fadd_rn(az, ez);
+            }
+            if (lane == 0) epilogue(t, make_float4(ax * mg, ay * mg, az * mg, 0.f));
+        }
+    } else {
+        for (uint32_t t = tid; t < nt; t += kThreads)
+            for (int k = 0; k < 6; ++k) s_acc[k][t] = 0.f;
+        for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
+            const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
+            __syncthreads();  // the previous chunk is no longer read; s_acc zeroed
+            stage(c0, c1);
+            __syncthreads();
+            for (uint32_t round = 0; round < rounds; ++round) {
+                const uint32_t t = round * kWarps + warp;
+                if (t >= nt) break;
+                const float4 pt = load_target(t);
+                float ax, ay, az, ex, ey, ez;
+                target_chunk(pt, c0, c1, ax, ay, az, ex, ey, ez);
+                if (lane == 0) {
+                    // only this warp touches target t's accumulators
+                    if (FIXED) {
+                        float e;
+                        two_sum(s_acc[0][t], ax, s_acc[0][t], e);
+                        s_acc[3][t] = __fadd_rn(s_acc[3][t], __fadd_rn(ex, e));
+                        two_sum(s_acc[1][t], ay, s_acc[1][t], e);
+                        s_acc[4][t] = __fadd_rn(s_acc[4][t], __fadd_rn(ey, e));
+                        two_sum(s_acc[2][t], az, s_acc[2][t], e);
+                        s_acc[5][t] = __fadd_rn(s_acc[5][t], __fadd_rn(ez, e));
+                    } else {
+                        s_acc[0][t] += ax;
+                        s_acc[1][t] += ay;
+                        s_acc[2][t] += az;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t t = tid; t < nt; t += kThreads) {
+            float ax = s_acc[0][t], ay = s_acc[1][t], az = s_acc[2][t];
+            if (FIXED) {
+                ax = __fadd_rn(ax, s_acc[3][t]);
+                ay = __fadd_rn(ay, s_acc[4][t]);
+                az = __fadd_rn(az, s_acc[5][t]);
+            }
+            epilogue(t, make_float4(ax * mg, ay * mg, az * mg, 0.f));
         }
     }
     if (COUNT) {
@@ -548,33 +618,131 @@ __device__ __forceinline__ void shortrange_segment(
     }
 }
 
+// The work plan of one launch: each segment's target count, and the kTMax
+// slices of the segments that have more (appended in any order: which CTA
+// computes a target does not change its result).
+template <CellFormat FMT>
+__device__ __forceinline__ void plan_segment(const ShortRangeParams &p, int S, uint32_t seg, uint32_t gseg,
+                                             const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
+                                             const SRWork &w) {
+    const int G = p.grid, segs = G / S;
+    const int ix = seg / (G * segs), iy = (seg / segs) % G, iz0 = (seg % segs) * S;
+    uint32_t tb = 0, te = 0;
+    bool found = false;
+    for (int k = 0; k < S; ++k) {
+        uint32_t st, cn;
+        cell_range<FMT>(ca, cb, p.cell_base + ((uint32_t)ix * G + iy) * G + iz0 + k, &st, &cn);
+        if (cn) {
+            if (!found) tb = st;
+            found = true;
+            te = st + cn;
+        }
+    }
+    const uint32_t nt = found ? te - tb : 0u;
+    w.seg_nt[gseg] = nt;
+    if (nt > (uint32_t)kTMax) {
+        const uint32_t c = (nt + kTMax - 1) / kTMax;
+        const uint32_t o = atomicAdd(&w.ctl[0], c);
+        for (uint32_t k = 0; k < c; ++k)
+            if (o + k < w.heavy_cap) w.heavy[o + k] = make_uint2(gseg, k);
+    }
+}
+
+template <CellFormat FMT>
+__global__ void k_sr_plan(const __grid_constant__ ShortRangeParams p, int S, uint32_t nseg,
+                          const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
+                          const __grid_constant__ SRWork w) {
+    const uint32_t seg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (seg < nseg) plan_segment<FMT>(p, S, seg, seg, ca, cb, w);
+}
+
+// The next unit for a persistent CTA: the dense segments' slices first (the
+// longest work), then every other non-empty segment whole.  Returns false
+// when none is left; `skip` for a segment that is empty or dense.
+__device__ __forceinline__ bool next_unit(const SRWork &w, uint32_t nseg, uint32_t *seg, uint32_t *lo,
+                                          bool *skip) {
+    __shared__ uint32_t s_item;
+    __syncthreads();  // the previous unit's shared memory is no longer read
+    if (threadIdx.x == 0) s_item = atomicAdd(&w.ctl[1], 1u);
+    __syncthreads();
+    const uint32_t item = s_item, nh = min(w.ctl[0], w.heavy_cap);
+    *skip = false;
+    if (item < nh) {
+        const uint2 h = w.heavy[item];
+        *seg = h.x;
+        *lo = h.y * kTMax;
+        return true;
+    }
+    *seg = item - nh;
+    if (*seg >= nseg) return false;
+    const uint32_t c = w.seg_nt[*seg];
+    *skip = c == 0 || c > (uint32_t)kTMax;
+    *lo = 0;
+    return true;
+}
+
+// Persistent: as many CTAs as fit on the GPU, each taking units until none
+// is left, so a few dense segments no longer leave most SMs idle.
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
 __global__ void __launch_bounds__(kThreads, 4)
-    k_shortrange(const __grid_constant__ ShortRangeParams p, const __grid_constant__ ColumnSet cs,
-                 const float4 *__restrict__ spos, const uint32_t *__restrict__ perm,
-                 const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
-                 const float *__restrict__ table_g, float4 *__restrict__ acc_out,
-                 const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
-    shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, blockIdx.x, kick.kick_pp, kick.kick_pm, spos, perm, ca,
-                                                cb, table_g, acc_out, kick, pair_counter);
+    k_shortrange(const __grid_constant__ ShortRangeParams p, const __grid_constant__ ColumnSet cs, uint32_t nseg,
+                 const __grid_constant__ SRWork w, const float4 *__restrict__ spos,
+                 const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
+                 const uint32_t *__restrict__ cb, const float *__restrict__ table_g,
+                 float4 *__restrict__ acc_out, const __grid_constant__ KickArgs kick,
+                 unsigned long long *__restrict__ pair_counter) {
+    uint32_t seg, lo;
+    bool skip;
+    while (next_unit(w, nseg, &seg, &lo, &skip)) {
+        if (skip) continue;
+        shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, (int)seg, lo, lo + kTMax, kick.kick_pp, kick.kick_pm,
+                                                    spos, perm, ca, cb, table_g, acc_out, kick, pair_counter);
+    }
 }
 
 // Many boxes in one launch: segments numbered box after box (seg_base, nbox+1
 // entries); particles, cells (p.cell_base) and outputs are the concatenated
 // arrays of all boxes.
+__global__ void k_sr_plan_multi(const SRBoxDesc *__restrict__ boxes, const uint32_t *__restrict__ seg_base,
+                                int nbox, uint32_t nseg, const uint32_t *__restrict__ cell_off,
+                                const __grid_constant__ SRWork w) {
+    const uint32_t gseg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gseg >= nseg) return;
+    const int b = find_box(seg_base, nbox, gseg);
+    const SRBoxDesc &d = boxes[b];
+    plan_segment<kCellOffsets>(d.p, d.cs.S, gseg - seg_base[b], gseg, cell_off, nullptr, w);
+}
+
 template <bool KICK, bool COUNT, bool FIXED>
 __global__ void __launch_bounds__(kThreads, 4)
     k_shortrange_multi(const SRBoxDesc *__restrict__ boxes, const double2 *__restrict__ kicks,
-                       const uint32_t *__restrict__ seg_base, int nbox, const float4 *__restrict__ spos,
+                       const uint32_t *__restrict__ seg_base, int nbox, uint32_t nseg,
+                       const __grid_constant__ SRWork w, const float4 *__restrict__ spos,
                        const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cell_off,
                        const float *__restrict__ table_g, float4 *__restrict__ acc_out,
                        const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
-    const int b = find_box(seg_base, nbox, blockIdx.x);
-    const SRBoxDesc &d = boxes[b];
-    const double2 k = KICK ? kicks[b] : make_double2(0.0, 0.0);
-    shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, d.cs, (int)(blockIdx.x - seg_base[b]), k.x, k.y,
-                                                         spos, perm, cell_off, nullptr, table_g, acc_out, kick,
-                                                         pair_counter);
+    uint32_t seg, lo;
+    bool skip;
+    while (next_unit(w, nseg, &seg, &lo, &skip)) {
+        if (skip) continue;
+        const int b = find_box(seg_base, nbox, seg);
+        const SRBoxDesc &d = boxes[b];
+        const double2 k = KICK ? kicks[b] : make_double2(0.0, 0.0);
+        shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, d.cs, (int)(seg - seg_base[b]), lo, lo + kTMax,
+                                                             k.x, k.y, spos, perm, cell_off, nullptr, table_g,
+                                                             acc_out, kick, pair_counter);
+    }
+}
+
+// CTAs a persistent launch of `kernel` keeps resident on this device.
+template <typename K>
+unsigned persistent_grid(K kernel, size_t smem) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, smem) != cudaSuccess || per < 1)
+        per = 1;
+    return (unsigned)(std::max(sms, 1) * per);
 }
 
 // Neighbour columns (dx, dy) whose xy cell distance is within rcut (+margin).
@@ -612,8 +780,8 @@ bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
 }  // namespace
 
 template <CellFormat FMT, bool KICK, bool FIXED>
-void launch_fmt_kick(unsigned blocks, cudaStream_t stream, const ShortRangeParams &p,
-                     const ColumnSet &cs, const float4 *sorted_pos, const uint32_t *perm,
+void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const ColumnSet &cs, uint32_t nseg,
+                     const SRWork &work, const float4 *sorted_pos, const uint32_t *perm,
                      const uint32_t *cell_a, const uint32_t *cell_b, const float *table,
                      float4 *acc_out, const KickArgs &kick, unsigned long long *counter) {
     const size_t sm = smem_bytes(cs.ncols, cs.S + 2 * cs.R);
@@ -627,17 +795,22 @@ void launch_fmt_kick(unsigned blocks, cudaStream_t stream, const ShortRangeParam
     }();
     (void)attr;
     if (counter)
-        k_shortrange<FMT, KICK, true, FIXED><<<blocks, kThreads, sm, stream>>>(
-            p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
+        k_shortrange<FMT, KICK, true, FIXED><<<persistent_grid(k_shortrange<FMT, KICK, true, FIXED>, sm), kThreads,
+                                               sm, stream>>>(p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b,
+                                                             table, acc_out, kick, counter);
     else
-        k_shortrange<FMT, KICK, false, FIXED><<<blocks, kThreads, sm, stream>>>(
-            p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, counter);
+        k_shortrange<FMT, KICK, false, FIXED><<<persistent_grid(k_shortrange<FMT, KICK, false, FIXED>, sm),
+                                                kThreads, sm, stream>>>(p, cs, nseg, work, sorted_pos, perm,
+                                                                        cell_a, cell_b, table, acc_out, kick,
+                                                                        counter);
 }
+
+uint32_t shortrange_heavy_cap(uint32_t n) { return 2u * (n / kTMax) + 16u; }
 
 cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,
                                 const uint32_t *perm, const uint32_t *cell_a,
                                 const uint32_t *cell_b, CellFormat fmt, const float *table,
-                                float4 *acc_out, const KickArgs &kick, cudaStream_t stream,
+                                float4 *acc_out, const KickArgs &kick, const SRWork &work, cudaStream_t stream,
                                 unsigned long long *pair_counter) {
     ColumnSet cs;
     if (!build_columns(p, &cs)) {
@@ -647,27 +820,36 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
     }
     if (p.n == 0) return CUCO_OK;
     const int G = p.grid;
-    const unsigned blocks = (unsigned)G * G * (G / cs.S);
+    const uint32_t nseg = (uint32_t)G * G * (G / cs.S);
+    if (nseg > work.seg_cap || work.heavy_cap < shortrange_heavy_cap(p.n)) {
+        set_error("short range: work-plan scratch too small for this grid or particle count");
+        return CUCO_ERR_INVALID;
+    }
     const bool kick_on = kick.vel != nullptr;
     if (p.fixed && fmt != kCellOffsets) {
         set_error("short range: fixed-point positions need the engine's cell-offset format");
         return CUCO_ERR_UNSUPPORTED;
     }
+    CUCO_TRY_CUDA(cudaMemsetAsync(work.ctl, 0, 2 * sizeof(uint32_t), stream));
+    if (fmt == kCellOffsets)
+        k_sr_plan<kCellOffsets><<<(nseg + 255) / 256, 256, 0, stream>>>(p, cs.S, nseg, cell_a, cell_b, work);
+    else
+        k_sr_plan<kCellStartEnd><<<(nseg + 255) / 256, 256, 0, stream>>>(p, cs.S, nseg, cell_a, cell_b, work);
     if (p.fixed) {
         if (kick_on)
-            launch_fmt_kick<kCellOffsets, true, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, true, true>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellOffsets, false, true>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, false, true>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     } else if (fmt == kCellOffsets) {
         if (kick_on)
-            launch_fmt_kick<kCellOffsets, true, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, true, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellOffsets, false, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, false, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     } else {
         if (kick_on)
-            launch_fmt_kick<kCellStartEnd, true, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellStartEnd, true, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellStartEnd, false, false>(blocks, stream, p, cs, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellStartEnd, false, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     }
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
@@ -693,7 +875,7 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
                                       int nbox, uint32_t segments, size_t smem, bool fixed,
                                       const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
                                       const float *table, float4 *acc_out, const KickArgs &kick,
-                                      cudaStream_t stream, unsigned long long *pair_counter) {
+                                      const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter) {
     static const size_t sm_max = smem_bytes(kMaxCols, kMaxSeg + 2 * kMaxR);
     static bool attr = [] {
         cudaFuncSetAttribute(k_shortrange_multi<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
@@ -708,12 +890,17 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
     }();
     (void)attr;
     if (!segments) return CUCO_OK;
+    if (segments > work.seg_cap) {
+        set_error("short range: work-plan scratch too small for the ensemble's segments");
+        return CUCO_ERR_INVALID;
+    }
     const SRBoxDesc *d = static_cast<const SRBoxDesc *>(descs);
     const bool kick_on = kick.vel != nullptr;
-#define CUCO_SR_MULTI(K, C, F)                                                                              \
-    k_shortrange_multi<K, C, F><<<segments, kThreads, smem, stream>>>(d, kicks, seg_base, nbox, sorted_pos, \
-                                                                     perm, cell_off, table, acc_out, kick,   \
-                                                                     pair_counter)
+    CUCO_TRY_CUDA(cudaMemsetAsync(work.ctl, 0, 2 * sizeof(uint32_t), stream));
+    k_sr_plan_multi<<<(segments + 255) / 256, 256, 0, stream>>>(d, seg_base, nbox, segments, cell_off, work);
+#define CUCO_SR_MULTI(K, C, F)                                                                                   \
+    k_shortrange_multi<K, C, F><<<persistent_grid(k_shortrange_multi<K, C, F>, smem), kThreads, smem, stream>>>( \
+        d, kicks, seg_base, nbox, segments, work, sorted_pos, perm, cell_off, table, acc_out, kick, pair_counter)
     if (fixed) {
         if (kick_on) {
             if (pair_counter) CUCO_SR_MULTI(true, true, true); else CUCO_SR_MULTI(true, false, true);
