@@ -45,77 +45,107 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 }
 
 // Stage radix for the remaining length: 4, 2, 3 or 5 (M = 2^a 3^b 5^c).
-__device__ __forceinline__ int stage_radix(int rem) {
+__host__ __device__ __forceinline__ int stage_radix(int rem) {
     return (rem & 3) == 0 ? 4 : (rem & 1) == 0 ? 2 : rem % 3 == 0 ? 3 : 5;
 }
 
-// Transform B columns of length M held in x[m*pitch + b]; returns the buffer
-// holding the result.  sign = -1: forward (e^{-i}), +1: inverse.  Stockham
-// autosort: stage with radix r over Ns already-combined points reads
-// x[j + p*M/r] (p < r), twiddles it by w^{p k M/(Ns r)} (k = j mod Ns), and
-// writes the r-point DFT to y[(j/Ns) Ns r + k + q Ns].
-__device__ float2 *fft_columns(float2 *x, float2 *y, const float2 *tw, int M, int B, int pitch,
-                               int sign) {
+// Division by a runtime d without a divide instruction: j / d is
+// umulhi(j, ceil(2^32 / d)), exact for j, d < 2^16 (checked exhaustively for
+// d <= 2048; every index here is below 2^16).
+struct FastDiv {
+    uint32_t d, inv;
+    __device__ __forceinline__ explicit FastDiv(uint32_t d_) : d(d_), inv(d_ > 1 ? (uint32_t)((0x100000000ull + d_ - 1) / d_) : 0u) {}
+    __device__ __forceinline__ uint32_t div(uint32_t j) const { return d > 1 ? __umulhi(j, inv) : j; }
+};
+
+template <int R>
+__device__ __forceinline__ void dft_small(float2 (&v)[R], int sign) {
+    if (R == 4) {
+        const float2 a0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
+        const float2 a1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
+        const float2 a2 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
+        const float2 d = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
+        // (v1 - v3) * (sign * i)
+        const float2 a3 = sign < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
+        v[0] = make_float2(a0.x + a2.x, a0.y + a2.y);
+        v[1] = make_float2(a1.x + a3.x, a1.y + a3.y);
+        v[2] = make_float2(a0.x - a2.x, a0.y - a2.y);
+        v[3] = make_float2(a1.x - a3.x, a1.y - a3.y);
+    } else if (R == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = make_float2(a.x + b.x, a.y + b.y);
+        v[1] = make_float2(a.x - b.x, a.y - b.y);
+    } else if (R == 3) {
+        // y1,2 = v0 - (v1+v2)/2 +- i s (v1-v2), s = sign sqrt(3)/2
+        const float s3 = sign * 0.866025403784438647f;
+        const float2 t = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
+        const float2 d = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
+        const float2 m = make_float2(v[0].x - 0.5f * t.x, v[0].y - 0.5f * t.y);
+        v[0] = make_float2(v[0].x + t.x, v[0].y + t.y);
+        v[1] = make_float2(m.x - s3 * d.y, m.y + s3 * d.x);
+        v[2] = make_float2(m.x + s3 * d.y, m.y - s3 * d.x);
+    } else {
+        // five-point DFT by the conjugate pairs (1,4), (2,3)
+        const float c1 = 0.309016994374947424f, c2 = -0.809016994374947424f;
+        const float s1 = sign * 0.951056516295153572f, s2 = sign * 0.587785252292473129f;
+        const float2 a1 = make_float2(v[1].x + v[R - 1].x, v[1].y + v[R - 1].y);
+        const float2 b1 = make_float2(v[1].x - v[R - 1].x, v[1].y - v[R - 1].y);
+        const float2 a2 = make_float2(v[2].x + v[R - 2].x, v[2].y + v[R - 2].y);
+        const float2 b2 = make_float2(v[2].x - v[R - 2].x, v[2].y - v[R - 2].y);
+        const float2 t1 = make_float2(v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y);
+        const float2 t2 = make_float2(v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y);
+        const float2 u1 = make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
+        const float2 u2 = make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
+        v[0] = make_float2(v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y);
+        v[1] = make_float2(t1.x - u1.y, t1.y + u1.x);      // t1 + i u1
+        v[2] = make_float2(t2.x - u2.y, t2.y + u2.x);      // t2 + i u2
+        v[R - 2] = make_float2(t2.x + u2.y, t2.y - u2.x);  // t2 - i u2
+        v[R - 1] = make_float2(t1.x + u1.y, t1.y - u1.x);  // t1 - i u1
+    }
+}
+
+// One Stockham stage of radix R over Ns already-combined points, for B = 2^bs
+// columns: reads x[j + p M/R] (p < R), twiddles it by w^{p k M/(Ns R)} (k = j
+// mod Ns), and writes the R-point DFT to y[(j/Ns) Ns R + k + q Ns].
+template <int R>
+__device__ __forceinline__ void stockham_stage(const float2 *in, float2 *out, const float2 *tw, int M, int Ns,
+                                               int bs, int pitch, int sign) {
+    const int nb = M / R, step = M / (Ns * R);
+    const FastDiv dns((uint32_t)Ns);
+    const int total = nb << bs, bmask = (1 << bs) - 1;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int b = e & bmask, j = e >> bs;
+        const int g = (int)dns.div((uint32_t)j), k = j - g * Ns;
+        const int dst = g * Ns * R + k;
+        float2 v[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) v[q] = in[(j + q * nb) * pitch + b];
+        if (k) {
+#pragma unroll
+            for (int q = 1; q < R; ++q) {
+                float2 w = tw[q * k * step];
+                if (sign > 0) w.y = -w.y;
+                v[q] = cmul(v[q], w);
+            }
+        }
+        dft_small<R>(v, sign);
+#pragma unroll
+        for (int q = 0; q < R; ++q) out[(dst + q * Ns) * pitch + b] = v[q];
+    }
+}
+
+// Transform B = 2^bs columns of length M held in x[m*pitch + b]; returns the
+// buffer holding the result.  sign = -1: forward (e^{-i}), +1: inverse.
+__device__ float2 *fft_columns(float2 *x, float2 *y, const float2 *tw, int M, int bs, int pitch, int sign) {
     int Ns = 1;
     float2 *in = x, *out = y;
     while (Ns < M) {
         const int r = stage_radix(M / Ns);
-        const int nb = M / r;
-        const int step = M / (Ns * r);
-        for (int e = threadIdx.x; e < nb * B; e += blockDim.x) {
-            const int b = e % B, j = e / B;
-            const int k = j % Ns;
-            const int dst = (j / Ns) * Ns * r + k;
-            float2 v[5];
-            for (int q = 0; q < r; ++q) v[q] = in[(j + q * nb) * pitch + b];
-            if (k) {
-                for (int q = 1; q < r; ++q) {
-                    float2 w = tw[q * k * step];
-                    if (sign > 0) w.y = -w.y;
-                    v[q] = cmul(v[q], w);
-                }
-            }
-            if (r == 4) {
-                const float2 a0 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
-                const float2 a1 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
-                const float2 a2 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
-                const float2 d = make_float2(v[1].x - v[3].x, v[1].y - v[3].y);
-                // (v1 - v3) * (sign * i)
-                const float2 a3 = sign < 0 ? make_float2(d.y, -d.x) : make_float2(-d.y, d.x);
-                out[dst * pitch + b] = make_float2(a0.x + a2.x, a0.y + a2.y);
-                out[(dst + Ns) * pitch + b] = make_float2(a1.x + a3.x, a1.y + a3.y);
-                out[(dst + 2 * Ns) * pitch + b] = make_float2(a0.x - a2.x, a0.y - a2.y);
-                out[(dst + 3 * Ns) * pitch + b] = make_float2(a1.x - a3.x, a1.y - a3.y);
-            } else if (r == 2) {
-                out[dst * pitch + b] = make_float2(v[0].x + v[1].x, v[0].y + v[1].y);
-                out[(dst + Ns) * pitch + b] = make_float2(v[0].x - v[1].x, v[0].y - v[1].y);
-            } else if (r == 3) {
-                // y1,2 = v0 - (v1+v2)/2 +- i s (v1-v2), s = sign sqrt(3)/2
-                const float s3 = sign * 0.866025403784438647f;
-                const float2 t = make_float2(v[1].x + v[2].x, v[1].y + v[2].y);
-                const float2 d = make_float2(v[1].x - v[2].x, v[1].y - v[2].y);
-                const float2 m = make_float2(v[0].x - 0.5f * t.x, v[0].y - 0.5f * t.y);
-                out[dst * pitch + b] = make_float2(v[0].x + t.x, v[0].y + t.y);
-                out[(dst + Ns) * pitch + b] = make_float2(m.x - s3 * d.y, m.y + s3 * d.x);
-                out[(dst + 2 * Ns) * pitch + b] = make_float2(m.x + s3 * d.y, m.y - s3 * d.x);
-            } else {
-                // five-point DFT by the conjugate pairs (1,4), (2,3)
-                const float c1 = 0.309016994374947424f, c2 = -0.809016994374947424f;
-                const float s1 = sign * 0.951056516295153572f, s2 = sign * 0.587785252292473129f;
-                const float2 a1 = make_float2(v[1].x + v[4].x, v[1].y + v[4].y);
-                const float2 b1 = make_float2(v[1].x - v[4].x, v[1].y - v[4].y);
-                const float2 a2 = make_float2(v[2].x + v[3].x, v[2].y + v[3].y);
-                const float2 b2 = make_float2(v[2].x - v[3].x, v[2].y - v[3].y);
-                const float2 t1 = make_float2(v[0].x + c1 * a1.x + c2 * a2.x, v[0].y + c1 * a1.y + c2 * a2.y);
-                const float2 t2 = make_float2(v[0].x + c2 * a1.x + c1 * a2.x, v[0].y + c2 * a1.y + c1 * a2.y);
-                const float2 u1 = make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
-                const float2 u2 = make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
-                out[dst * pitch + b] = make_float2(v[0].x + a1.x + a2.x, v[0].y + a1.y + a2.y);
-                out[(dst + Ns) * pitch + b] = make_float2(t1.x - u1.y, t1.y + u1.x);      // t1 + i u1
-                out[(dst + 2 * Ns) * pitch + b] = make_float2(t2.x - u2.y, t2.y + u2.x);  // t2 + i u2
-                out[(dst + 3 * Ns) * pitch + b] = make_float2(t2.x + u2.y, t2.y - u2.x);  // t2 - i u2
-                out[(dst + 4 * Ns) * pitch + b] = make_float2(t1.x + u1.y, t1.y - u1.x);  // t1 - i u1
-            }
+        switch (r) {
+            case 4: stockham_stage<4>(in, out, tw, M, Ns, bs, pitch, sign); break;
+            case 2: stockham_stage<2>(in, out, tw, M, Ns, bs, pitch, sign); break;
+            case 3: stockham_stage<3>(in, out, tw, M, Ns, bs, pitch, sign); break;
+            default: stockham_stage<5>(in, out, tw, M, Ns, bs, pitch, sign); break;
         }
         __syncthreads();
         float2 *t = in;
@@ -124,6 +154,12 @@ __device__ float2 *fft_columns(float2 *x, float2 *y, const float2 *tw, int M, in
         Ns *= r;
     }
     return in;
+}
+
+__host__ __device__ __forceinline__ int ilog2(int v) {
+    int l = 0;
+    while ((1 << (l + 1)) <= v) ++l;
+    return l;
 }
 
 __device__ __forceinline__ void load_twiddles(float2 *tw_s, const float2 *tw, int M) {
@@ -138,6 +174,8 @@ __device__ __forceinline__ void fft_z_r2c(const unsigned long long *__restrict__
     float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
     const int Mh = M / 2 + 1;
     const size_t r0 = (size_t)blk * 2 * P;
+    const FastDiv dM((uint32_t)M), dMh((uint32_t)Mh);
+    const int ps = ilog2(P);  // P is a power of two
     load_twiddles(tw_s, tw, M);
     // kLoadBatch loads in flight per thread before their shared-memory stores
     for (int e0 = threadIdx.x; e0 < 2 * P * M; e0 += kLoadBatch * blockDim.x) {
@@ -152,16 +190,16 @@ __device__ __forceinline__ void fft_z_r2c(const unsigned long long *__restrict__
         for (int u = 0; u < kLoadBatch; ++u) {
             int e = e0 + u * blockDim.x;
             if (e < 2 * P * M) {
-                int row = e / M, m = e % M;
+                const int row = (int)dM.div((uint32_t)e), m = e - row * M;
                 float *slot = reinterpret_cast<float *>(&x[m * pitch + (row >> 1)]);
                 slot[row & 1] = v[u];
             }
         }
     }
     __syncthreads();
-    float2 *res = fft_columns(x, y, tw_s, M, P, pitch, -1);
+    float2 *res = fft_columns(x, y, tw_s, M, ps, pitch, -1);
     for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) {
-        int row = e / Mh, k = e % Mh, pr = row >> 1;
+        const int row = (int)dMh.div((uint32_t)e), k = e - row * Mh, pr = row >> 1;
         float2 z = res[k * pitch + pr];
         float2 zc = res[((M - k) % M) * pitch + pr];
         zc.y = -zc.y;
@@ -181,6 +219,8 @@ __device__ __forceinline__ void fft_z_c2r(const float2 *__restrict__ spec, float
     float2 *x = sm, *y = sm + M * pitch, *tw_s = sm + 2 * M * pitch;
     const int Mh = M / 2 + 1;
     const size_t r0 = (size_t)blk * 2 * P;
+    const FastDiv dM((uint32_t)M), dMh((uint32_t)Mh);
+    const int ps = ilog2(P);  // P is a power of two
     load_twiddles(tw_s, tw, M);
     // rows into y as h[row*Mh + k]
     for (int e0 = threadIdx.x; e0 < 2 * P * Mh; e0 += kLoadBatch * blockDim.x) {
@@ -194,7 +234,7 @@ __device__ __forceinline__ void fft_z_c2r(const float2 *__restrict__ spec, float
         for (int u = 0; u < kLoadBatch; ++u) {
             int e = e0 + u * blockDim.x;
             if (e < 2 * P * Mh) {
-                int k = e % Mh;
+                const int k = e - (int)dMh.div((uint32_t)e) * Mh;
                 if (k == 0 || k == M / 2) v[u].y = 0.f;
                 y[e] = v[u];
             }
@@ -202,7 +242,7 @@ __device__ __forceinline__ void fft_z_c2r(const float2 *__restrict__ spec, float
     }
     __syncthreads();
     for (int e = threadIdx.x; e < P * M; e += blockDim.x) {
-        int pr = e % P, k = e / P;
+        const int pr = e & (P - 1), k = e >> ps;
         float2 a, b;
         if (k <= M / 2) {
             a = y[(2 * pr) * Mh + k];
@@ -216,9 +256,9 @@ __device__ __forceinline__ void fft_z_c2r(const float2 *__restrict__ spec, float
         x[k * pitch + pr] = make_float2(a.x - b.y, a.y + b.x);  // a + i b
     }
     __syncthreads();
-    float2 *res = fft_columns(x, y, tw_s, M, P, pitch, +1);
+    float2 *res = fft_columns(x, y, tw_s, M, ps, pitch, +1);
     for (int e = threadIdx.x; e < 2 * P * M; e += blockDim.x) {
-        int row = e / M, m = e % M;
+        const int row = (int)dM.div((uint32_t)e), m = e - row * M;
         float2 z = res[m * pitch + (row >> 1)];
         out[(r0 + row) * M + m] = (row & 1) ? z.y : z.x;
     }
@@ -236,6 +276,7 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
     const int Mh = M / 2 + 1;
     const int o = by;
     const int kz0 = bx * B;
+    const int bsh = ilog2(B);  // B is a power of two
     const int nb = min(B, Mh - kz0);
     const size_t sm_stride = axis == 1 ? (size_t)Mh : (size_t)M * Mh;
     const size_t base = axis == 1 ? (size_t)o * M * Mh : (size_t)o * Mh;
@@ -245,7 +286,7 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             int e = e0 + u * blockDim.x;
-            int m = e / B, b = e % B;
+            const int m = e >> bsh, b = e & (B - 1);
             v[u] = (e < M * B && b < nb) ? spec[base + m * sm_stride + kz0 + b] : make_float2(0.f, 0.f);
         }
 #pragma unroll
@@ -255,13 +296,13 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
         }
     }
     __syncthreads();
-    float2 *res = fft_columns(x, y, tw_s, M, B, pitch, sign);
+    float2 *res = fft_columns(x, y, tw_s, M, bsh, pitch, sign);
     if (green) {
         // res holds the full forward transform: k index m along x, y index o, kz0+b
         const int ky = o <= M / 2 ? o : M - o;
         const float gy = green1d[ky];
         for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
-            int m = e / B, b = e % B;
+            const int m = e >> bsh, b = e & (B - 1);
             int kx = m <= M / 2 ? m : M - m;
             int kz = kz0 + b;
             float2 v = res[m * pitch + b];
@@ -274,10 +315,10 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
         }
         __syncthreads();
         float2 *other = res == x ? y : x;
-        res = fft_columns(res, other, tw_s, M, B, pitch, +1);
+        res = fft_columns(res, other, tw_s, M, bsh, pitch, +1);
     }
     for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
-        int m = e / B, b = e % B;
+        const int m = e >> bsh, b = e & (B - 1);
         if (b < nb) spec[base + m * sm_stride + kz0 + b] = res[m * pitch + b];
     }
 }
@@ -455,11 +496,14 @@ __global__ void k_interp_multi(const float4 *__restrict__ pos, uint32_t n, const
     acc[i] = interp_one<FIXED>(pos[i], d.rho, d.M, d.to_slab_fac, d.fd_fac);
 }
 
+// Batch sizes are powers of two: the transforms split a flat index into
+// (row, column) with a shift and a mask.
 int fft_batch_z(int M) {
     int P = 4096 / M;
     if (P > 16) P = 16;
     if (P > M / 2) P = M / 2;  // k_fft_z_c2r stages 2P rows of M/2+1 in an M*(P+1) buffer
     if (P < 1) P = 1;
+    P = 1 << ilog2(P);
     // P pairs per CTA must divide the M*M/2 row pairs
     while (P > 1 && ((M * M / 2) % P)) P >>= 1;
     return P;
@@ -469,7 +513,7 @@ int fft_batch_axis(int M) {
     int B = 4096 / M;
     if (B > 16) B = 16;
     if (B < 1) B = 1;
-    return B;
+    return 1 << ilog2(B);
 }
 
 }  // namespace
