@@ -58,6 +58,12 @@ constexpr int kMaxSeg = 8;
 // kTMax slice of a denser segment.
 constexpr int kTMax = 128;
 constexpr unsigned kFull = 0xffffffffu;
+// CTAs per SM the register allocation is sized for (65536 / (256 * 4) = 64
+// registers a thread at 4)
+#ifndef CUCO_SR_MIN_BLOCKS
+#define CUCO_SR_MIN_BLOCKS 4
+#endif
+constexpr int kMinBlocks = CUCO_SR_MIN_BLOCKS;
 
 struct ColumnSet {
     int ncols;
@@ -122,6 +128,14 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
+// 1 << k for k < 32, else 0: PTX clamps a shift count above the width, so
+// this is one shift with no compare and select.
+__device__ __forceinline__ uint32_t bit_at(uint32_t k) {
+    uint32_t b;
+    asm("shl.b32 %0, %1, %2;" : "=r"(b) : "r"(1u), "r"(k));
+    return b;
+}
+
 // r^2 with a fixed operation order: the candidate test and the force pass
 // must agree on it bit for bit.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
@@ -141,7 +155,8 @@ __device__ __forceinline__ void shortrange_segment(
     extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
     __shared__ uint32_t s_wdelta[kWarps][32];
-    __shared__ float s_acc[6][kTMax];  // multi-chunk units: per-target sums (and FIXED error terms)
+    __shared__ float s_acc[6][kTMax];  // per-target sums (multi-chunk units: and FIXED error terms)
+    __shared__ float4 s_tpos[kTMax];   // the unit's target positions
 
     const int G = p.grid;
     const int S = cs.S, R = cs.R, nz = S + 2 * R, ncols = cs.ncols;
@@ -299,30 +314,34 @@ __device__ __forceinline__ void shortrange_segment(
     // the cut, away from a table-bin edge and from the cut, outside the
     // softening length - without a branch, and reports the rest (its
     // contribution there is zero): a candidate whose bin or cut decision is
-    // made in double, the spline inside h, and the self pair (r = 0 < hmin).
-    // pair_slow applies the full law to those.  Both add into the same
+    // made in double and the spline inside h (the self pair, r = 0, adds
+    // nothing and is skipped).  pair_slow applies the full law to those.  Both add into the same
     // accumulators in the same order as a single law would.
-    const float hmin = fmaxf(hh, 1e-9f);  // r2 < 1e-20 always takes the full law
+    const float hmin = fmaxf(hh, 1e-9f);
+    const float hmin2 = hmin * hmin;  // r2 below it (the spline, r2 = 0) takes the full law
+    // bin = floor(asmthfac * r): a round-toward-zero fma onto 2^23 leaves the
+    // floor in the mantissa, with no conversion instruction.  Plain: the bins
+    // of r * asmthfac * (1 -/+ kEdge) differ when r lies within kEdge
+    // (relative) of a bin edge, and such a pair is decided in double.
+    const float alo = FIXED ? asmf : asmf * (1.f - kEdge), ahi = FIXED ? asmf : asmf * (1.f + kEdge);
     auto pair_fast = [&](float4 s, float &ax, float &ay, float &az) -> bool {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
-        const float rinv = rsqrtf(fmaxf(r2, 1e-20f));
+        // r2 = 0 gives rinv = inf and r = NaN: not fast (r2 < hmin2), not flagged
+        const float rinv = rsqrtf(r2);
         const float r = r2 * rinv;
-        // bin = floor(asmthfac * r) without a conversion instruction: a
-        // round-toward-zero add of 2^23 leaves floor(x) in the mantissa (and a
-        // larger non-negative value for x >= 2^23, clamped below)
-        const float xt = asmf * r;
-        const float xf = __fadd_rz(xt, 8388608.0f);
-        const uint32_t ti = (uint32_t)(__float_as_int(xf) - 0x4B000000);
-        const float frac = xt - (xf - 8388608.0f);
-        const bool edge = !FIXED && fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f);
-        const bool fast = r2 <= rc2_lo && !edge && r >= hmin;
+        const float xl = __fmaf_rz(r, alo, 8388608.0f);
+        const bool edge = !FIXED && xl != __fmaf_rz(r, ahi, 8388608.0f);
+        const uint32_t ti = (uint32_t)(__float_as_int(xl) - 0x4B000000);
+        const bool fast = r2 <= rc2_lo && r2 >= hmin2 && !edge;
         const float fac = fast ? rinv * rinv * rinv * tab[min(ti, (uint32_t)kNTab - 1u)] : 0.f;
         ax = __fmaf_rn(dx, fac, ax);
         ay = __fmaf_rn(dy, fac, ay);
         az = __fmaf_rn(dz, fac, az);
         if (COUNT) npairs += fast;
-        return r2 <= rc2_hi && !fast;
+        // r2 == 0 (the self pair, or a coincident source) adds dx*fac = 0:
+        // not flagged, so the rare-case branch is not taken once per target
+        return r2 <= rc2_hi && r2 != 0.f && !fast;
     };
     auto pair_slow = [&](float4 s, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
@@ -330,12 +349,10 @@ __device__ __forceinline__ void shortrange_segment(
         bool ok = r2 <= rc2_hi && r2 != 0.f;
         const float rinv = rsqrtf(ok ? r2 : 1.f);
         const float r = r2 * rinv;
-        const float xt = asmf * r;
-        const float xf = __fadd_rz(xt, 8388608.0f);
-        int ti = __float_as_int(xf) - 0x4B000000;
-        const float frac = xt - (xf - 8388608.0f);
+        const float xl = __fmaf_rz(r, alo, 8388608.0f);
+        int ti = __float_as_int(xl) - 0x4B000000;
         float fac = rinv * rinv * rinv;
-        if (!FIXED && (fabsf(frac - 0.5f) > __fmaf_rn(-kEdge, xt, 0.5f) || r2 > rc2_lo)) {
+        if (!FIXED && (xl != __fmaf_rz(r, ahi, 8388608.0f) || r2 > rc2_lo)) {
             // decided in double as the reference's CPU path computes it
             const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
             ok = ok && dd <= rcut2_d;
@@ -419,8 +436,8 @@ __device__ __forceinline__ void shortrange_segment(
             uint32_t before = 0, base = 0;
             for (; base + 32u < T; base += 64) {
                 const uint32_t r0 = ps - base, r1 = r0 - 32u;
-                const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
-                const uint32_t m1 = __reduce_or_sync(kFull, r1 < 32u ? 1u << r1 : 0u);
+                const uint32_t m0 = __reduce_or_sync(kFull, bit_at(r0));
+                const uint32_t m1 = __reduce_or_sync(kFull, bit_at(r1));
                 const uint32_t n0 = before + __popc(m0);
                 const uint32_t k0 = base + lane, k1 = k0 + 32;
                 const uint32_t i0 = k0 + wdelta[before + __popc(m0 & le_mask) - 1];
@@ -437,7 +454,7 @@ __device__ __forceinline__ void shortrange_segment(
             }
             if (base < T) {
                 const uint32_t r0 = ps - base;
-                const uint32_t m0 = __reduce_or_sync(kFull, r0 < 32u ? 1u << r0 : 0u);
+                const uint32_t m0 = __reduce_or_sync(kFull, bit_at(r0));
                 const uint32_t k0 = base + lane;
                 const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
                 const float4 s0 = src[k0 < T ? k0 + d0 : (uint32_t)kMaxStage];
@@ -483,8 +500,7 @@ __device__ __forceinline__ void shortrange_segment(
     // the target's coordinates: pt absolute float (for the culling; fixed
     // point rounded to float, which the culling margin covers), tx..tz
     // origin-relative (for the pair law)
-    auto load_target = [&](uint32_t t) {
-        const float4 praw = spos[t_begin + t];
+    auto load_target = [&](float4 praw) {
         float4 pt = praw;
         if (FIXED) {
             pt = make_float4(__fmul_rn((float)__float_as_uint(praw.x), fs),
@@ -552,13 +568,16 @@ __device__ __forceinline__ void shortrange_segment(
         }
     };
 
+    // the unit's targets, read by every round (and chunk) from shared memory
+    for (uint32_t t = tid; t < nt; t += kThreads) s_tpos[t] = spos[t_begin + t];
+
     if (single_chunk) {
         stage(0, total);
         __syncthreads();
         for (uint32_t round = 0; round < rounds; ++round) {
             const uint32_t t = round * kWarps + warp;
-            if (t >= nt) break;  // warp-uniform; no barrier follows
-            const float4 pt = load_target(t);
+            if (t >= nt) break;  // warp-uniform
+            const float4 pt = load_target(s_tpos[t]);
             float ax, ay, az, ex, ey, ez;
             target_chunk(pt, 0, total, ax, ay, az, ex, ey, ez);
             if (FIXED) {
@@ -566,8 +585,16 @@ __device__ __forceinline__ void shortrange_segment(
                 ay = __fadd_rn(ay, ey);
                 az = __fadd_rn(az, ez);
             }
-            if (lane == 0) epilogue(t, make_float4(ax * mg, ay * mg, az * mg, 0.f));
+            if (lane == 0) {
+                s_acc[0][t] = ax * mg;
+                s_acc[1][t] = ay * mg;
+                s_acc[2][t] = az * mg;
+            }
         }
+        // the epilogues of all the unit's targets side by side
+        __syncthreads();
+        for (uint32_t t = tid; t < nt; t += kThreads)
+            epilogue(t, make_float4(s_acc[0][t], s_acc[1][t], s_acc[2][t], 0.f));
     } else {
         for (uint32_t t = tid; t < nt; t += kThreads)
             for (int k = 0; k < 6; ++k) s_acc[k][t] = 0.f;
@@ -579,7 +606,7 @@ __device__ __forceinline__ void shortrange_segment(
             for (uint32_t round = 0; round < rounds; ++round) {
                 const uint32_t t = round * kWarps + warp;
                 if (t >= nt) break;
-                const float4 pt = load_target(t);
+                const float4 pt = load_target(s_tpos[t]);
                 float ax, ay, az, ex, ey, ez;
                 target_chunk(pt, c0, c1, ax, ay, az, ex, ey, ez);
                 if (lane == 0) {
@@ -684,7 +711,7 @@ __device__ __forceinline__ bool next_unit(const SRWork &w, uint32_t nseg, uint32
 // Persistent: as many CTAs as fit on the GPU, each taking units until none
 // is left, so a few dense segments no longer leave most SMs idle.
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     k_shortrange(const __grid_constant__ ShortRangeParams p, const __grid_constant__ ColumnSet cs, uint32_t nseg,
                  const __grid_constant__ SRWork w, const float4 *__restrict__ spos,
                  const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca,
@@ -714,7 +741,7 @@ __global__ void k_sr_plan_multi(const SRBoxDesc *__restrict__ boxes, const uint3
 }
 
 template <bool KICK, bool COUNT, bool FIXED>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
     k_shortrange_multi(const SRBoxDesc *__restrict__ boxes, const double2 *__restrict__ kicks,
                        const uint32_t *__restrict__ seg_base, int nbox, uint32_t nseg,
                        const __grid_constant__ SRWork w, const float4 *__restrict__ spos,
