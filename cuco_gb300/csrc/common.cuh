@@ -61,11 +61,33 @@ cuco_status_t launch_reorder_start_end(uint32_t *cell_start, uint32_t *cell_end,
                                        uint32_t ncells, cudaStream_t stream);
 
 // Engine cell-bound format: cell_off[c] = first sorted index with key >= c,
-// for c in [0, ncells], plus the gather.
+// for c in [0, ncells], plus the gather (none when sorted_pos is null).
 cuco_status_t launch_reorder_offsets(uint32_t *cell_off, float4 *sorted_pos,
                                      const uint32_t *sorted_keys, const uint32_t *perm,
                                      const float4 *pos, uint32_t n, uint32_t ncells,
                                      cudaStream_t stream);
+
+// A box's cell grid within a concatenated cell numbering (cells
+// cell_base .. cell_base + G^3 - 1).
+struct CellBox {
+    uint32_t G, cell_base;
+    float boxsize, gridfac;  // gridfac = (float)G / L, the key rule's factor
+};
+
+// Each cell's particles ordered by z slice: kZSub slices of the cell along z,
+// stable within a slice.  From the cell-sorted permutation `perm` (cell_off:
+// the cells' first sorted indices) it gathers sorted_pos in that order, with
+// w = the slice as a float, and perm_s = its map to original indices.
+// slices[c] holds eight u16: entry j = the cell's particles in slices 0..j
+// (all 0xffff for a cell of 65535 or more).  Boxes: one (boxes null, `one`)
+// or nbox descriptors sorted by cell_base.  fixed: positions are 32-bit fixed
+// point.
+constexpr int kZSubBits = 3;
+constexpr int kZSub = 1 << kZSubBits;
+cuco_status_t launch_cell_subsort(const uint32_t *cell_off, const uint32_t *perm, const float4 *pos,
+                                  float4 *sorted_pos, uint32_t *perm_s, uint4 *slices, uint32_t ncells,
+                                  const CellBox &one, const CellBox *boxes, int nbox, bool fixed,
+                                  cudaStream_t stream);
 
 // ----------------------------------------------------------- short range
 
@@ -84,6 +106,10 @@ struct ShortRangeParams {
     bool fixed;      // positions are 32-bit fixed point (bit patterns in the float4s)
     float fscale;    // L / 2^32
     uint32_t cell_base;  // first cell of this box in a multi-box cell array (0 otherwise)
+    // the z-slice counts of the cells (launch_cell_subsort), indexed by cell
+    // id; null when the sources are not in slice order or the per-segment
+    // table would not fit in shared memory
+    const uint4 *slices;
 };
 
 // Which cell-bound format the kernel reads.

@@ -293,7 +293,9 @@ struct cuco_box {
     float4 *spos = nullptr, *acc_pm_s = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr;
     uint32_t *hist = nullptr, *cell_off = nullptr;
+    uint4 *cell_sl = nullptr;  // per cell: z-slice counts
     uint32_t *sorted_keys = nullptr, *sorted_perm = nullptr;  // where the last sort ended
+    uint32_t *perm_s = nullptr;  // the z-slice order's map to original indices (the sort's spare buffer)
     float *table = nullptr;
     float *stage3 = nullptr;  // n x 3 staging for host/device float3 transfers
     PMPlan pm{};
@@ -337,6 +339,7 @@ ShortRangeParams make_sr_params(const cuco_box *b) {
     p.n = b->n;
     p.fixed = b->cfg.mode == CUCO_MODE_FIXED;
     p.fscale = ldexpf(b->cfg.boxsize, -32);
+    p.slices = b->cell_sl;
     return p;
 }
 
@@ -360,9 +363,17 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
     b->sorted_keys = in_alt ? b->keys_alt : b->keys;
     b->sorted_perm = in_alt ? b->perm_alt : b->perm;
     record(b, 2);
-    CUCO_TRY(launch_reorder_offsets(b->cell_off, b->spos, b->sorted_keys, b->sorted_perm, b->pos,
+    CUCO_TRY(launch_reorder_offsets(b->cell_off, nullptr, b->sorted_keys, b->sorted_perm, b->pos,
                                     b->n, b->ncells, b->stream));
-    b->launches += 1;
+    // the cell order refined by z slice (the short range trims its column
+    // ranges to the slices a target reaches); its map to original indices
+    // goes to the sort's spare buffer
+    uint32_t *perm_s = in_alt ? b->perm : b->perm_alt;
+    b->perm_s = perm_s;
+    const CellBox cb{(uint32_t)b->G, 0u, b->cfg.boxsize, b->gridfac};
+    CUCO_TRY(launch_cell_subsort(b->cell_off, b->sorted_perm, b->pos, b->spos, perm_s, b->cell_sl, b->ncells, cb,
+                                 nullptr, 1, b->cfg.mode == CUCO_MODE_FIXED, b->stream));
+    b->launches += 2;
     record(b, 3);
     if (pm) {
         CUCO_TRY(pm_forces(b->pm, b->spos, b->n, b->acc_pm_s, b->stream,
@@ -378,12 +389,12 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
         if (kick) k = *kick;
         k.acc_pm_s = pm ? b->acc_pm_s : nullptr;
         k.acc_pm_out = pm ? b->acc_pm : nullptr;
-        CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, b->sorted_perm, b->cell_off,
+        CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, perm_s, b->cell_off,
                                    nullptr, kCellOffsets, b->table, b->acc_pp, k, b->work, b->stream,
                                    b->timing ? b->pair_counter : nullptr));
         b->launches += 2;  // work plan + persistent short range
     } else if (pm) {
-        CUCO_TRY(scatter4(b->acc_pm_s, b->sorted_perm, b->acc_pm, b->n, b->stream));
+        CUCO_TRY(scatter4(b->acc_pm_s, perm_s, b->acc_pm, b->n, b->stream));
         b->launches += 1;
     }
     record(b, 7);
@@ -463,7 +474,8 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         (s = alloc(&b->keys, n)) || (s = alloc(&b->perm, n)) || (s = alloc(&b->keys_alt, n)) ||
         (s = alloc(&b->perm_alt, n)) ||
         (s = alloc(&b->hist, sort_hist_entries(b->n, b->key_bits, 8))) ||
-        (s = alloc(&b->cell_off, (size_t)b->ncells + 1)) || (s = alloc(&b->table, kNTab)) ||
+        (s = alloc(&b->cell_off, (size_t)b->ncells + 1)) || (s = alloc(&b->cell_sl, (size_t)b->ncells)) ||
+        (s = alloc(&b->table, kNTab)) ||
         (s = alloc(&b->stage3, 3 * n)) || (s = alloc(&b->pair_counter, 1)) ||
         (s = alloc(&b->work.heavy, shortrange_heavy_cap(b->n))) || (s = alloc(&b->work.seg_nt, b->ncells)) ||
         (s = alloc(&b->work.ctl, 2)))
@@ -505,6 +517,7 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     cudaFree(b->perm_alt);
     cudaFree(b->hist);
     cudaFree(b->cell_off);
+    cudaFree(b->cell_sl);
     cudaFree(b->table);
     cudaFree(b->stage3);
     cudaFree(b->pair_counter);
@@ -689,6 +702,19 @@ cuco_status_t cuco_box_debug(cuco_box_t *b, uint32_t *sorted_keys, uint32_t *per
             if (cell_end) cell_end[c] = empty ? kEmptyCell : off[c + 1];
         }
     }
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_cell_order(cuco_box_t *b, uint32_t *perm_s, float *slice) {
+    if (!b || !b->perm_s) {
+        set_error("cuco_box_cell_order: no forces computed yet");
+        return CUCO_ERR_STATE;
+    }
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    if (perm_s) CUCO_TRY_CUDA(cudaMemcpy(perm_s, b->perm_s, 4 * (size_t)b->n, cudaMemcpyDeviceToHost));
+    if (slice && b->n)
+        CUCO_TRY_CUDA(cudaMemcpy2D(slice, sizeof(float), &b->spos[0].w, sizeof(float4), sizeof(float), b->n,
+                                   cudaMemcpyDeviceToHost));
     return CUCO_OK;
 }
 

@@ -31,10 +31,7 @@ namespace cuco {
 
 namespace {
 
-struct DriftBox {
-    uint32_t G, cell_base;
-    float boxsize, gridfac;
-};
+using DriftBox = CellBox;  // a box's cell grid: drift, keys and the z-slice order
 
 struct StepFactors {
     float units_per_time;  // fixed point: drift * 2^32 / L; plain: the drift factor
@@ -136,7 +133,7 @@ cuco_status_t palloc(T **p, size_t count, cudaStream_t s) {
     return CUCO_OK;
 }
 
-ShortRangeParams sr_params(const cuco_config_t &c, uint32_t n, uint32_t cell_base) {
+ShortRangeParams sr_params(const cuco_config_t &c, uint32_t n, uint32_t cell_base, const uint4 *slices) {
     ShortRangeParams p{};
     p.boxsize = c.boxsize;
     p.gridfac = (float)c.cell_grid / c.boxsize;
@@ -155,6 +152,7 @@ ShortRangeParams sr_params(const cuco_config_t &c, uint32_t n, uint32_t cell_bas
     p.fixed = c.mode == CUCO_MODE_FIXED;
     p.fscale = ldexpf(c.boxsize, -32);
     p.cell_base = cell_base;
+    p.slices = slices;
     return p;
 }
 
@@ -288,6 +286,7 @@ struct cuco_ensemble {
            *acc_pm_s = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr, *hist = nullptr,
              *cell_off = nullptr, *sorted_perm = nullptr;
+    uint4 *cell_sl = nullptr;  // per cell: z-slice counts
     float *stage3 = nullptr;
     // meshes, concatenated
     float *rho = nullptr, *green = nullptr, *table = nullptr;
@@ -316,7 +315,7 @@ struct cuco_ensemble {
     size_t cap_n = 0, cap_hist = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
            cap_green = 0, cap_tw = 0, cap_table = 0, cap_pbeg = 0, cap_segbase = 0, cap_drift = 0, cap_pm = 0,
            cap_kicks = 0, cap_factors = 0, cap_counter = 0, cap_sr = 0, cap_hfactors = 0, cap_hkicks = 0,
-           cap_mapz = 0, cap_mapa = 0, cap_heavy = 0, cap_segnt = 0, cap_ctl = 0;
+           cap_mapz = 0, cap_mapa = 0, cap_heavy = 0, cap_segnt = 0, cap_ctl = 0, cap_cellsl = 0;
     // the short range's work-plan scratch
     uint2 *sr_heavy = nullptr;
     uint32_t *sr_segnt = nullptr, *sr_ctl = nullptr;
@@ -339,9 +338,14 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
                         e->stream, &in_alt, &e->launches));
     const uint32_t *skeys = in_alt ? e->keys_alt : e->keys;
     e->sorted_perm = in_alt ? e->perm_alt : e->perm;
-    CUCO_TRY(launch_reorder_offsets(e->cell_off, e->spos, skeys, e->sorted_perm, e->pos, e->n, (uint32_t)e->ncells,
+    CUCO_TRY(launch_reorder_offsets(e->cell_off, nullptr, skeys, e->sorted_perm, e->pos, e->n, (uint32_t)e->ncells,
                                     e->stream));
-    e->launches++;
+    // cells refined by z slice, as for one box; the map to original indices
+    // goes to the sort's spare buffer
+    uint32_t *perm_s = in_alt ? e->perm : e->perm_alt;
+    CUCO_TRY(launch_cell_subsort(e->cell_off, e->sorted_perm, e->pos, e->spos, perm_s, e->cell_sl,
+                                 (uint32_t)e->ncells, CellBox{}, e->d_drift, e->nbox, e->fixed, e->stream));
+    e->launches += 2;
     CUCO_TRY(pm_forces_multi(e->pm, e->spos, e->n, e->acc_pm_s, e->stream, &e->launches));
     KickArgs k{};
     k.vel = kick ? e->vel : nullptr;
@@ -349,7 +353,7 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
     k.acc_pm_out = e->acc_pm;
     SRWork w{e->sr_heavy, (uint32_t)e->cap_heavy, e->sr_segnt, (uint32_t)e->cap_segnt, e->sr_ctl};
     CUCO_TRY(launch_shortrange_multi(e->d_sr, e->d_kicks, e->d_segbase, e->nbox, e->segments, e->sr_smem, e->fixed,
-                                     e->spos, e->sorted_perm, e->cell_off, e->table, e->acc_pp, k, w, e->stream,
+                                     e->spos, perm_s, e->cell_off, e->table, e->acc_pp, k, w, e->stream,
                                      e->count_pairs ? e->pair_counter : nullptr));
     e->launches += 2;  // work plan + persistent short range
     return CUCO_OK;
@@ -540,7 +544,7 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
     }
     const size_t nbc = (size_t)nbox + 1;
     if ((s = grow(e->hist, e->cap_hist, sort_hist_entries((uint32_t)n, kbits, 8), st)) ||
-        (s = grow(e->cell_off, e->cap_cells, ncells + 1, st)) || (s = grow(e->stage3, e->cap_stage3, 3 * maxn, st)) ||
+        (s = grow(e->cell_off, e->cap_cells, ncells + 1, st)) || (s = grow(e->cell_sl, e->cap_cellsl, ncells, st)) || (s = grow(e->stage3, e->cap_stage3, 3 * maxn, st)) ||
         (s = grow(e->rho, e->cap_mesh, mbase[nbox], st)) ||
         (s = grow(e->rho64, e->cap_mesh64, mbase[nbox], st)) || (s = grow(e->spec, e->cap_spec, sbase[nbox], st)) ||
         (s = grow(e->green, e->cap_green, gbase[nbox], st)) || (s = grow(e->tw, e->cap_tw, tbase[nbox], st)) ||
@@ -578,7 +582,7 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
         sma = std::max(sma, pm_smem_axis(M, B[b]));
         uint32_t nseg = 0;
         size_t sm = 0;
-        if ((s = shortrange_desc_fill(sr_params(c, (uint32_t)c.n, (uint32_t)cbase[b]),
+        if ((s = shortrange_desc_fill(sr_params(c, (uint32_t)c.n, (uint32_t)cbase[b], e->cell_sl),
                                       srd.data() + b * shortrange_desc_bytes(), &nseg, &sm)))
             return s;
         segbase[b + 1] = segbase[b] + nseg;
@@ -678,7 +682,7 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
     drop_graph(e);
     for (void *p : {(void *)e->pos, (void *)e->vel, (void *)e->acc_pp, (void *)e->acc_pm, (void *)e->spos,
                     (void *)e->acc_pm_s, (void *)e->keys, (void *)e->perm, (void *)e->keys_alt, (void *)e->perm_alt,
-                    (void *)e->hist, (void *)e->cell_off, (void *)e->stage3, (void *)e->rho, (void *)e->rho64,
+                    (void *)e->hist, (void *)e->cell_off, (void *)e->cell_sl, (void *)e->stage3, (void *)e->rho, (void *)e->rho64,
                     (void *)e->spec,
                     (void *)e->green, (void *)e->tw, (void *)e->table, (void *)e->d_pbeg, (void *)e->d_segbase,
                     (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, (void *)e->d_sr,
@@ -854,7 +858,7 @@ cuco_status_t cuco_ensemble_footprint(const cuco_config_t *boxes, int nbox, uint
         const uint64_t n = (uint64_t)boxes[k].n, M = (uint64_t)boxes[k].pm_grid;
         const uint64_t G = boxes[k].cell_grid > 0 ? (uint64_t)boxes[k].cell_grid : M / 2;  // the largest tuned grid
         b += n * (6 * sizeof(float4) + 4 * sizeof(uint32_t));    // state, sorted copies, keys
-        b += 4 * (G * G * G + 1);                                // cell offsets
+        b += 4 * (G * G * G + 1) + 16 * G * G * G;               // cell offsets, z-slice counts
         b += 12 * M * M * M + 8 * M * M * (M / 2 + 1);           // deposit + real grid + half spectrum
         b += 12 * (M / 2 + 1) + 8 * M + 2048 + 16 * (M * M);    // tables, descriptors, CTA maps
         maxn = std::max(maxn, n);

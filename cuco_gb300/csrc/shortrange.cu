@@ -69,6 +69,7 @@ struct ColumnSet {
     int ncols;
     int R;
     int S;
+    int c00;       // the column (0, 0)
     float margin;  // culling slack for the float cell assignment (length units)
     signed char dx[kMaxCols];
     signed char dy[kMaxCols];
@@ -90,11 +91,18 @@ struct Run {
 // Dynamic shared memory, in order: staged sources and one sentinel source,
 // split table, column xy bounds, per-(column, z-cell) staged offsets, cell
 // starts and counts, column runs, column totals.
-__host__ __device__ inline size_t smem_bytes(int ncols, int nz) {
-    return sizeof(float4) * (kMaxStage + 1) + sizeof(float) * kNTab + sizeof(float4) * (size_t)ncols +
-           sizeof(uint32_t) * (size_t)ncols * (nz + 1) + 2 * sizeof(uint32_t) * (size_t)ncols * nz +
-           sizeof(Run) * 2 * (size_t)ncols + sizeof(uint32_t) * (size_t)ncols;
+__host__ __device__ inline size_t smem_base_bytes(int ncols, int nz) {
+    const size_t b = sizeof(float4) * (kMaxStage + 1) + sizeof(float) * kNTab + sizeof(float4) * (size_t)ncols +
+                     sizeof(uint32_t) * (size_t)ncols * (nz + 1) + 2 * sizeof(uint32_t) * (size_t)ncols * nz +
+                     sizeof(Run) * 2 * (size_t)ncols + sizeof(uint32_t) * (size_t)ncols;
+    return (b + 15) & ~(size_t)15;
 }
+// ... then, with z slices, every (column, z-cell)'s slice counts
+__host__ __device__ inline size_t smem_bytes(int ncols, int nz, bool zs) {
+    return smem_base_bytes(ncols, nz) + (zs ? sizeof(uint4) * (size_t)ncols * nz : 0);
+}
+// The slice table is used where it adds at most this much shared memory.
+constexpr size_t kMaxSliceTable = 16384;
 
 // A staged source this far away is beyond any cut: list positions past the
 // end of a target's candidates read it instead of branching.
@@ -155,6 +163,7 @@ __device__ __forceinline__ void shortrange_segment(
     extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
     __shared__ uint32_t s_wdelta[kWarps][32];
+    __shared__ uint32_t s_wsum[kWarps];
     __shared__ float s_acc[6][kTMax];  // per-target sums (multi-chunk units: and FIXED error terms)
     __shared__ float4 s_tpos[kTMax];   // the unit's target positions
 
@@ -169,6 +178,9 @@ __device__ __forceinline__ void shortrange_segment(
     uint32_t *ccn = cst + ncols * nz;
     Run *runs = reinterpret_cast<Run *>(ccn + ncols * nz);
     uint32_t *coltot = reinterpret_cast<uint32_t *>(runs + 2 * ncols);
+    // (column, z-cell) -> eight u16 slice counts of that cell
+    uint4 *s_sl = reinterpret_cast<uint4 *>(reinterpret_cast<char *>(smem_f4) + smem_base_bytes(ncols, nz));
+    const uint16_t *sl16 = reinterpret_cast<const uint16_t *>(s_sl);
 
     const int segs = G / S;
     const int ix = seg / (G * segs);
@@ -176,102 +188,176 @@ __device__ __forceinline__ void shortrange_segment(
     const int iz0 = (seg % segs) * S;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const float L = p.boxsize;
+    const bool ZS = p.slices != nullptr;  // sources in z-slice order within cells, with slice counts
 
-    // every (column, z-cell) range, loaded in parallel
+    // every (column, z-cell) range, loaded in parallel; e = col * nz + zc
+    // (the float quotient is exact here: (e + 1/2) / nz is at least 1/(2 nz)
+    // from an integer)
+    const float inv_nz = 1.0f / (float)nz;
+    auto col_of = [&](int e) { return (int)(((float)e + 0.5f) * inv_nz); };
     for (int e = tid; e < ncols * nz; e += kThreads) {
-        const int col = e / nz, zc = e % nz;
+        const int col = col_of(e), zc = e - col * nz;
         int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col], czu = iz0 - R + zc;
         int cx = cxu < 0 ? cxu + G : (cxu >= G ? cxu - G : cxu);
         int cy = cyu < 0 ? cyu + G : (cyu >= G ? cyu - G : cyu);
         int cz = czu < 0 ? czu + G : (czu >= G ? czu - G : czu);
         uint32_t st, cn;
-        cell_range<FMT>(ca, cb, p.cell_base + ((uint32_t)cx * G + cy) * G + cz, &st, &cn);
+        const uint32_t cell = p.cell_base + ((uint32_t)cx * G + cy) * G + cz;
+        cell_range<FMT>(ca, cb, cell, &st, &cn);
         cst[e] = st;
         ccn[e] = cn;
+        if (ZS) s_sl[e] = p.slices[cell];
     }
     __syncthreads();
-    if (tid == 0) {
-        // the segment's cells are column (0, 0), z-cells R .. R+S-1
-        int c00 = -1;
-        for (int col = 0; col < ncols; ++col)
-            if (cs.dx[col] == 0 && cs.dy[col] == 0) c00 = col;
-        uint32_t tb = 0, te = 0;
-        bool found = false;
-        for (int k = 0; k < S; ++k) {
-            const uint32_t st = cst[c00 * nz + R + k], cn = ccn[c00 * nz + R + k];
-            if (cn) {
-                if (!found) tb = st;
-                found = true;
-                te = st + cn;
+    uint32_t t_begin, t_end, total;
+    if (FMT == kCellOffsets) {
+        // The segment's targets are cells R .. R+S-1 of column (0, 0):
+        // consecutive keys, so one range of the cell order.
+        const int e00 = cs.c00 * nz + R;
+        const uint32_t t_seg = cst[e00], t_seg_end = cst[e00 + S - 1] + ccn[e00 + S - 1];
+        t_begin = t_seg + min(slice_lo, t_seg_end - t_seg);
+        t_end = t_seg + min(slice_hi, t_seg_end - t_seg);
+        if (t_begin >= t_end) return;  // uniform over the CTA
+        // staged offsets: an exclusive scan of the cell counts in (column,
+        // z-cell) order, each thread over a run of consecutive entries
+        const int ne = ncols * nz;
+        const int per = (ne + kThreads - 1) / kThreads;
+        const int e0 = min(tid * per, ne), e1 = min(e0 + per, ne);
+        uint32_t loc = 0;
+        for (int e = e0; e < e1; ++e) loc += ccn[e];
+        uint32_t inc = loc;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(kFull, inc, off);
+            if (lane >= off) inc += v;
+        }
+        if (lane == 31) s_wsum[warp] = inc;
+        __syncthreads();
+        uint32_t run = inc - loc;
+        total = 0;
+        for (int k = 0; k < kWarps; ++k) {
+            const uint32_t v = s_wsum[k];
+            if (k < warp) run += v;
+            total += v;
+        }
+        for (int e = e0; e < e1; ++e) {
+            const int col = col_of(e);
+            coff[col * zst + e - col * nz] = run;
+            run += ccn[e];
+        }
+        __syncthreads();
+        // per column: its end offset, its xy bounds and its (at most two)
+        // runs of z-cells with one periodic shift, each one contiguous range
+        // of the cell order (consecutive keys; the offset of an empty cell is
+        // where the next cell starts)
+        for (int col = tid; col < ncols; col += kThreads) {
+            const uint32_t cend = col + 1 < ncols ? coff[(col + 1) * zst] : total;
+            coff[col * zst + nz] = cend;
+            const int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
+            const float x0 = __fmul_rn((float)cxu, p.cellw), y0 = __fmul_rn((float)cyu, p.cellw);
+            cgeo[col] = make_float4(x0, __fadd_rn(x0, p.cellw), y0, __fadd_rn(y0, p.cellw));
+            const float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
+            const float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
+            const int z0 = iz0 - R;
+            // z-cells before the wrap (below z = 0 or from z = G on), if any
+            const int zw = z0 < 0 ? -z0 : (z0 + nz > G ? G - z0 : nz);
+            Run &r0 = runs[col * 2], &r1 = runs[col * 2 + 1];
+            r0.gsrc = cst[col * nz];
+            r0.soff = coff[col * zst];
+            r0.cnt = (zw < nz ? coff[col * zst + zw] : cend) - r0.soff;
+            r0.sx = sx;
+            r0.sy = sy;
+            r0.sz = z0 < 0 ? -L : 0.0f;
+            r1.cnt = 0;
+            if (zw < nz) {
+                r1.gsrc = cst[col * nz + zw];
+                r1.soff = coff[col * zst + zw];
+                r1.cnt = cend - r1.soff;
+                r1.sx = sx;
+                r1.sy = sy;
+                r1.sz = z0 < 0 ? 0.0f : L;
             }
         }
-        s_tbegin = tb;
-        s_tend = found ? te : tb;
-    }
-    __syncthreads();
-    const uint32_t t_seg = s_tbegin, t_seg_end = s_tend;
-    const uint32_t t_begin = t_seg + min(slice_lo, t_seg_end - t_seg);
-    const uint32_t t_end = t_seg + min(slice_hi, t_seg_end - t_seg);
-    if (t_begin >= t_end) return;
+        __syncthreads();
+    } else {
+        if (tid == 0) {
+            // the segment's cells are column (0, 0), z-cells R .. R+S-1
+            const int c00 = cs.c00;
+            uint32_t tb = 0, te = 0;
+            bool found = false;
+            for (int k = 0; k < S; ++k) {
+                const uint32_t st = cst[c00 * nz + R + k], cn = ccn[c00 * nz + R + k];
+                if (cn) {
+                    if (!found) tb = st;
+                    found = true;
+                    te = st + cn;
+                }
+            }
+            s_tbegin = tb;
+            s_tend = found ? te : tb;
+        }
+        __syncthreads();
+        const uint32_t t_seg = s_tbegin, t_seg_end = s_tend;
+        t_begin = t_seg + min(slice_lo, t_seg_end - t_seg);
+        t_end = t_seg + min(slice_hi, t_seg_end - t_seg);
+        if (t_begin >= t_end) return;
 
-    for (int i = tid; i < kNTab; i += kThreads) tab[i] = table_g[i];
-    if (tid == 0) src[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
-
-    // per column: staged offsets of its z-cells, runs of consecutive cells with one shift
-    for (int col = tid; col < ncols; col += kThreads) {
-        int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
-        const float x0 = __fmul_rn((float)cxu, p.cellw), y0 = __fmul_rn((float)cyu, p.cellw);
-        cgeo[col] = make_float4(x0, __fadd_rn(x0, p.cellw), y0, __fadd_rn(y0, p.cellw));
-        float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
-        float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
-        uint32_t acc = 0;
-        int nrun = 0;
-        int prev_wrap = -2;
-        for (int zc = 0; zc < nz; ++zc) {
-            int czu = iz0 - R + zc;
-            int wrap = czu < 0 ? -1 : (czu >= G ? 1 : 0);
-            const uint32_t st = cst[col * nz + zc], cn = ccn[col * nz + zc];
-            coff[col * zst + zc] = acc;  // relative, made absolute below
-            if (wrap != prev_wrap) {
-                Run &r = runs[col * 2 + (nrun < 2 ? nrun : 1)];
-                r.gsrc = 0xffffffffu;
-                r.soff = acc;
-                r.cnt = 0;
-                r.sx = sx;
-                r.sy = sy;
-                r.sz = wrap * L;
-                nrun++;
-                prev_wrap = wrap;
+        // per column: staged offsets of its z-cells, runs of consecutive cells with one shift
+        for (int col = tid; col < ncols; col += kThreads) {
+            int cxu = ix + cs.dx[col], cyu = iy + cs.dy[col];
+            const float x0 = __fmul_rn((float)cxu, p.cellw), y0 = __fmul_rn((float)cyu, p.cellw);
+            cgeo[col] = make_float4(x0, __fadd_rn(x0, p.cellw), y0, __fadd_rn(y0, p.cellw));
+            float sx = cxu < 0 ? -L : (cxu >= G ? L : 0.0f);
+            float sy = cyu < 0 ? -L : (cyu >= G ? L : 0.0f);
+            uint32_t acc = 0;
+            int nrun = 0;
+            int prev_wrap = -2;
+            for (int zc = 0; zc < nz; ++zc) {
+                int czu = iz0 - R + zc;
+                int wrap = czu < 0 ? -1 : (czu >= G ? 1 : 0);
+                const uint32_t st = cst[col * nz + zc], cn = ccn[col * nz + zc];
+                coff[col * zst + zc] = acc;  // relative, made absolute below
+                if (wrap != prev_wrap) {
+                    Run &r = runs[col * 2 + (nrun < 2 ? nrun : 1)];
+                    r.gsrc = 0xffffffffu;
+                    r.soff = acc;
+                    r.cnt = 0;
+                    r.sx = sx;
+                    r.sy = sy;
+                    r.sz = wrap * L;
+                    nrun++;
+                    prev_wrap = wrap;
+                }
+                if (cn) {
+                    Run &r = runs[col * 2 + (nrun - 1 < 1 ? nrun - 1 : 1)];
+                    if (r.gsrc == 0xffffffffu) r.gsrc = st;
+                    r.cnt += cn;
+                }
+                acc += cn;
             }
-            if (cn) {
-                Run &r = runs[col * 2 + (nrun - 1 < 1 ? nrun - 1 : 1)];
-                if (r.gsrc == 0xffffffffu) r.gsrc = st;
-                r.cnt += cn;
+            coff[col * zst + nz] = acc;
+            if (nrun < 2) runs[col * 2 + 1].cnt = 0;
+            coltot[col] = acc;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t run = 0;
+            for (int col = 0; col < ncols; ++col) {
+                uint32_t t = coltot[col];
+                coltot[col] = run;
+                run += t;
             }
-            acc += cn;
+            s_total = run;
         }
-        coff[col * zst + nz] = acc;
-        if (nrun < 2) runs[col * 2 + 1].cnt = 0;
-        coltot[col] = acc;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t run = 0;
-        for (int col = 0; col < ncols; ++col) {
-            uint32_t t = coltot[col];
-            coltot[col] = run;
-            run += t;
+        __syncthreads();
+        for (int e = tid; e < ncols * zst; e += kThreads) coff[e] += coltot[e / zst];
+        for (int col = tid; col < ncols; col += kThreads) {
+            runs[col * 2].soff += coltot[col];
+            runs[col * 2 + 1].soff += coltot[col];
         }
-        s_total = run;
+        __syncthreads();
+        total = s_total;
     }
-    __syncthreads();
-    for (int e = tid; e < ncols * zst; e += kThreads) coff[e] += coltot[e / zst];
-    for (int col = tid; col < ncols; col += kThreads) {
-        runs[col * 2].soff += coltot[col];
-        runs[col * 2 + 1].soff += coltot[col];
-    }
-    __syncthreads();
-    const uint32_t total = s_total;
     const bool single_chunk = total <= (uint32_t)kMaxStage;
 
     const uint32_t nt = t_end - t_begin;
@@ -401,13 +487,36 @@ __device__ __forceinline__ void shortrange_segment(
                 const float q = __fsub_rn(rc2m, __fmaf_rn(ddy, ddy, __fmul_rn(ddx, ddx)));
                 if (q >= 0.f) {
                     // half-height of the cut disc over this column (an
-                    // approximate square root: the margin covers it)
+                    // approximate square root: the margin covers it), in
+                    // cells from the column's first z-cell
                     const float hz = __fmul_rn(q, rsqrtf(fmaxf(q, 1e-30f)));
-                    const int zlo = max(__float2int_rd(__fmaf_rn(pt.z - hz, winv, -zbase)), 0);
-                    const int zhi = min(__float2int_rd(__fmaf_rn(pt.z + hz, winv, -zbase)), nz - 1);
+                    const float ul = __fmaf_rn(pt.z - hz, winv, -zbase), uh = __fmaf_rn(pt.z + hz, winv, -zbase);
+                    const int fl = __float2int_rd(ul), fh = __float2int_rd(uh);
+                    const int zlo = max(fl, 0), zhi = min(fh, nz - 1);
                     if (zlo <= zhi) {
-                        b = max(coff[col * zst + zlo], c0);
-                        e = min(coff[col * zst + zhi + 1], c1);
+                        b = coff[col * zst + zlo];
+                        e = coff[col * zst + zhi + 1];
+                        if (ZS) {
+                            // the end cells hold their sources by z slice: drop
+                            // the slices below ul and above uh (a cell whose
+                            // counts saturated, 0xffff, is kept whole)
+                            if (fl >= 0) {
+                                const int kl = __float2int_rd(__fmul_rn(__fsub_rn(ul, (float)fl), (float)kZSub));
+                                if (kl > 0) {
+                                    const uint32_t o = sl16[(col * nz + zlo) * kZSub + min(kl, kZSub) - 1];
+                                    if (o != 0xffffu) b += o;
+                                }
+                            }
+                            if (fh <= nz - 1) {
+                                const int kh = __float2int_rd(__fmul_rn(__fsub_rn(uh, (float)fh), (float)kZSub));
+                                if (kh < kZSub - 1) {
+                                    const uint32_t o = sl16[(col * nz + zhi) * kZSub + max(kh, 0)];
+                                    if (o != 0xffffu) e = coff[col * zst + zhi] + o;
+                                }
+                            }
+                        }
+                        b = max(b, c0);
+                        e = min(e, c1);
                     }
                 }
             }
@@ -564,6 +673,7 @@ __device__ __forceinline__ void shortrange_segment(
                     src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
                     if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
                 }
+
             }
         }
     };
@@ -591,10 +701,10 @@ __device__ __forceinline__ void shortrange_segment(
                 s_acc[2][t] = az * mg;
             }
         }
-        // the epilogues of all the unit's targets side by side
-        __syncthreads();
-        for (uint32_t t = tid; t < nt; t += kThreads)
-            epilogue(t, make_float4(s_acc[0][t], s_acc[1][t], s_acc[2][t], 0.f));
+        // the warp's epilogues side by side: lane r takes its round r target
+        __syncwarp();
+        const uint32_t t = lane * kWarps + warp;
+        if (lane < rounds && t < nt) epilogue(t, make_float4(s_acc[0][t], s_acc[1][t], s_acc[2][t], 0.f));
     } else {
         for (uint32_t t = tid; t < nt; t += kThreads)
             for (int k = 0; k < 6; ++k) s_acc[k][t] = 0.f;
@@ -708,6 +818,15 @@ __device__ __forceinline__ bool next_unit(const SRWork &w, uint32_t nseg, uint32
     return true;
 }
 
+// The split table and the sentinel source, once per CTA: every unit reads
+// them (the first unit's barrier orders these writes).
+__device__ __forceinline__ void load_table(const float *__restrict__ table_g) {
+    extern __shared__ float4 smem_f4[];
+    float *tab = reinterpret_cast<float *>(smem_f4 + kMaxStage + 1);
+    for (int i = threadIdx.x; i < kNTab; i += kThreads) tab[i] = table_g[i];
+    if (threadIdx.x == 0) smem_f4[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
+}
+
 // Persistent: as many CTAs as fit on the GPU, each taking units until none
 // is left, so a few dense segments no longer leave most SMs idle.
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
@@ -720,6 +839,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                  unsigned long long *__restrict__ pair_counter) {
     uint32_t seg, lo;
     bool skip;
+    load_table(table_g);
     while (next_unit(w, nseg, &seg, &lo, &skip)) {
         if (skip) continue;
         shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, (int)seg, lo, lo + kTMax, kick.kick_pp, kick.kick_pm,
@@ -750,6 +870,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                        const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
     uint32_t seg, lo;
     bool skip;
+    load_table(table_g);
     while (next_unit(w, nseg, &seg, &lo, &skip)) {
         if (skip) continue;
         const int b = find_box(seg_base, nbox, seg);
@@ -796,6 +917,7 @@ bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
         for (int dy = -R; dy <= R; ++dy) {
             double ex = fmax(abs(dx) - 1, 0) * w, ey = fmax(abs(dy) - 1, 0) * w;
             if (ex * ex + ey * ey > rc * rc) continue;
+            if (dx == 0 && dy == 0) cs->c00 = n;
             cs->dx[n] = (signed char)dx;
             cs->dy[n] = (signed char)dy;
             n++;
@@ -811,8 +933,8 @@ void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const Colum
                      const SRWork &work, const float4 *sorted_pos, const uint32_t *perm,
                      const uint32_t *cell_a, const uint32_t *cell_b, const float *table,
                      float4 *acc_out, const KickArgs &kick, unsigned long long *counter) {
-    const size_t sm = smem_bytes(cs.ncols, cs.S + 2 * cs.R);
-    static const size_t sm_max = smem_bytes(kMaxCols, kMaxSeg + 2 * kMaxR);
+    const size_t sm = smem_bytes(cs.ncols, cs.S + 2 * cs.R, p.slices != nullptr);
+    static const size_t sm_max = smem_base_bytes(kMaxCols, kMaxSeg + 2 * kMaxR) + kMaxSliceTable;
     static bool attr = [] {
         cudaFuncSetAttribute(k_shortrange<FMT, KICK, true, FIXED>,
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
@@ -834,12 +956,18 @@ void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const Colum
 
 uint32_t shortrange_heavy_cap(uint32_t n) { return 2u * (n / kTMax) + 16u; }
 
-cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,
+// The slice table where the sources are in slice order and it fits.
+static bool use_slices(const ShortRangeParams &p, const ColumnSet &cs) {
+    return p.slices != nullptr && sizeof(uint4) * (size_t)cs.ncols * (cs.S + 2 * cs.R) <= kMaxSliceTable;
+}
+
+cuco_status_t launch_shortrange(const ShortRangeParams &p_in, const float4 *sorted_pos,
                                 const uint32_t *perm, const uint32_t *cell_a,
                                 const uint32_t *cell_b, CellFormat fmt, const float *table,
                                 float4 *acc_out, const KickArgs &kick, const SRWork &work, cudaStream_t stream,
                                 unsigned long long *pair_counter) {
     ColumnSet cs;
+    ShortRangeParams p = p_in;
     if (!build_columns(p, &cs)) {
         set_error("short range: cell grid does not fit rcut (need rcut <= 8 cell widths, "
                   "rcut < L/2 and at least S+2R cells per dimension)");
@@ -853,6 +981,7 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
         return CUCO_ERR_INVALID;
     }
     const bool kick_on = kick.vel != nullptr;
+    if (fmt != kCellOffsets || !use_slices(p, cs)) p.slices = nullptr;
     if (p.fixed && fmt != kCellOffsets) {
         set_error("short range: fixed-point positions need the engine's cell-offset format");
         return CUCO_ERR_UNSUPPORTED;
@@ -892,9 +1021,10 @@ cuco_status_t shortrange_desc_fill(const ShortRangeParams &p, void *desc, uint32
                   "rcut < L/2 and at least S+2R cells per dimension)");
         return CUCO_ERR_UNSUPPORTED;
     }
+    if (!use_slices(d.p, d.cs)) d.p.slices = nullptr;
     memcpy(desc, &d, sizeof d);
     *segments = (uint32_t)p.grid * p.grid * (p.grid / d.cs.S);
-    *smem = smem_bytes(d.cs.ncols, d.cs.S + 2 * d.cs.R);
+    *smem = smem_bytes(d.cs.ncols, d.cs.S + 2 * d.cs.R, d.p.slices != nullptr);
     return CUCO_OK;
 }
 
@@ -903,7 +1033,7 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
                                       const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
                                       const float *table, float4 *acc_out, const KickArgs &kick,
                                       const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter) {
-    static const size_t sm_max = smem_bytes(kMaxCols, kMaxSeg + 2 * kMaxR);
+    static const size_t sm_max = smem_base_bytes(kMaxCols, kMaxSeg + 2 * kMaxR) + kMaxSliceTable;
     static bool attr = [] {
         cudaFuncSetAttribute(k_shortrange_multi<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
         cudaFuncSetAttribute(k_shortrange_multi<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);

@@ -300,10 +300,122 @@ __global__ void k_reorder_offsets(uint32_t *__restrict__ cell_off, float4 *__res
     uint32_t prev = i == 0 ? 0u : skeys[i - 1] + 1u;
     uint32_t cur = i == n ? ncells : skeys[i];
     for (uint32_t c = prev; c <= cur; ++c) cell_off[c] = i;
-    if (i < n) sorted_pos[i] = pos[perm[i]];
+    if (i < n && sorted_pos) sorted_pos[i] = pos[perm[i]];
+}
+
+// One warp per cell: a stable counting sort of the cell's particles by z
+// slice.  A lane's slice is spelled out by four ballots (three slice bits and
+// "no particle"), so the lanes of each slice, their counts and each lane's
+// rank among equal slices are popcounts; lane k < kZSub keeps slice k's
+// running offset.  The order is fixed by the input order alone.
+__global__ void k_cell_subsort(const uint32_t *__restrict__ cell_off, const uint32_t *__restrict__ perm,
+                               const float4 *__restrict__ pos, float4 *__restrict__ sorted_pos,
+                               uint32_t *__restrict__ perm_s, uint4 *__restrict__ slices, uint32_t ncells,
+                               const __grid_constant__ CellBox one, const CellBox *__restrict__ boxes, int nbox,
+                               int fixed) {
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    if (c >= ncells) return;  // warp-uniform
+    const uint32_t a = cell_off[c], b = cell_off[c + 1];
+    // lanes 0..kZSub-1 write the cell's inclusive slice counts as u16
+    uint16_t *sl = reinterpret_cast<uint16_t *>(slices + c);
+    auto put_counts = [&](uint32_t incl) {
+        if (lane < kZSub) sl[lane] = b - a >= 0xffffu ? (uint16_t)0xffffu : (uint16_t)incl;
+    };
+    if (a >= b) {
+        put_counts(0);
+        return;
+    }
+    CellBox d = one;
+    if (boxes) {
+        int lo = 0, hi = nbox;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(&boxes[mid].cell_base) <= c)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        d = boxes[lo];
+    }
+    const uint32_t cz = (c - d.cell_base) % d.G;
+    const uint32_t lt = (1u << lane) - 1u;
+    // slice of z within cell cz: plain, of the key rule's product G/L * z
+    // (in [cz, cz + 1) but for the clamped top face); fixed point, the three
+    // bits below the cell index of z * G / 2^32
+    auto slice = [&](float4 p) -> uint32_t {
+        if (fixed) return (uint32_t)(((uint64_t)__float_as_uint(p.z) * d.G) >> (32 - kZSubBits)) & (kZSub - 1);
+        const float t = __fmul_rn(p.z, d.gridfac);
+        const int s = __float2int_rd(__fmul_rn(__fsub_rn(t, (float)cz), (float)kZSub));
+        return (uint32_t)min(max(s, 0), kZSub - 1);
+    };
+    // lanes holding slice k (k = kZSub: no particle)
+    auto lanes_of = [&](uint32_t k, uint32_t b0, uint32_t b1, uint32_t b2, uint32_t none) {
+        return ((k & 1) ? b0 : ~b0) & ((k & 2) ? b1 : ~b1) & ((k & 4) ? b2 : ~b2) & ~none;
+    };
+    uint32_t base = 0;  // lane k < kZSub: slice k's next offset
+    if (b - a > 32) {
+        for (uint32_t i0 = a; i0 < b; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const uint32_t s = i < b ? slice(pos[perm[i]]) : (uint32_t)kZSub;
+            const uint32_t b0 = __ballot_sync(0xffffffffu, s & 1), b1 = __ballot_sync(0xffffffffu, s & 2),
+                           b2 = __ballot_sync(0xffffffffu, s & 4), none = __ballot_sync(0xffffffffu, s == kZSub);
+            if (lane < kZSub) base += __popc(lanes_of(lane, b0, b1, b2, none));
+        }
+        // exclusive scan of the slice counts over lanes 0..kZSub-1
+        uint32_t incl = base;
+        for (int off = 1; off < kZSub; off <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= (uint32_t)off) incl += v;
+        }
+        put_counts(incl);
+        base = incl - base;
+    }
+    for (uint32_t i0 = a; i0 < b; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        uint32_t o = 0, s = kZSub;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (i < b) {
+            o = perm[i];
+            p = pos[o];
+            s = slice(p);
+        }
+        const uint32_t b0 = __ballot_sync(0xffffffffu, s & 1), b1 = __ballot_sync(0xffffffffu, s & 2),
+                       b2 = __ballot_sync(0xffffffffu, s & 4), none = __ballot_sync(0xffffffffu, s == kZSub);
+        const uint32_t mine = lanes_of(s, b0, b1, b2, none);
+        const uint32_t cnt = lane < kZSub ? __popc(lanes_of(lane, b0, b1, b2, none)) : 0u;
+        if (b - a <= 32) {
+            // one chunk: the offsets are the exclusive scan of this chunk's counts
+            uint32_t incl = cnt;
+            for (int off = 1; off < kZSub; off <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= (uint32_t)off) incl += v;
+            }
+            put_counts(incl);
+            base = incl - cnt;
+        }
+        const uint32_t at = __shfl_sync(0xffffffffu, base, s & (kZSub - 1)) + __popc(mine & lt);
+        if (i < b) {
+            sorted_pos[a + at] = make_float4(p.x, p.y, p.z, (float)s);
+            perm_s[a + at] = o;
+        }
+        base += cnt;
+    }
 }
 
 }  // namespace
+
+cuco_status_t launch_cell_subsort(const uint32_t *cell_off, const uint32_t *perm, const float4 *pos,
+                                  float4 *sorted_pos, uint32_t *perm_s, uint4 *slices, uint32_t ncells,
+                                  const CellBox &one, const CellBox *boxes, int nbox, bool fixed,
+                                  cudaStream_t stream) {
+    if (ncells == 0) return CUCO_OK;
+    const uint64_t threads = 32ull * ncells;
+    k_cell_subsort<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(
+        cell_off, perm, pos, sorted_pos, perm_s, slices, ncells, one, boxes, nbox, fixed ? 1 : 0);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return CUCO_OK;
+}
 
 size_t sort_hist_entries(uint32_t n, int key_bits, int max_radix_bits) {
     int passes, rb;

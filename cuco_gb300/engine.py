@@ -191,6 +191,13 @@ class Box:
     def launches(self) -> int:
         return int(self.lib.cuco_box_launches_per_step(self.h))
 
+    def cell_order(self):
+        """The short range's source order: (perm_s, slice) per sorted position."""
+        perm_s = np.empty(self.n, dtype=np.uint32)
+        sl = np.empty(self.n, dtype=np.float32)
+        check(self.lib.cuco_box_cell_order(self.h, ptr(perm_s), ptr(sl)), "cuco_box_cell_order")
+        return perm_s, sl
+
     def debug(self):
         n, nc = self.n, self.c.cell_grid ** 3
         keys = np.empty(n, dtype=np.uint32)

@@ -252,6 +252,12 @@ cuco_status_t cuco_box_timings(cuco_box_t *box, float *ms /* 8 */);
 cuco_status_t cuco_box_debug(cuco_box_t *box, uint32_t *sorted_keys, uint32_t *perm,
                              uint32_t *cell_start, uint32_t *cell_end);
 
+/* The order the short range reads its sources in (no counterpart in the
+ * reference): the sort's cells, each refined by z slice (8 slices of the cell
+ * along z, stable within a slice).  perm_s[i] is the original index of the
+ * i-th particle in that order, slice[i] its slice.  Either pointer may be NULL. */
+cuco_status_t cuco_box_cell_order(cuco_box_t *box, uint32_t *perm_s, float *slice);
+
 /* Number of kernel launches one cuco_box_step issues. */
 int cuco_box_launches_per_step(cuco_box_t *box);
 
