@@ -136,6 +136,7 @@ SIGNATURES = {
     "cuco_box_debug": (_I, [_P, _P, _P, _P, _P]),
     "cuco_box_cell_order": (_I, [_P, _P, _P]),
     "cuco_box_launches_per_step": (_I, [_P]),
+    "cuco_box_count_pairs": (_I, [_P, _I]),
     "cuco_box_pair_count": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), _I]),
     "cuco_box_timer": (_I, [_P, _I, ctypes.POINTER(ctypes.c_float)]),
     "cuco_ensemble_create": (_I, [ctypes.POINTER(CucoConfig), _I, ctypes.POINTER(_P)]),

@@ -106,6 +106,12 @@ struct ShortRangeParams {
     bool fixed;      // positions are 32-bit fixed point (bit patterns in the float4s)
     float fscale;    // L / 2^32
     uint32_t cell_base;  // first cell of this box in a multi-box cell array (0 otherwise)
+    // pair-law bounds, filled in by the short-range launch from the above:
+    // fast-path cut and flag cut (plain: a band around rcut^2 decided in
+    // double), the softening bound below which the spline applies, the bin
+    // factor scaled down and up by the bin-edge band, rcut^2 in double
+    float rc2_lo, rc2_hi, hmin2, alo, ahi;
+    double rcut2_d;
     // the z-slice counts of the cells (launch_cell_subsort), indexed by cell
     // id; null when the sources are not in slice order or the per-segment
     // table would not fit in shared memory

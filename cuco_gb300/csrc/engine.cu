@@ -301,6 +301,7 @@ struct cuco_box {
     PMPlan pm{};
     bool has_state = false;
     bool timing = false;
+    bool count_pairs = false;
     cudaEvent_t ev[8] = {};
     float last_ms[8] = {};
     int launches = 0;
@@ -391,7 +392,7 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
         k.acc_pm_out = pm ? b->acc_pm : nullptr;
         CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, perm_s, b->cell_off,
                                    nullptr, kCellOffsets, b->table, b->acc_pp, k, b->work, b->stream,
-                                   b->timing ? b->pair_counter : nullptr));
+                                   b->count_pairs ? b->pair_counter : nullptr));
         b->launches += 2;  // work plan + persistent short range
     } else if (pm) {
         CUCO_TRY(scatter4(b->acc_pm_s, perm_s, b->acc_pm, b->n, b->stream));
@@ -719,6 +720,12 @@ cuco_status_t cuco_box_cell_order(cuco_box_t *b, uint32_t *perm_s, float *slice)
 }
 
 int cuco_box_launches_per_step(cuco_box_t *b) { return b ? b->launches : 0; }
+
+cuco_status_t cuco_box_count_pairs(cuco_box_t *b, int enable) {
+    if (!b) return CUCO_ERR_INVALID;
+    b->count_pairs = enable != 0;
+    return CUCO_OK;
+}
 
 cuco_status_t cuco_box_pair_count(cuco_box_t *b, uint64_t *pairs, int reset) {
     if (!b || !pairs) return CUCO_ERR_INVALID;

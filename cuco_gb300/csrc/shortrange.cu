@@ -57,6 +57,9 @@ constexpr int kMaxSeg = 8;
 // A unit of work is at most kTMax targets: a segment with that many, or a
 // kTMax slice of a denser segment.
 constexpr int kTMax = 128;
+// the split table in shared memory, padded to a power of two
+constexpr int kTabPad = 1024;
+static_assert(kTabPad >= kNTab && (kTabPad & (kTabPad - 1)) == 0, "table padding");
 constexpr unsigned kFull = 0xffffffffu;
 // CTAs per SM the register allocation is sized for (65536 / (256 * 4) = 64
 // registers a thread at 4)
@@ -92,7 +95,7 @@ struct Run {
 // split table, column xy bounds, per-(column, z-cell) staged offsets, cell
 // starts and counts, column runs, column totals.
 __host__ __device__ inline size_t smem_base_bytes(int ncols, int nz) {
-    const size_t b = sizeof(float4) * (kMaxStage + 1) + sizeof(float) * kNTab + sizeof(float4) * (size_t)ncols +
+    const size_t b = sizeof(float4) * (kMaxStage + 1) + sizeof(float) * kTabPad + sizeof(float4) * (size_t)ncols +
                      sizeof(uint32_t) * (size_t)ncols * (nz + 1) + 2 * sizeof(uint32_t) * (size_t)ncols * nz +
                      sizeof(Run) * 2 * (size_t)ncols + sizeof(uint32_t) * (size_t)ncols;
     return (b + 15) & ~(size_t)15;
@@ -172,7 +175,7 @@ __device__ __forceinline__ void shortrange_segment(
     const int zst = nz + 1;  // coff stride per column
     float4 *src = smem_f4;
     float *tab = reinterpret_cast<float *>(src + kMaxStage + 1);
-    float4 *cgeo = reinterpret_cast<float4 *>(tab + kNTab);  // x0, x1, y0, y1 (16-B aligned: 4000 = 250 * 16)
+    float4 *cgeo = reinterpret_cast<float4 *>(tab + kTabPad);  // x0, x1, y0, y1
     uint32_t *coff = reinterpret_cast<uint32_t *>(cgeo + ncols);
     uint32_t *cst = coff + ncols * zst;
     uint32_t *ccn = cst + ncols * nz;
@@ -382,19 +385,12 @@ __device__ __forceinline__ void shortrange_segment(
                            __fmul_rn((float)(int32_t)(__float_as_uint(a.y) - oyu), fs),
                            __fmul_rn((float)(int32_t)(__float_as_uint(a.z) - ozu), fs), 0.f);
     };
-    const float kEdge = 4e-7f;
-    // plain: cut-edge band decided in double; fixed: the float cut
-    const float rc2_lo = FIXED ? p.rcut2 : p.rcut2 * (1.f - 2.f * kEdge);
-    const float rc2_hi = FIXED ? p.rcut2 : p.rcut2 * (1.f + 2.f * kEdge);
-    const double rcut2_d = (double)p.rcut * (double)p.rcut;
     uint32_t npairs = 0;
     uint32_t *wdelta = s_wdelta[warp];
     const uint32_t lt_mask = (1u << lane) - 1u, le_mask = lt_mask | (1u << lane);
     float tx = 0.f, ty = 0.f, tz = 0.f;  // the current target, origin-relative
 
     // Kernel parameters used per candidate, held in registers.
-    const float asmf = p.asmthfac, hh = p.h, hinv = p.hinv, h3inv = p.h3inv;
-    const double asmd = p.asmthfac_d;
 
     // The pair law, in two parts.  pair_fast takes the common case - inside
     // the cut, away from a table-bin edge and from the cut, outside the
@@ -403,49 +399,51 @@ __device__ __forceinline__ void shortrange_segment(
     // made in double and the spline inside h (the self pair, r = 0, adds
     // nothing and is skipped).  pair_slow applies the full law to those.  Both add into the same
     // accumulators in the same order as a single law would.
-    const float hmin = fmaxf(hh, 1e-9f);
-    const float hmin2 = hmin * hmin;  // r2 below it (the spline, r2 = 0) takes the full law
+    // The bounds (p.rc2_lo, ...) are the launch's constants, read where used.
     // bin = floor(asmthfac * r): a round-toward-zero fma onto 2^23 leaves the
     // floor in the mantissa, with no conversion instruction.  Plain: the bins
     // of r * asmthfac * (1 -/+ kEdge) differ when r lies within kEdge
-    // (relative) of a bin edge, and such a pair is decided in double.
-    const float alo = FIXED ? asmf : asmf * (1.f - kEdge), ahi = FIXED ? asmf : asmf * (1.f + kEdge);
+    // (relative) of a bin edge, and such a pair is decided in double.  The
+    // table is padded to kTabPad entries with its last value, so a bin index
+    // masked to the padding is the clamped one (fast pairs have bins below
+    // kNTab; others read a padding value they do not use).
     auto pair_fast = [&](float4 s, float &ax, float &ay, float &az) -> bool {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
         // r2 = 0 gives rinv = inf and r = NaN: not fast (r2 < hmin2), not flagged
         const float rinv = rsqrtf(r2);
         const float r = r2 * rinv;
-        const float xl = __fmaf_rz(r, alo, 8388608.0f);
-        const bool edge = !FIXED && xl != __fmaf_rz(r, ahi, 8388608.0f);
+        const float xl = __fmaf_rz(r, p.alo, 8388608.0f);
+        const bool edge = !FIXED && xl != __fmaf_rz(r, p.ahi, 8388608.0f);
         const uint32_t ti = (uint32_t)(__float_as_int(xl) - 0x4B000000);
-        const bool fast = r2 <= rc2_lo && r2 >= hmin2 && !edge;
-        const float fac = fast ? rinv * rinv * rinv * tab[min(ti, (uint32_t)kNTab - 1u)] : 0.f;
+        const bool fast = r2 <= p.rc2_lo && r2 >= p.hmin2 && !edge;
+        const float fac = fast ? rinv * rinv * rinv * tab[ti & (kTabPad - 1)] : 0.f;
         ax = __fmaf_rn(dx, fac, ax);
         ay = __fmaf_rn(dy, fac, ay);
         az = __fmaf_rn(dz, fac, az);
         if (COUNT) npairs += fast;
         // r2 == 0 (the self pair, or a coincident source) adds dx*fac = 0:
         // not flagged, so the rare-case branch is not taken once per target
-        return r2 <= rc2_hi && r2 != 0.f && !fast;
+        return r2 <= p.rc2_hi && r2 != 0.f && !fast;
     };
     auto pair_slow = [&](float4 s, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
-        bool ok = r2 <= rc2_hi && r2 != 0.f;
+        bool ok = r2 <= p.rc2_hi && r2 != 0.f;
         const float rinv = rsqrtf(ok ? r2 : 1.f);
         const float r = r2 * rinv;
-        const float xl = __fmaf_rz(r, alo, 8388608.0f);
+        const float xl = __fmaf_rz(r, p.alo, 8388608.0f);
         int ti = __float_as_int(xl) - 0x4B000000;
         float fac = rinv * rinv * rinv;
-        if (!FIXED && (xl != __fmaf_rz(r, ahi, 8388608.0f) || r2 > rc2_lo)) {
+        if (!FIXED && (xl != __fmaf_rz(r, p.ahi, 8388608.0f) || r2 > p.rc2_lo)) {
             // decided in double as the reference's CPU path computes it
             const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
-            ok = ok && dd <= rcut2_d;
-            ti = (int)(asmd * sqrt(dd));
+            ok = ok && dd <= p.rcut2_d;
+            ti = (int)(p.asmthfac_d * sqrt(dd));
         }
-        if (r < hh) {
-            const float u = r * hinv;
+        if (r < p.h) {
+            const float u = r * p.hinv;
+            const float h3inv = p.h3inv;
             if (u < 0.5f)
                 fac = __fmul_rn(h3inv, __fmaf_rn(__fmul_rn(u, u), __fmaf_rn(32.0f, u, -38.4f), 10.66667f));
             else
@@ -823,7 +821,7 @@ __device__ __forceinline__ bool next_unit(const SRWork &w, uint32_t nseg, uint32
 __device__ __forceinline__ void load_table(const float *__restrict__ table_g) {
     extern __shared__ float4 smem_f4[];
     float *tab = reinterpret_cast<float *>(smem_f4 + kMaxStage + 1);
-    for (int i = threadIdx.x; i < kNTab; i += kThreads) tab[i] = table_g[i];
+    for (int i = threadIdx.x; i < kTabPad; i += kThreads) tab[i] = table_g[min(i, kNTab - 1)];
     if (threadIdx.x == 0) smem_f4[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
 }
 
@@ -956,6 +954,19 @@ void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const Colum
 
 uint32_t shortrange_heavy_cap(uint32_t n) { return 2u * (n / kTMax) + 16u; }
 
+// The pair-law bounds the kernel reads from its parameters.
+static void finish_pair_law(ShortRangeParams &p) {
+    const float kEdge = 4e-7f;
+    // plain: cut-edge band decided in double; fixed: the float cut
+    p.rc2_lo = p.fixed ? p.rcut2 : p.rcut2 * (1.f - 2.f * kEdge);
+    p.rc2_hi = p.fixed ? p.rcut2 : p.rcut2 * (1.f + 2.f * kEdge);
+    const float hmin = std::max(p.h, 1e-9f);
+    p.hmin2 = hmin * hmin;
+    p.alo = p.fixed ? p.asmthfac : p.asmthfac * (1.f - kEdge);
+    p.ahi = p.fixed ? p.asmthfac : p.asmthfac * (1.f + kEdge);
+    p.rcut2_d = (double)p.rcut * (double)p.rcut;
+}
+
 // The slice table where the sources are in slice order and it fits.
 static bool use_slices(const ShortRangeParams &p, const ColumnSet &cs) {
     return p.slices != nullptr && sizeof(uint4) * (size_t)cs.ncols * (cs.S + 2 * cs.R) <= kMaxSliceTable;
@@ -968,6 +979,7 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p_in, const float4 *sort
                                 unsigned long long *pair_counter) {
     ColumnSet cs;
     ShortRangeParams p = p_in;
+    finish_pair_law(p);
     if (!build_columns(p, &cs)) {
         set_error("short range: cell grid does not fit rcut (need rcut <= 8 cell widths, "
                   "rcut < L/2 and at least S+2R cells per dimension)");
@@ -1016,6 +1028,7 @@ size_t shortrange_desc_bytes() { return sizeof(SRBoxDesc); }
 cuco_status_t shortrange_desc_fill(const ShortRangeParams &p, void *desc, uint32_t *segments, size_t *smem) {
     SRBoxDesc d{};
     d.p = p;
+    finish_pair_law(d.p);
     if (!build_columns(p, &d.cs)) {
         set_error("short range: cell grid does not fit rcut (need rcut <= 8 cell widths, "
                   "rcut < L/2 and at least S+2R cells per dimension)");

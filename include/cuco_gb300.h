@@ -262,7 +262,10 @@ cuco_status_t cuco_box_cell_order(cuco_box_t *box, uint32_t *perm_s, float *slic
 int cuco_box_launches_per_step(cuco_box_t *box);
 
 /* In-range pair count (r^2 <= rcut^2, self excluded) of the short-range
- * launches since the last reset; counted only while phase timing is enabled. */
+ * launches since the last reset, counted only while cuco_box_count_pairs is
+ * enabled (the counting kernel is slightly slower; no counterpart in the
+ * reference). */
+cuco_status_t cuco_box_count_pairs(cuco_box_t *box, int enable);
 cuco_status_t cuco_box_pair_count(cuco_box_t *box, uint64_t *pairs, int reset);
 
 /* Device-time bracket on the box's stream: op 0 records the start event,
