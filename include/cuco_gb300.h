@@ -181,7 +181,7 @@ typedef enum {
 
 typedef struct {
     int64_t n;        /* particles */
-    int pm_grid;      /* PM mesh size M (power of two, 16..1024) */
+    int pm_grid;      /* PM mesh size M (even, 8..1024, no prime factor above 5) */
     int cell_grid;    /* short-range cell grid G (cell width >= rcut/2) */
     float boxsize;    /* L, internal length units */
     float mass;       /* particle mass */
