@@ -133,6 +133,7 @@ SIGNATURES = {
     "cuco_box_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "cuco_box_enable_timing": (_I, [_P, _I]),
     "cuco_box_timings": (_I, [_P, _P]),
+    "cuco_box_phase_totals": (_I, [_P, _P, _I]),
     "cuco_box_debug": (_I, [_P, _P, _P, _P, _P]),
     "cuco_box_cell_order": (_I, [_P, _P, _P]),
     "cuco_box_launches_per_step": (_I, [_P]),

@@ -302,8 +302,14 @@ struct cuco_box {
     bool has_state = false;
     bool timing = false;
     bool count_pairs = false;
-    cudaEvent_t ev[8] = {};
+    // phase events, two sets: a step records into ev[ev_cur] and the set of
+    // the step before is read then, so timing never waits on the step just
+    // enqueued
+    cudaEvent_t ev[2][8] = {};
+    int ev_cur = 0;
+    bool ev_pending = false;  // ev[ev_cur ^ 1] holds a recorded step not yet read
     float last_ms[8] = {};
+    float acc_ms[8] = {};     // phase sums since timing was enabled (or reset)
     int launches = 0;
     unsigned long long *pair_counter = nullptr;
     cudaEvent_t tstart = nullptr, tstop = nullptr;
@@ -353,7 +359,7 @@ cuco_status_t drift_keys(cuco_box *b, double drift, bool do_drift) {
 }
 
 void record(cuco_box *b, int i) {
-    if (b->timing) cudaEventRecord(b->ev[i], b->stream);
+    if (b->timing) cudaEventRecord(b->ev[b->ev_cur][i], b->stream);
 }
 
 // keys must already be in b->keys; runs sort, reorder, PM, short range (+kick)
@@ -378,7 +384,7 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
     record(b, 3);
     if (pm) {
         CUCO_TRY(pm_forces(b->pm, b->spos, b->n, b->acc_pm_s, b->stream,
-                           b->timing ? &b->ev[4] : nullptr, b->timing ? &b->ev[5] : nullptr,
+                           b->timing ? &b->ev[b->ev_cur][4] : nullptr, b->timing ? &b->ev[b->ev_cur][5] : nullptr,
                            &b->launches));
     } else {
         record(b, 4);
@@ -402,17 +408,32 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
     return CUCO_OK;
 }
 
-cuco_status_t finish_timing(cuco_box *b) {
-    if (!b->timing) return CUCO_OK;
-    CUCO_TRY_CUDA(cudaEventSynchronize(b->ev[7]));
+// Phase times of the pending set into last_ms and acc_ms.
+cuco_status_t read_pending(cuco_box *b) {
+    if (!b->ev_pending) return CUCO_OK;
+    b->ev_pending = false;
+    cudaEvent_t *e = b->ev[b->ev_cur ^ 1];
+    CUCO_TRY_CUDA(cudaEventSynchronize(e[7]));
     for (int i = 0; i < 7; ++i) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, b->ev[i], b->ev[i + 1]);
+        cudaEventElapsedTime(&ms, e[i], e[i + 1]);
         b->last_ms[i] = ms;
+        b->acc_ms[i] += ms;
     }
     float tot = 0.f;
-    cudaEventElapsedTime(&tot, b->ev[0], b->ev[7]);
+    cudaEventElapsedTime(&tot, e[0], e[7]);
     b->last_ms[7] = tot;
+    b->acc_ms[7] += tot;
+    return CUCO_OK;
+}
+
+// End of a timed force pass: read the step before (done, or nearly, by the
+// time this one is enqueued), leave this one pending, switch sets.
+cuco_status_t finish_timing(cuco_box *b) {
+    if (!b->timing) return CUCO_OK;
+    CUCO_TRY(read_pending(b));
+    b->ev_pending = true;
+    b->ev_cur ^= 1;
     return CUCO_OK;
 }
 
@@ -496,7 +517,8 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
     cudaMemsetAsync(b->acc_pp, 0, sizeof(float4) * (n ? n : 1), b->stream);
     cudaMemsetAsync(b->acc_pm, 0, sizeof(float4) * (n ? n : 1), b->stream);
     cudaMemsetAsync(b->vel, 0, sizeof(float4) * (n ? n : 1), b->stream);
-    for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[i]);
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[k][i]);
     cudaEventCreate(&b->tstart);
     cudaEventCreate(&b->tstop);
     *out = b;
@@ -528,8 +550,9 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     if (b->tstart) cudaEventDestroy(b->tstart);
     if (b->tstop) cudaEventDestroy(b->tstop);
     if (b->pm.rho) pm_plan_destroy(&b->pm);
-    for (int i = 0; i < 8; ++i)
-        if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    for (int k = 0; k < 2; ++k)
+        for (int i = 0; i < 8; ++i)
+            if (b->ev[k][i]) cudaEventDestroy(b->ev[k][i]);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return CUCO_OK;
@@ -674,13 +697,24 @@ cuco_status_t cuco_box_stream(cuco_box_t *b, void **stream) {
 
 cuco_status_t cuco_box_enable_timing(cuco_box_t *b, int enable) {
     if (!b) return CUCO_ERR_INVALID;
+    CUCO_TRY(read_pending(b));
     b->timing = enable != 0;
+    memset(b->acc_ms, 0, sizeof(b->acc_ms));
     return CUCO_OK;
 }
 
 cuco_status_t cuco_box_timings(cuco_box_t *b, float *ms) {
     if (!b || !ms) return CUCO_ERR_INVALID;
+    CUCO_TRY(read_pending(b));
     memcpy(ms, b->last_ms, sizeof(b->last_ms));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_phase_totals(cuco_box_t *b, float *ms, int reset) {
+    if (!b || !ms) return CUCO_ERR_INVALID;
+    CUCO_TRY(read_pending(b));
+    memcpy(ms, b->acc_ms, sizeof(b->acc_ms));
+    if (reset) memset(b->acc_ms, 0, sizeof(b->acc_ms));
     return CUCO_OK;
 }
 

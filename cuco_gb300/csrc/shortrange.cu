@@ -468,8 +468,42 @@ __device__ __forceinline__ void shortrange_segment(
 
     // The target's force from the sources of chunk [c0, c1), warp-reduced
     // (lane 0 holds it); FIXED: compensated, with the error terms in e*.
+    // A lane's partial force (FIXED: with its rounding errors), the unit of
+    // the warp reductions.
+    struct Part {
+        float x, y, z, ex, ey, ez;
+    };
+    auto xor_part = [&](const Part &q, int off) {
+        Part o;
+        o.x = __shfl_xor_sync(kFull, q.x, off);
+        o.y = __shfl_xor_sync(kFull, q.y, off);
+        o.z = __shfl_xor_sync(kFull, q.z, off);
+        if (FIXED) {
+            o.ex = __shfl_xor_sync(kFull, q.ex, off);
+            o.ey = __shfl_xor_sync(kFull, q.ey, off);
+            o.ez = __shfl_xor_sync(kFull, q.ez, off);
+        }
+        return o;
+    };
+    // q += o (FIXED: compensated, two-sum of the sums and the errors carried)
+    auto add_part = [&](Part &q, const Part &o) {
+        if (FIXED) {
+            float e;
+            two_sum(q.x, o.x, q.x, e);
+            q.ex = __fadd_rn(q.ex, __fadd_rn(o.ex, e));
+            two_sum(q.y, o.y, q.y, e);
+            q.ey = __fadd_rn(q.ey, __fadd_rn(o.ey, e));
+            two_sum(q.z, o.z, q.z, e);
+            q.ez = __fadd_rn(q.ez, __fadd_rn(o.ez, e));
+        } else {
+            q.x += o.x;
+            q.y += o.y;
+            q.z += o.z;
+        }
+    };
+
     auto target_chunk = [&](float4 pt, uint32_t c0, uint32_t c1, float &ax, float &ay, float &az, float &ex,
-                            float &ey, float &ez) {
+                            float &ey, float &ez, bool reduce) {
         float bx = 0.f, by = 0.f, bz = 0.f;
         ax = ay = az = 0.f;
         for (int cb = 0; cb < ncols; cb += 32) {
@@ -572,35 +606,23 @@ __device__ __forceinline__ void shortrange_segment(
             }
             __syncwarp();
         }
+        // the lane's two accumulator sets merged (FIXED: with the rounding
+        // error carried), then, when asked, the warp's sum
         ex = ey = ez = 0.f;
         if (FIXED) {
-            // compensated: two-sum of the lanes' partial sums, errors carried
             two_sum(ax, bx, ax, ex);
             two_sum(ay, by, ay, ey);
             two_sum(az, bz, az, ez);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                float e;
-                const float ox_ = __shfl_xor_sync(kFull, ax, off), oex = __shfl_xor_sync(kFull, ex, off);
-                two_sum(ax, ox_, ax, e);
-                ex = __fadd_rn(ex, __fadd_rn(oex, e));
-                const float oy_ = __shfl_xor_sync(kFull, ay, off), oey = __shfl_xor_sync(kFull, ey, off);
-                two_sum(ay, oy_, ay, e);
-                ey = __fadd_rn(ey, __fadd_rn(oey, e));
-                const float oz_ = __shfl_xor_sync(kFull, az, off), oez = __shfl_xor_sync(kFull, ez, off);
-                two_sum(az, oz_, az, e);
-                ez = __fadd_rn(ez, __fadd_rn(oez, e));
-            }
         } else {
             ax += bx;
             ay += by;
             az += bz;
+        }
+        if (reduce) {
+            Part q{ax, ay, az, ex, ey, ez};
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                ax += __shfl_xor_sync(kFull, ax, off);
-                ay += __shfl_xor_sync(kFull, ay, off);
-                az += __shfl_xor_sync(kFull, az, off);
-            }
+            for (int off = 16; off > 0; off >>= 1) add_part(q, xor_part(q, off));
+            ax = q.x, ay = q.y, az = q.z, ex = q.ex, ey = q.ey, ez = q.ez;
         }
     };
 
@@ -687,7 +709,7 @@ __device__ __forceinline__ void shortrange_segment(
             if (t >= nt) break;  // warp-uniform
             const float4 pt = load_target(s_tpos[t]);
             float ax, ay, az, ex, ey, ez;
-            target_chunk(pt, 0, total, ax, ay, az, ex, ey, ez);
+            target_chunk(pt, 0, total, ax, ay, az, ex, ey, ez, true);
             if (FIXED) {
                 ax = __fadd_rn(ax, ex);
                 ay = __fadd_rn(ay, ey);
@@ -716,7 +738,7 @@ __device__ __forceinline__ void shortrange_segment(
                 if (t >= nt) break;
                 const float4 pt = load_target(s_tpos[t]);
                 float ax, ay, az, ex, ey, ez;
-                target_chunk(pt, c0, c1, ax, ay, az, ex, ey, ez);
+                target_chunk(pt, c0, c1, ax, ay, az, ex, ey, ez, true);
                 if (lane == 0) {
                     // only this warp touches target t's accumulators
                     if (FIXED) {

@@ -188,6 +188,12 @@ class Box:
         check(self.lib.cuco_box_timings(self.h, ptr(ms)), "cuco_box_timings")
         return dict(zip(self.PHASES, ms.tolist()))
 
+    def phase_totals(self, reset: bool = True) -> dict:
+        """Per-phase device time summed over the timed steps since the last reset."""
+        ms = np.zeros(8, dtype=np.float32)
+        check(self.lib.cuco_box_phase_totals(self.h, ptr(ms), int(reset)), "cuco_box_phase_totals")
+        return dict(zip(self.PHASES, ms.tolist()))
+
     def launches(self) -> int:
         return int(self.lib.cuco_box_launches_per_step(self.h))
 

@@ -246,6 +246,10 @@ cuco_status_t cuco_box_stream(cuco_box_t *box, void **stream);
  * Only filled when phase timing is enabled. */
 cuco_status_t cuco_box_enable_timing(cuco_box_t *box, int enable);
 cuco_status_t cuco_box_timings(cuco_box_t *box, float *ms /* 8 */);
+/* Sums of the phase times since timing was enabled (or the last reset).  A
+ * timed step does not wait for itself, only for the step before, so a run of
+ * timed steps keeps the GPU busy; this call waits for the last one. */
+cuco_status_t cuco_box_phase_totals(cuco_box_t *box, float *ms /* 8 */, int reset);
 
 /* Copies of internal arrays for inspection (device -> host): keys and the
  * sort permutation in sorted order, cell bounds.  Any pointer may be NULL. */
