@@ -166,6 +166,308 @@ __device__ __forceinline__ void load_twiddles(float2 *tw_s, const float2 *tw, in
     for (int i = threadIdx.x; i < M; i += blockDim.x) tw_s[i] = tw[i];
 }
 
+// ------------------------------------------------ register transforms
+// Power-of-two meshes M = M1 * M2 (M1, M2 <= 32) take a two-level
+// Cooley-Tukey transform with the points in registers: one DFT over M1
+// points strided by M2, a twiddle, one shared-memory exchange, one DFT over
+// M2 contiguous points.  Each column is handled by max(M1, M2) threads and
+// visits shared memory twice instead of once per radix-4 stage.  The
+// forward transform leaves X[k] in slot M2 (k mod M1) + k / M1; the inverse
+// starts from that layout and ends in natural order, so a forward pass, a
+// multiply and an inverse pass (the x pass with the Green's function) need
+// no reordering in between.
+
+// cos and sin of 2 pi j / 32, j < 32
+__host__ __device__ constexpr float cos32(int j) {
+    constexpr float c[32] = {1.0f, 9.807852804e-01f, 9.238795325e-01f, 8.314696123e-01f, 7.071067812e-01f,
+                             5.555702330e-01f, 3.826834324e-01f, 1.950903220e-01f, 0.0f, -1.950903220e-01f,
+                             -3.826834324e-01f, -5.555702330e-01f, -7.071067812e-01f, -8.314696123e-01f,
+                             -9.238795325e-01f, -9.807852804e-01f, -1.0f, -9.807852804e-01f, -9.238795325e-01f,
+                             -8.314696123e-01f, -7.071067812e-01f, -5.555702330e-01f, -3.826834324e-01f,
+                             -1.950903220e-01f, 0.0f, 1.950903220e-01f, 3.826834324e-01f, 5.555702330e-01f,
+                             7.071067812e-01f, 8.314696123e-01f, 9.238795325e-01f, 9.807852804e-01f};
+    return c[j & 31];
+}
+__host__ __device__ constexpr float sin32(int j) { return cos32(j - 8); }
+
+// exp(S 2 pi i m / N) for N dividing 32
+template <int N, int S>
+__device__ __forceinline__ float2 wconst(int m) {
+    const int j = (m * (32 / N)) & 31;
+    return make_float2(cos32(j), S * sin32(j));
+}
+
+// In-register DFT of N = 2^a <= 32 points, X[k] = sum_n v[n] exp(S 2 pi i n k / N),
+// as radix-4 Cooley-Tukey (N = 4 Q: DFTs over n1 of v[Q n1 + n2], twiddle,
+// DFTs over n2; X[k1 + 4 k2]).  All indices are compile-time constants.
+template <int N, int S>
+__device__ __forceinline__ void dft_reg(float2 (&v)[N]) {
+    if constexpr (N == 2) {
+        const float2 a = v[0], b = v[1];
+        v[0] = make_float2(a.x + b.x, a.y + b.y);
+        v[1] = make_float2(a.x - b.x, a.y - b.y);
+    } else if constexpr (N == 4) {
+        dft_small<4>(v, S);
+    } else {
+        constexpr int Q = N / 4;
+        float2 w[N];
+#pragma unroll
+        for (int n2 = 0; n2 < Q; ++n2) {
+            float2 t[4] = {v[n2], v[n2 + Q], v[n2 + 2 * Q], v[n2 + 3 * Q]};
+            dft_small<4>(t, S);
+#pragma unroll
+            for (int k1 = 0; k1 < 4; ++k1) w[Q * k1 + n2] = (n2 * k1) ? cmul(t[k1], wconst<N, S>(n2 * k1)) : t[k1];
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) {
+            float2 u[Q];
+#pragma unroll
+            for (int j = 0; j < Q; ++j) u[j] = w[Q * k1 + j];
+            dft_reg<Q, S>(u);
+#pragma unroll
+            for (int k2 = 0; k2 < Q; ++k2) v[k1 + 4 * k2] = u[k2];
+        }
+    }
+}
+
+template <int M1, int M2>
+struct RegFFT {
+    static constexpr int M = M1 * M2, N1 = M1, N2 = M2;
+    static constexpr int T = M1 > M2 ? M1 : M2;  // threads per column
+    __device__ static int slot(int k) { return M2 * (k & (M1 - 1)) + k / M1; }
+    // twiddle exp(S 2 pi i j / M) from the table of exp(-2 pi i j / M)
+    template <int S>
+    __device__ static float2 tw(const float2 *tw_s, int j) {
+        float2 w = tw_s[j];
+        if (S > 0) w.y = -w.y;
+        return w;
+    }
+    // the 2^lb columns x[m * pitch + b]: natural order in, slot order out
+    template <int S>
+    __device__ static void forward(float2 *x, const float2 *tw_s, int pitch, int lb) {
+        const int b = threadIdx.x & ((1 << lb) - 1), r = threadIdx.x >> lb;
+        if (r < M2) {
+            const int n2 = r;
+            float2 v[M1];
+#pragma unroll
+            for (int n1 = 0; n1 < M1; ++n1) v[n1] = x[(M2 * n1 + n2) * pitch + b];
+            dft_reg<M1, S>(v);
+#pragma unroll
+            for (int k1 = 0; k1 < M1; ++k1)
+                x[(M2 * k1 + n2) * pitch + b] = k1 ? cmul(v[k1], tw<S>(tw_s, n2 * k1)) : v[k1];
+        }
+        __syncthreads();
+        if (r < M1) {
+            const int k1 = r;
+            float2 u[M2];
+#pragma unroll
+            for (int n2 = 0; n2 < M2; ++n2) u[n2] = x[(M2 * k1 + n2) * pitch + b];
+            dft_reg<M2, S>(u);
+#pragma unroll
+            for (int k2 = 0; k2 < M2; ++k2) x[(M2 * k1 + k2) * pitch + b] = u[k2];
+        }
+        __syncthreads();
+    }
+    // slot order in, natural order out
+    template <int S>
+    __device__ static void inverse(float2 *x, const float2 *tw_s, int pitch, int lb) {
+        const int b = threadIdx.x & ((1 << lb) - 1), r = threadIdx.x >> lb;
+        if (r < M1) {
+            const int k1 = r;
+            float2 u[M2];
+#pragma unroll
+            for (int k2 = 0; k2 < M2; ++k2) u[k2] = x[(M2 * k1 + k2) * pitch + b];
+            dft_reg<M2, S>(u);
+#pragma unroll
+            for (int n2 = 0; n2 < M2; ++n2)
+                x[(M2 * k1 + n2) * pitch + b] = k1 ? cmul(u[n2], tw<S>(tw_s, n2 * k1)) : u[n2];
+        }
+        __syncthreads();
+        if (r < M2) {
+            const int n2 = r;
+            float2 v[M1];
+#pragma unroll
+            for (int k1 = 0; k1 < M1; ++k1) v[k1] = x[(M2 * k1 + n2) * pitch + b];
+            dft_reg<M1, S>(v);
+#pragma unroll
+            for (int n1 = 0; n1 < M1; ++n1) x[(M2 * n1 + n2) * pitch + b] = v[n1];
+        }
+        __syncthreads();
+    }
+};
+
+// Whether M takes the register transforms with `cols` columns per CTA (the
+// one-box and many-box passes decide alike, so a box's transform is the same
+// in both).
+__host__ __device__ inline bool reg_fft_ok(int M, int cols) {
+    int T;
+    switch (M) {
+        case 16: T = 4; break;
+        case 32: T = 8; break;
+        case 64: T = 8; break;
+        case 128: T = 16; break;
+        case 256: T = 16; break;
+        default: return false;  // 512 and 1024 would need 32-point register DFTs: twice the registers
+    }
+    return T * cols <= kFFTThreads;
+}
+
+// The passes below with the register transforms (M = FT::M; one buffer of
+// M * pitch points, the twiddle table after it).
+template <typename FT>
+__device__ __forceinline__ void fft_z_r2c_reg(const unsigned long long *__restrict__ rho64, float mscale,
+                                              float2 *__restrict__ spec, const float2 *tw, int P, int blk) {
+    constexpr int M = FT::M, Mh = M / 2 + 1;
+    extern __shared__ float2 sm[];
+    const int pitch = P + 1;
+    float2 *x = sm, *tw_s = sm + M * pitch;
+    const size_t r0 = (size_t)blk * 2 * P;
+    load_twiddles(tw_s, tw, M);
+    for (int e0 = threadIdx.x; e0 < 2 * P * M; e0 += kLoadBatch * blockDim.x) {
+        float v[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = e0 + u * blockDim.x;
+            v[u] = e < 2 * P * M ? __fmul_rn(__ull2float_rn(rho64[r0 * M + e]), mscale) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < 2 * P * M) {
+                const int row = e / M, m = e & (M - 1);
+                reinterpret_cast<float *>(&x[m * pitch + (row >> 1)])[row & 1] = v[u];
+            }
+        }
+    }
+    __syncthreads();
+    FT::template forward<-1>(x, tw_s, pitch, ilog2(P));
+    for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) {
+        const int row = e / Mh, k = e - row * Mh, pr = row >> 1;
+        const float2 z = x[FT::slot(k) * pitch + pr];
+        float2 zc = x[FT::slot((M - k) & (M - 1)) * pitch + pr];
+        zc.y = -zc.y;
+        float2 o;
+        if ((row & 1) == 0)
+            o = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
+        else  // (z - zc) / (2i)
+            o = make_float2(0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x));
+        spec[(r0 + row) * Mh + k] = o;
+    }
+}
+
+template <typename FT>
+__device__ __forceinline__ void fft_z_c2r_reg(const float2 *__restrict__ spec, float *__restrict__ out,
+                                              const float2 *tw, int P, int blk) {
+    constexpr int M = FT::M, Mh = M / 2 + 1;
+    extern __shared__ float2 sm[];
+    const int pitch = P + 1;
+    float2 *x = sm, *tw_s = sm + M * pitch;
+    const size_t r0 = (size_t)blk * 2 * P;
+    load_twiddles(tw_s, tw, M);
+    // row pair pr packed as one complex column a + i b (a, b the Hermitian
+    // rows 2pr and 2pr+1, imaginary parts at k = 0 and M/2 dropped), placed
+    // in the slot order the inverse transform starts from
+    for (int e0 = threadIdx.x; e0 < P * M; e0 += kLoadBatch * blockDim.x) {
+        float2 va[kLoadBatch], vb[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = e0 + u * blockDim.x;
+            va[u] = vb[u] = make_float2(0.f, 0.f);
+            if (e < P * M) {
+                const int pr = e / M, k = e & (M - 1);
+                const int kk = k <= M / 2 ? k : M - k;
+                va[u] = spec[(r0 + 2 * pr) * Mh + kk];
+                vb[u] = spec[(r0 + 2 * pr + 1) * Mh + kk];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < P * M) {
+                const int pr = e / M, k = e & (M - 1);
+                float2 a = va[u], b = vb[u];
+                if (k == 0 || k == M / 2) a.y = b.y = 0.f;
+                if (k > M / 2) a.y = -a.y, b.y = -b.y;
+                x[FT::slot(k) * pitch + pr] = make_float2(a.x - b.y, a.y + b.x);  // a + i b
+            }
+        }
+    }
+    __syncthreads();
+    FT::template inverse<+1>(x, tw_s, pitch, ilog2(P));
+    for (int e = threadIdx.x; e < 2 * P * M; e += blockDim.x) {
+        const int row = e / M, m = e & (M - 1);
+        const float2 z = x[m * pitch + (row >> 1)];
+        out[(r0 + row) * M + m] = (row & 1) ? z.y : z.x;
+    }
+}
+
+template <typename FT>
+__device__ __forceinline__ void fft_axis_reg(float2 *__restrict__ spec, const float2 *tw,
+                                             const float *__restrict__ green1d, int B, int axis, int sign,
+                                             int green, int bx, int by) {
+    constexpr int M = FT::M, Mh = M / 2 + 1;
+    extern __shared__ float2 sm[];
+    const int pitch = B;
+    float2 *x = sm, *tw_s = sm + M * pitch;
+    const int o = by, kz0 = bx * B, bsh = ilog2(B), nb = min(B, Mh - kz0);
+    const size_t sm_stride = axis == 1 ? (size_t)Mh : (size_t)M * Mh;
+    const size_t base = axis == 1 ? (size_t)o * M * Mh : (size_t)o * Mh;
+    // an inverse-only pass starts from the slot order
+    const bool to_slots = sign > 0;
+    load_twiddles(tw_s, tw, M);
+    for (int e0 = threadIdx.x; e0 < M * B; e0 += kLoadBatch * blockDim.x) {
+        float2 v[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = e0 + u * blockDim.x;
+            const int m = e >> bsh, b = e & (B - 1);
+            v[u] = (e < M * B && b < nb) ? spec[base + m * sm_stride + kz0 + b] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = e0 + u * blockDim.x;
+            if (e < M * B) {
+                const int m = e >> bsh, b = e & (B - 1);
+                x[(to_slots ? FT::slot(m) : m) * pitch + b] = v[u];
+            }
+        }
+    }
+    __syncthreads();
+    bool natural = true;
+    if (sign < 0) {
+        FT::template forward<-1>(x, tw_s, pitch, bsh);
+        natural = false;
+        if (green) {
+            // slot s = M2 k1 + k2 holds X[k1 + M1 k2]
+            const int ky = o <= M / 2 ? o : M - o;
+            const float gy = green1d[ky];
+            for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
+                const int sl = e >> bsh, b = e & (B - 1);
+                const int k1 = sl / FT::N2, k2 = sl - k1 * FT::N2;
+                const int m = k1 + FT::N1 * k2;  // the transform index along x
+                const int kx = m <= M / 2 ? m : M - m;
+                const int kz = kz0 + b;
+                const float2 v = x[sl * pitch + b];
+                float g = 0.f;
+                if (b < nb) {
+                    const int k2s = kx * kx + ky * ky + kz * kz;
+                    if (k2s > 0) g = -green1d[kx] * gy * green1d[kz] / (float)k2s;
+                }
+                x[sl * pitch + b] = make_float2(v.x * g, v.y * g);
+            }
+            __syncthreads();
+            FT::template inverse<+1>(x, tw_s, pitch, bsh);
+            natural = true;
+        }
+    } else {
+        FT::template inverse<+1>(x, tw_s, pitch, bsh);
+    }
+    for (int e = threadIdx.x; e < M * B; e += blockDim.x) {
+        const int m = e >> bsh, b = e & (B - 1);
+        if (b < nb) spec[base + m * sm_stride + kz0 + b] = x[(natural ? m : FT::slot(m)) * pitch + b];
+    }
+}
+
 // rows r0 .. r0+2P-1 of the M^3 real grid (row = x*M + y) -> spectrum rows
 __device__ __forceinline__ void fft_z_r2c(const unsigned long long *__restrict__ rho64, float mscale,
                                           float2 *__restrict__ spec, const float2 *tw, int M, int P, int blk) {
@@ -340,19 +642,84 @@ __global__ void __launch_bounds__(kFFTThreads)
     fft_axis(spec, tw, green1d, M, B, axis, sign, green, blockIdx.x, blockIdx.y);
 }
 
+// One box, power-of-two mesh M = M1 * M2: the register transforms, one
+// instantiation per split (its registers sized for its DFT lengths).
+template <int M1, int M2>
+__global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
+    k_fft_z_r2c_r(const unsigned long long *__restrict__ rho64, float mscale, float2 *__restrict__ spec,
+                  const float2 *tw, int P) {
+    fft_z_r2c_reg<RegFFT<M1, M2>>(rho64, mscale, spec, tw, P, blockIdx.x);
+}
+
+template <int M1, int M2>
+__global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
+    k_fft_z_c2r_r(const float2 *__restrict__ spec, float *__restrict__ out, const float2 *tw, int P) {
+    fft_z_c2r_reg<RegFFT<M1, M2>>(spec, out, tw, P, blockIdx.x);
+}
+
+template <int M1, int M2>
+__global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
+    k_fft_axis_r(float2 *__restrict__ spec, const float2 *tw, const float *__restrict__ green1d, int B, int axis,
+                 int sign, int green) {
+    fft_axis_reg<RegFFT<M1, M2>>(spec, tw, green1d, B, axis, sign, green, blockIdx.x, blockIdx.y);
+}
+
+// The five transform passes of one box with the register transforms.
+template <int M1, int M2>
+cudaError_t fft_passes_reg(const PMPlan &plan, int P, int B, cudaStream_t stream) {
+    constexpr int M = M1 * M2, Mh = M / 2 + 1;
+    const size_t smz = sizeof(float2) * ((size_t)M * (P + 1) + M), sma = sizeof(float2) * ((size_t)M * B + M);
+    static bool attr = [&] {
+        cudaFuncSetAttribute(k_fft_z_r2c_r<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_fft_z_c2r_r<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        cudaFuncSetAttribute(k_fft_axis_r<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        return true;
+    }();
+    (void)attr;
+    const unsigned zblocks = (unsigned)((size_t)M * M / (2 * P));
+    k_fft_z_r2c_r<M1, M2><<<zblocks, kFFTThreads, smz, stream>>>(plan.rho64, ldexpf(plan.mass, -32), plan.spec,
+                                                                 plan.twiddle, P);
+    dim3 ag((Mh + B - 1) / B, M);
+    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, B, 1, -1, 0);
+    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, B, 0, -1, 1);
+    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, B, 1, +1, 0);
+    k_fft_z_c2r_r<M1, M2><<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, P);
+    return cudaGetLastError();
+}
+
 // Many boxes in one launch: map[blockIdx.x] = (box, the box's own block index).
 __global__ void __launch_bounds__(kFFTThreads)
     k_fft_z_r2c_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
-    fft_z_r2c(d.rho64, d.mscale, d.spec, d.twiddle, d.M, d.P, m.y);
+    if (reg_fft_ok(d.M, d.P)) {
+        switch (d.M) {
+            case 16: fft_z_r2c_reg<RegFFT<4, 4>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
+            case 32: fft_z_r2c_reg<RegFFT<4, 8>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
+            case 64: fft_z_r2c_reg<RegFFT<8, 8>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
+            case 128: fft_z_r2c_reg<RegFFT<8, 16>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
+            default: fft_z_r2c_reg<RegFFT<16, 16>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
+        }
+    } else {
+        fft_z_r2c(d.rho64, d.mscale, d.spec, d.twiddle, d.M, d.P, m.y);
+    }
 }
 
 __global__ void __launch_bounds__(kFFTThreads)
     k_fft_z_c2r_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
-    fft_z_c2r(d.spec, d.rho, d.twiddle, d.M, d.P, m.y);
+    if (reg_fft_ok(d.M, d.P)) {
+        switch (d.M) {
+            case 16: fft_z_c2r_reg<RegFFT<4, 4>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
+            case 32: fft_z_c2r_reg<RegFFT<4, 8>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
+            case 64: fft_z_c2r_reg<RegFFT<8, 8>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
+            case 128: fft_z_c2r_reg<RegFFT<8, 16>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
+            default: fft_z_c2r_reg<RegFFT<16, 16>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
+        }
+    } else {
+        fft_z_c2r(d.spec, d.rho, d.twiddle, d.M, d.P, m.y);
+    }
 }
 
 __global__ void __launch_bounds__(kFFTThreads)
@@ -361,7 +728,18 @@ __global__ void __launch_bounds__(kFFTThreads)
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
     const int nbx = (d.M / 2 + 1 + d.B - 1) / d.B;
-    fft_axis(d.spec, d.twiddle, d.green1d, d.M, d.B, axis, sign, green, m.y % nbx, m.y / nbx);
+    const int bx = m.y % nbx, by = m.y / nbx;
+    if (reg_fft_ok(d.M, d.B)) {
+        switch (d.M) {
+            case 16: fft_axis_reg<RegFFT<4, 4>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
+            case 32: fft_axis_reg<RegFFT<4, 8>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
+            case 64: fft_axis_reg<RegFFT<8, 8>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
+            case 128: fft_axis_reg<RegFFT<8, 16>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
+            default: fft_axis_reg<RegFFT<16, 16>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
+        }
+    } else {
+        fft_axis(d.spec, d.twiddle, d.green1d, d.M, d.B, axis, sign, green, bx, by);
+    }
 }
 
 __device__ __forceinline__ void cic_axis(float to_slab_fac, float p, int M, int *s, int *ss,
@@ -660,15 +1038,27 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
     }
     CUCO_TRY_CUDA(cudaGetLastError());
     if (ev_deposit_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_deposit_done, stream));
-    const unsigned zblocks = (unsigned)((size_t)M * M / (2 * P));
-    k_fft_z_r2c<<<zblocks, kFFTThreads, smz, stream>>>(plan.rho64, ldexpf(plan.mass, -32), plan.spec,
-                                                       plan.twiddle, M, P);
-    dim3 ag((Mh + B - 1) / B, M);
-    k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, -1, 0);
-    k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 0, -1, 1);
-    k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, +1, 0);
-    k_fft_z_c2r<<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, M, P);
-    CUCO_TRY_CUDA(cudaGetLastError());
+    if (reg_fft_ok(M, P) && reg_fft_ok(M, B)) {
+        cudaError_t e;
+        switch (M) {
+            case 16: e = fft_passes_reg<4, 4>(plan, P, B, stream); break;
+            case 32: e = fft_passes_reg<4, 8>(plan, P, B, stream); break;
+            case 64: e = fft_passes_reg<8, 8>(plan, P, B, stream); break;
+            case 128: e = fft_passes_reg<8, 16>(plan, P, B, stream); break;
+            default: e = fft_passes_reg<16, 16>(plan, P, B, stream); break;
+        }
+        CUCO_TRY_CUDA(e);
+    } else {
+        const unsigned zblocks = (unsigned)((size_t)M * M / (2 * P));
+        k_fft_z_r2c<<<zblocks, kFFTThreads, smz, stream>>>(plan.rho64, ldexpf(plan.mass, -32), plan.spec,
+                                                           plan.twiddle, M, P);
+        dim3 ag((Mh + B - 1) / B, M);
+        k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, -1, 0);
+        k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 0, -1, 1);
+        k_fft_axis<<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, M, B, 1, +1, 0);
+        k_fft_z_c2r<<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, M, P);
+        CUCO_TRY_CUDA(cudaGetLastError());
+    }
     if (ev_fft_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_fft_done, stream));
     if (n) {
         if (plan.fixed)
