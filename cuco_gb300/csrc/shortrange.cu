@@ -147,6 +147,15 @@ __device__ __forceinline__ uint32_t bit_at(uint32_t k) {
     return b;
 }
 
+// The hardware reciprocal square root, flushing subnormal inputs (the fast
+// path only sees r^2 well above them; without the flush the compiler wraps
+// the instruction in a subnormal rescale).
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // r^2 with a fixed operation order: the candidate test and the force pass
 // must agree on it bit for bit.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
@@ -411,7 +420,7 @@ __device__ __forceinline__ void shortrange_segment(
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
         // r2 = 0 gives rinv = inf and r = NaN: not fast (r2 < hmin2), not flagged
-        const float rinv = rsqrtf(r2);
+        const float rinv = rsqrt_ftz(r2);
         const float r = r2 * rinv;
         const float xl = __fmaf_rz(r, p.alo, 8388608.0f);
         const bool edge = !FIXED && xl != __fmaf_rz(r, p.ahi, 8388608.0f);
@@ -521,7 +530,7 @@ __device__ __forceinline__ void shortrange_segment(
                     // half-height of the cut disc over this column (an
                     // approximate square root: the margin covers it), in
                     // cells from the column's first z-cell
-                    const float hz = __fmul_rn(q, rsqrtf(fmaxf(q, 1e-30f)));
+                    const float hz = __fmul_rn(q, rsqrt_ftz(fmaxf(q, 1e-30f)));
                     const float ul = __fmaf_rn(pt.z - hz, winv, -zbase), uh = __fmaf_rn(pt.z + hz, winv, -zbase);
                     const int fl = __float2int_rd(ul), fh = __float2int_rd(uh);
                     const int zlo = max(fl, 0), zhi = min(fh, nz - 1);
