@@ -209,7 +209,12 @@ struct PMMulti {
     size_t smz, sma;          // dynamic shared memory of the z and axis passes
     unsigned long long *rho64_all;  // all boxes' deposit grids, contiguous (one memset)
     size_t rho_all_count;
+    bool big;  // some box's transforms need the large register kernels (pm_big_fft)
 };
+// Whether a box of mesh M with transform batches P, B takes the large (32-point)
+// register transforms, which run in kernels of their own.
+bool pm_big_fft(int M, int P, int B);
+bool pm_fft_batches_ok(int M, int P, int B);
 int pm_batch_z(int M);
 int pm_batch_axis(int M);
 size_t pm_smem_z(int M, int P);

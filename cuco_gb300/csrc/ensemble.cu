@@ -235,7 +235,7 @@ void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out
         for (int P : {1, 2, 4, 8, 16}) {
             if (P > M / 2 || (M * M / 2) % P || pm_smem_z(M, P) > 200 * 1024) continue;
             for (int B : {4, 8, 16}) {
-                if (pm_smem_axis(M, B) > 200 * 1024) continue;
+                if (pm_smem_axis(M, B) > 200 * 1024 || !pm_fft_batches_ok(M, P, B)) continue;
                 PMBoxDesc d{M, P, B, 1.f, 0.f, 0.f, rho, rho64, 1.f, spec, green, tw};
                 cudaMemcpy(dd, &d, sizeof d, cudaMemcpyHostToDevice);
                 const uint32_t nz = (uint32_t)(M * M / (2 * P)), nbx = (uint32_t)((Mh + B - 1) / B),
@@ -247,6 +247,7 @@ void tune_fft(int M, float boxsize, float asmth, cudaStream_t stream, int *P_out
                 cudaMemcpy(ma, va.data(), sizeof(uint2) * na, cudaMemcpyHostToDevice);
                 PMMulti m{1, false, dd, pbeg, mz, ma, nz, na, pm_smem_z(M, P), pm_smem_axis(M, B), rho64,
                           (size_t)M * M * M};
+                m.big = pm_big_fft(M, P, B);
                 if (pm_forces_multi(m, nullptr, 0, nullptr, stream, nullptr) != CUCO_OK) continue;  // warm-up
                 cudaEventRecord(e0, stream);
                 for (int r = 0; r < 3; ++r) pm_forces_multi(m, nullptr, 0, nullptr, stream, nullptr);
@@ -621,6 +622,7 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
     e->sr_smem = sr_smem;
     e->pm = PMMulti{nbox, e->fixed, e->d_pm, e->d_pbeg, e->d_mapz, e->d_mapa, (uint32_t)mapz.size(),
                     (uint32_t)mapa.size(), smz, sma, e->rho64, (size_t)mbase[nbox]};
+    for (int b = 0; b < nbox; ++b) e->pm.big = e->pm.big || pm_big_fft(cfg[b].pm_grid, P[b], B[b]);
     e->has_state = e->has_state || carry != nullptr;
     return CUCO_OK;
 }

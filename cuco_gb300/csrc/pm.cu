@@ -298,7 +298,8 @@ struct RegFFT {
 
 // Whether M takes the register transforms with `cols` columns per CTA (the
 // one-box and many-box passes decide alike, so a box's transform is the same
-// in both).
+// in both).  512 and 1024 use 32-point register DFTs, which need twice the
+// registers: the many-box passes run those boxes in kernels of their own.
 __host__ __device__ inline bool reg_fft_ok(int M, int cols) {
     int T;
     switch (M) {
@@ -307,7 +308,9 @@ __host__ __device__ inline bool reg_fft_ok(int M, int cols) {
         case 64: T = 8; break;
         case 128: T = 16; break;
         case 256: T = 16; break;
-        default: return false;  // 512 and 1024 would need 32-point register DFTs: twice the registers
+        case 512: T = 32; break;
+        case 1024: T = 32; break;
+        default: return false;
     }
     return T * cols <= kFFTThreads;
 }
@@ -687,12 +690,25 @@ cudaError_t fft_passes_reg(const PMPlan &plan, int P, int B, cudaStream_t stream
     return cudaGetLastError();
 }
 
-// Many boxes in one launch: map[blockIdx.x] = (box, the box's own block index).
-__global__ void __launch_bounds__(kFFTThreads)
+// Many boxes in one launch: map[blockIdx.x] = (box, the box's own block
+// index).  BIG: only the boxes with 32-point register transforms (meshes 512
+// and 1024), every other block returns; !BIG: every other box.
+__device__ __forceinline__ bool big_box(const PMBoxDesc &d, int cols) {
+    return d.M >= 512 && reg_fft_ok(d.M, cols);
+}
+
+template <bool BIG>
+__global__ void __launch_bounds__(kFFTThreads, BIG ? 2 : 3)
     k_fft_z_r2c_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
-    if (reg_fft_ok(d.M, d.P)) {
+    if (big_box(d, d.P) != BIG) return;
+    if (BIG) {
+        if (d.M == 512)
+            fft_z_r2c_reg<RegFFT<16, 32>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y);
+        else
+            fft_z_r2c_reg<RegFFT<32, 32>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y);
+    } else if (reg_fft_ok(d.M, d.P)) {
         switch (d.M) {
             case 16: fft_z_r2c_reg<RegFFT<4, 4>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
             case 32: fft_z_r2c_reg<RegFFT<4, 8>>(d.rho64, d.mscale, d.spec, d.twiddle, d.P, m.y); break;
@@ -705,11 +721,18 @@ __global__ void __launch_bounds__(kFFTThreads)
     }
 }
 
-__global__ void __launch_bounds__(kFFTThreads)
+template <bool BIG>
+__global__ void __launch_bounds__(kFFTThreads, BIG ? 2 : 3)
     k_fft_z_c2r_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map) {
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
-    if (reg_fft_ok(d.M, d.P)) {
+    if (big_box(d, d.P) != BIG) return;
+    if (BIG) {
+        if (d.M == 512)
+            fft_z_c2r_reg<RegFFT<16, 32>>(d.spec, d.rho, d.twiddle, d.P, m.y);
+        else
+            fft_z_c2r_reg<RegFFT<32, 32>>(d.spec, d.rho, d.twiddle, d.P, m.y);
+    } else if (reg_fft_ok(d.M, d.P)) {
         switch (d.M) {
             case 16: fft_z_c2r_reg<RegFFT<4, 4>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
             case 32: fft_z_c2r_reg<RegFFT<4, 8>>(d.spec, d.rho, d.twiddle, d.P, m.y); break;
@@ -722,14 +745,21 @@ __global__ void __launch_bounds__(kFFTThreads)
     }
 }
 
-__global__ void __launch_bounds__(kFFTThreads)
+template <bool BIG>
+__global__ void __launch_bounds__(kFFTThreads, BIG ? 2 : 3)
     k_fft_axis_multi(const PMBoxDesc *__restrict__ boxes, const uint2 *__restrict__ map, int axis, int sign,
                      int green) {
     const uint2 m = map[blockIdx.x];
     const PMBoxDesc &d = boxes[m.x];
+    if (big_box(d, d.B) != BIG) return;
     const int nbx = (d.M / 2 + 1 + d.B - 1) / d.B;
     const int bx = m.y % nbx, by = m.y / nbx;
-    if (reg_fft_ok(d.M, d.B)) {
+    if (BIG) {
+        if (d.M == 512)
+            fft_axis_reg<RegFFT<16, 32>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by);
+        else
+            fft_axis_reg<RegFFT<32, 32>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by);
+    } else if (reg_fft_ok(d.M, d.B)) {
         switch (d.M) {
             case 16: fft_axis_reg<RegFFT<4, 4>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
             case 32: fft_axis_reg<RegFFT<4, 8>>(d.spec, d.twiddle, d.green1d, d.B, axis, sign, green, bx, by); break;
@@ -896,6 +926,15 @@ int fft_batch_axis(int M) {
 
 }  // namespace
 
+bool pm_big_fft(int M, int P, int B) { return M >= 512 && reg_fft_ok(M, P) && reg_fft_ok(M, B); }
+
+// A power-of-two mesh must take the register transforms in every pass (as one
+// box does): its batches may not exceed what they hold.
+bool pm_fft_batches_ok(int M, int P, int B) {
+    const bool pow2 = M >= 16 && M <= 1024 && (M & (M - 1)) == 0;
+    return !pow2 || (reg_fft_ok(M, P) && reg_fft_ok(M, B));
+}
+
 int pm_batch_z(int M) { return fft_batch_z(M); }
 int pm_batch_axis(int M) { return fft_batch_axis(M); }
 
@@ -929,9 +968,14 @@ cuco_status_t pm_forces_multi(const PMMulti &m, const float4 *pos, uint32_t n, f
                               cudaStream_t stream, int *launches) {
     static bool attr = [] {
         const int mx = 227 * 1024;
-        cudaFuncSetAttribute(k_fft_z_r2c_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-        cudaFuncSetAttribute(k_fft_z_c2r_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-        cudaFuncSetAttribute(k_fft_axis_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        for (bool big : {false, true}) {
+            cudaFuncSetAttribute(big ? k_fft_z_r2c_multi<true> : k_fft_z_r2c_multi<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+            cudaFuncSetAttribute(big ? k_fft_z_c2r_multi<true> : k_fft_z_c2r_multi<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+            cudaFuncSetAttribute(big ? k_fft_axis_multi<true> : k_fft_axis_multi<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+        }
         return true;
     }();
     (void)attr;
@@ -942,11 +986,20 @@ cuco_status_t pm_forces_multi(const PMMulti &m, const float4 *pos, uint32_t n, f
         else
             k_deposit_multi<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox);
     }
-    k_fft_z_r2c_multi<<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
-    k_fft_axis_multi<<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, 1, -1, 0);
-    k_fft_axis_multi<<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, 0, -1, 1);
-    k_fft_axis_multi<<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, 1, +1, 0);
-    k_fft_z_c2r_multi<<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
+    // each pass: the boxes of the common kernels, then (when the ensemble has
+    // any) the boxes of the large register transforms
+    k_fft_z_r2c_multi<false><<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
+    if (m.big) k_fft_z_r2c_multi<true><<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
+    for (int pass = 0; pass < 3; ++pass) {
+        const int axis = pass == 1 ? 0 : 1, sign = pass == 2 ? +1 : -1, green = pass == 1;
+        k_fft_axis_multi<false><<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, axis, sign,
+                                                                                green);
+        if (m.big)
+            k_fft_axis_multi<true><<<m.naxis_blocks, kFFTThreads, m.sma, stream>>>(m.boxes, m.map_axis, axis, sign,
+                                                                                   green);
+    }
+    k_fft_z_c2r_multi<false><<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
+    if (m.big) k_fft_z_c2r_multi<true><<<m.nz_blocks, kFFTThreads, m.smz, stream>>>(m.boxes, m.map_z);
     if (n) {
         if (m.fixed)
             k_interp_multi<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox, acc);
@@ -954,7 +1007,7 @@ cuco_status_t pm_forces_multi(const PMMulti &m, const float4 *pos, uint32_t n, f
             k_interp_multi<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, m.boxes, m.pbeg, m.nbox, acc);
     }
     CUCO_TRY_CUDA(cudaGetLastError());
-    if (launches) *launches += 7;
+    if (launches) *launches += m.big ? 12 : 7;
     return CUCO_OK;
 }
 
@@ -1045,7 +1098,9 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
             case 32: e = fft_passes_reg<4, 8>(plan, P, B, stream); break;
             case 64: e = fft_passes_reg<8, 8>(plan, P, B, stream); break;
             case 128: e = fft_passes_reg<8, 16>(plan, P, B, stream); break;
-            default: e = fft_passes_reg<16, 16>(plan, P, B, stream); break;
+            case 256: e = fft_passes_reg<16, 16>(plan, P, B, stream); break;
+            case 512: e = fft_passes_reg<16, 32>(plan, P, B, stream); break;
+            default: e = fft_passes_reg<32, 32>(plan, P, B, stream); break;
         }
         CUCO_TRY_CUDA(e);
     } else {

@@ -88,6 +88,42 @@ def test_single_box_mixed_radix_pm_vs_oracle(port):
         assert rms_rel(apm, port.pm(ic.pos, p, M, 8)) < 1e-4
 
 
+@pytest.mark.parametrize("M", [64, 256, 512])
+def test_single_box_register_fft_pm_vs_oracle(port, M):
+    """Power-of-two meshes take the register transforms (16- and 32-point
+    DFTs at M = 512)."""
+    ic = ics.zeldovich(24, 80.0, 49.0, 10)
+    box = Box(BoxConfig(n=ic.n, pm_grid=M, boxsize=ic.boxsize, mass=ic.mass, G=ics.G_INTERNAL,
+                        softening=soft(80.0, 24), cell_grid=max(8, M // 8)))
+    box.set_state(ic.pos)
+    box.forces(pm=True, pp=False)
+    apm = box.get_state()[3]
+    box.close()
+    p = oracle.reference_params(ic.boxsize, ic.mass, ics.G_INTERNAL, M, soft(80.0, 24))
+    e = rms_rel(apm, port.pm(ic.pos, p, M, 16))
+    print(f"M={M}: pm {e:.2e}")
+    assert e < 1e-4
+
+
+def test_ensemble_large_mesh_matches_single_box():
+    """A 512 mesh runs in the ensemble's own large-transform kernels; the box
+    still gets exactly what it gets alone."""
+    ics_, cfgs = make([(24, 512, 80.0, 11), (16, 32, 60.0, 1)], MODE_FIXED)
+    ens = Ensemble(cfgs)
+    for b, ic in enumerate(ics_):
+        ens.set_state(b, ic.pos)
+    ens.forces()
+    for b, (ic, c) in enumerate(zip(ics_, cfgs)):
+        _, _, _, apm = ens.get_state(b)
+        box = Box(BoxConfig(**{**c.__dict__, "cell_grid": ens.plan(b)[0]}))
+        box.set_state(ic.pos)
+        box.forces()
+        apm1 = box.get_state()[3]
+        box.close()
+        assert np.array_equal(apm, apm1), f"box {b}: PM differs from the box alone"
+    ens.close()
+
+
 def test_ensemble_graph_steps_track_single_boxes():
     ics_, cfgs = make(SPECS, MODE_FIXED)
     ens = Ensemble(cfgs)
