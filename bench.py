@@ -288,6 +288,12 @@ def run_serving(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_shortrange launch at
+# z = 49 (ncu --set full, the first timed step of
+# `bench.py --steps 2 --warmup 3 --e2e-steps 0 --no-cpu`)
+SR_TRAFFIC = {"plain-128^3-L256-M256-G64-z49to0-200steps": 172.3e6}
+
+
 def apply_preset(name):
     global N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD
     N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD = PRESETS[name]
@@ -526,7 +532,9 @@ def run_gpu_arm(args, world, rank, local):
         "config": workload_config(),
         "roofline": {"bound": "fp32", "kernel": "k_shortrange", "achieved": achieved,
                      "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
-                     "traffic": None,
+                     "traffic": SR_TRAFFIC.get(WORKLOAD),
+                     "traffic_note": "DRAM bytes read + written by one short-range launch at z = 49, from an ncu "
+                                     "capture of this workload (not measured by this run)",
                      "convention": "20 FP32 flops per in-range pair (pairs counted in-kernel in an untimed replay "
                                    "of the same steps), "
                                    "peak = measured FMA throughput"},
