@@ -477,40 +477,6 @@ __device__ __forceinline__ void shortrange_segment(
 
     // The target's force from the sources of chunk [c0, c1), warp-reduced
     // (lane 0 holds it); FIXED: compensated, with the error terms in e*.
-    // A lane's partial force (FIXED: with its rounding errors), the unit of
-    // the warp reductions.
-    struct Part {
-        float x, y, z, ex, ey, ez;
-    };
-    auto xor_part = [&](const Part &q, int off) {
-        Part o;
-        o.x = __shfl_xor_sync(kFull, q.x, off);
-        o.y = __shfl_xor_sync(kFull, q.y, off);
-        o.z = __shfl_xor_sync(kFull, q.z, off);
-        if (FIXED) {
-            o.ex = __shfl_xor_sync(kFull, q.ex, off);
-            o.ey = __shfl_xor_sync(kFull, q.ey, off);
-            o.ez = __shfl_xor_sync(kFull, q.ez, off);
-        }
-        return o;
-    };
-    // q += o (FIXED: compensated, two-sum of the sums and the errors carried)
-    auto add_part = [&](Part &q, const Part &o) {
-        if (FIXED) {
-            float e;
-            two_sum(q.x, o.x, q.x, e);
-            q.ex = __fadd_rn(q.ex, __fadd_rn(o.ex, e));
-            two_sum(q.y, o.y, q.y, e);
-            q.ey = __fadd_rn(q.ey, __fadd_rn(o.ey, e));
-            two_sum(q.z, o.z, q.z, e);
-            q.ez = __fadd_rn(q.ez, __fadd_rn(o.ez, e));
-        } else {
-            q.x += o.x;
-            q.y += o.y;
-            q.z += o.z;
-        }
-    };
-
     auto target_chunk = [&](float4 pt, uint32_t c0, uint32_t c1, float &ax, float &ay, float &az, float &ex,
                             float &ey, float &ez, bool reduce) {
         float bx = 0.f, by = 0.f, bz = 0.f;
@@ -615,23 +581,51 @@ __device__ __forceinline__ void shortrange_segment(
             }
             __syncwarp();
         }
-        // the lane's two accumulator sets merged (FIXED: with the rounding
-        // error carried), then, when asked, the warp's sum
+        // the warp's sum of the lanes' two accumulator sets
         ex = ey = ez = 0.f;
         if (FIXED) {
-            two_sum(ax, bx, ax, ex);
-            two_sum(ay, by, ay, ey);
-            two_sum(az, bz, az, ez);
+            // Compensated by error-free splitting: with V a power of two above
+            // every lane's partial sums, each is split against the quantum
+            // q = V / 2^17 into a multiple of q (h = (v + C) - C, C = 1.5 *
+            // 2^23 q) and an exact remainder l = v - h (|l| <= q/2).  The 64
+            // multiples of q add exactly in any order (|sum| <= 64 V = 2^23 q);
+            // the remainders add in float, their error far below q.  The
+            // result is the pair (sum of the h, sum of the l).
+            const float m = fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))),
+                                  fmaxf(fabsf(az), fabsf(bz)));
+            const uint32_t eb = __reduce_max_sync(kFull, __float_as_uint(m) >> 23);  // V = 2^(eb - 126)
+            const float C = __uint_as_float(((eb + 7u) << 23) | 0x400000u);      // 1.5 * 2^6 V
+            auto split2 = [&](float a, float b, float &h, float &l) {
+                const float ha = __fsub_rn(__fadd_rn(a, C), C), hb = __fsub_rn(__fadd_rn(b, C), C);
+                h = __fadd_rn(ha, hb);
+                l = __fadd_rn(__fsub_rn(a, ha), __fsub_rn(b, hb));
+            };
+            split2(ax, bx, ax, ex);
+            split2(ay, by, ay, ey);
+            split2(az, bz, az, ez);
         } else {
             ax += bx;
             ay += by;
             az += bz;
         }
         if (reduce) {
-            Part q{ax, ay, az, ex, ey, ez};
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) add_part(q, xor_part(q, off));
-            ax = q.x, ay = q.y, az = q.z, ex = q.ex, ey = q.ey, ez = q.ez;
+            for (int off = 16; off > 0; off >>= 1) {
+                ax = __fadd_rn(ax, __shfl_xor_sync(kFull, ax, off));
+                ay = __fadd_rn(ay, __shfl_xor_sync(kFull, ay, off));
+                az = __fadd_rn(az, __shfl_xor_sync(kFull, az, off));
+                if (FIXED) {
+                    ex = __fadd_rn(ex, __shfl_xor_sync(kFull, ex, off));
+                    ey = __fadd_rn(ey, __shfl_xor_sync(kFull, ey, off));
+                    ez = __fadd_rn(ez, __shfl_xor_sync(kFull, ez, off));
+                }
+            }
+            if (FIXED) {
+                // (sum, error) as a normalised pair for the callers
+                two_sum(ax, ex, ax, ex);
+                two_sum(ay, ey, ay, ey);
+                two_sum(az, ez, az, ez);
+            }
         }
     };
 
