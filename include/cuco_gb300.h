@@ -231,8 +231,8 @@ cuco_status_t cuco_box_forces(cuco_box_t *box, int pm, int pp);
  * The factors are cosmological integrals (cuco_cosmo_factors). */
 cuco_status_t cuco_box_step(cuco_box_t *box, double drift, double kick_pp, double kick_pm);
 
-/* Run `nsteps` steps with per-step factors (arrays of nsteps), recorded once as
- * a CUDA graph and replayed. */
+/* Run `nsteps` steps with per-step factors (arrays of nsteps), enqueued
+ * back to back on the box's stream. */
 cuco_status_t cuco_box_run(cuco_box_t *box, int nsteps, const double *drift,
                            const double *kick_pp, const double *kick_pm);
 
