@@ -7,13 +7,14 @@
 // The sort is a three-kernel-per-pass LSD radix sort designed for sm_103a:
 //   1. k_sort_hist:   per 4096-key tile, a digit histogram (warp match_any
 //                     aggregation into shared-memory counters);
-//   2. k_sort_scan:   one CTA turns the [digit][tile] histogram into global
-//                     scatter offsets (coalesced warp scans per digit);
+//   2. k_sort_scan:   one CTA per digit turns its tile counts into inclusive
+//                     prefixes over the tiles (the digit's total is the last);
 //   3. k_sort_scatter: each tile ranks its keys stably with warp ballots
 //                     (the lanes sharing a digit are found from RB ballots, the
-//                     rank is a popcount below the lane), stages the tile in
-//                     digit order in shared memory and writes out digit runs
-//                     with coalesced stores.
+//                     rank is a popcount below the lane), takes each run's
+//                     global offset from the digit totals and its own
+//                     prefix, stages the tile in digit order in shared memory
+//                     and writes out digit runs with coalesced stores.
 // Digits are 4..8 bits; a pass count of ceil(bits/8) with equal digit widths
 // is used (18-bit keys: three 6-bit passes).
 #include "common.cuh"
@@ -69,72 +70,41 @@ __global__ void __launch_bounds__(kSortThreads)
     for (int d = threadIdx.x; d < RADIX; d += kSortThreads) hist[d * tiles + tile] = h[d];
 }
 
-// hist[d*tiles + t] (count of digit d in tile t) -> global offset of that run.
-template <int RB>
-__global__ void __launch_bounds__(1024) k_sort_scan(uint32_t *__restrict__ hist, uint32_t tiles) {
-    constexpr int RADIX = 1 << RB;
-    __shared__ uint32_t total[RADIX];
+// hist[d*tiles + t] (count of digit d in tile t) -> the inclusive prefix of
+// those counts over the tiles, one CTA per digit.  A digit's total is then its
+// last entry, and the scatter derives every run's global offset from these
+// (no second pass over the table, no scratch beyond it).
+__global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__restrict__ hist, uint32_t tiles) {
+    __shared__ uint32_t wsum[kSortWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // Warp per digit, 32 consecutive tiles per round with 8 rounds of
-    // coalesced loads in flight, then 8 warp scans chained by the carry.
-    for (int d = warp; d < RADIX; d += 32) {
-        uint32_t *h = hist + (size_t)d * tiles;
-        uint32_t carry = 0;
-        for (uint32_t t0 = 0; t0 < tiles; t0 += 32 * 8) {
-            uint32_t v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const uint32_t t = t0 + u * 32 + lane;
-                v[u] = t < tiles ? h[t] : 0u;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                uint32_t incl = v[u];
-#pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    uint32_t y = __shfl_up_sync(kFull, incl, off);
-                    if (lane >= off) incl += y;
-                }
-                const uint32_t t = t0 + u * 32 + lane;
-                if (t < tiles) h[t] = carry + incl - v[u];
-                carry += __shfl_sync(kFull, incl, 31);
-            }
-        }
-        if (lane == 0) total[d] = carry;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        constexpr int PER = (RADIX + 31) / 32;
-        uint32_t v[PER], s = 0;
-#pragma unroll
-        for (int j = 0; j < PER; ++j) {
-            int d = lane * PER + j;
-            v[j] = d < RADIX ? total[d] : 0;
-            s += v[j];
-        }
-        uint32_t incl = s;
+    uint32_t *h = hist + (size_t)blockIdx.x * tiles;
+    uint32_t carry = 0;
+    for (uint32_t t0 = 0; t0 < tiles; t0 += kSortThreads) {
+        const uint32_t t = t0 + threadIdx.x;
+        const uint32_t v = t < tiles ? h[t] : 0u;
+        uint32_t incl = v;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            uint32_t y = __shfl_up_sync(kFull, incl, off);
+            const uint32_t y = __shfl_up_sync(kFull, incl, off);
             if (lane >= off) incl += y;
         }
-        uint32_t run = incl - s;
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, all = 0;
 #pragma unroll
-        for (int j = 0; j < PER; ++j) {
-            int d = lane * PER + j;
-            if (d < RADIX) {
-                total[d] = run;
-                run += v[j];
-            }
+        for (int w = 0; w < kSortWarps; ++w) {
+            const uint32_t x = wsum[w];
+            before += w < warp ? x : 0u;
+            all += x;
         }
+        if (t < tiles) h[t] = carry + before + incl;
+        carry += all;
+        __syncthreads();  // wsum is rewritten by the next round
     }
-    __syncthreads();
-    const uint32_t entries = (uint32_t)RADIX * tiles;
-    for (uint32_t e = threadIdx.x; e < entries; e += blockDim.x) hist[e] += total[e / tiles];
 }
 
 template <int RB, bool WITH_VALS, bool SINGLE_TILE>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, 4)
     k_sort_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                    uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint32_t n,
                    int shift, const uint32_t *__restrict__ hist, uint32_t tiles) {
@@ -152,25 +122,30 @@ __global__ void __launch_bounds__(kSortThreads)
     for (int e = threadIdx.x; e < kSortWarps * RADIX; e += kSortThreads) (&wcnt[0][0])[e] = 0;
     __syncthreads();
 
-    uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
     // Warp w owns tile elements [w*512, w*512+512); item k covers 32 of them in
     // lane order, so (k, lane) order is input order and the ranks are stable.
+    // The ranks (below 4096) are kept two to a register; keys and values are
+    // read again when they are placed, so few registers stay live.
+    uint32_t rank2[kSortItems / 2];
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
-        uint32_t i = base + warp * (32 * kSortItems) + k * 32 + lane;
-        bool valid = i < n;
-        key[k] = valid ? kin[i] : 0xffffffffu;
-        if (WITH_VALS) val[k] = valid ? (vin ? vin[i] : i) : 0u;
-        uint32_t d = (key[k] >> shift) & (RADIX - 1);
+        const uint32_t i = base + warp * (32 * kSortItems) + k * 32 + lane;
+        const bool valid = i < n;
+        const uint32_t key = valid ? kin[i] : 0xffffffffu;
+        const uint32_t d = (key >> shift) & (RADIX - 1);
         uint32_t peers = __ballot_sync(kFull, valid);
 #pragma unroll
         for (int b = 0; b < RB; ++b) {
-            uint32_t bit = (d >> b) & 1u;
-            uint32_t m = __ballot_sync(kFull, bit);
+            const uint32_t bit = (d >> b) & 1u;
+            const uint32_t m = __ballot_sync(kFull, bit);
             peers &= bit ? m : ~m;
         }
-        uint32_t cnt = wcnt[warp][d];
-        rank[k] = cnt + __popc(peers & lt);
+        const uint32_t cnt = wcnt[warp][d];
+        const uint32_t r = cnt + __popc(peers & lt);
+        if (k & 1)
+            rank2[k >> 1] |= r << 16;
+        else
+            rank2[k >> 1] = r;
         __syncwarp();
         if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = cnt + __popc(peers);
         __syncwarp();
@@ -188,50 +163,56 @@ __global__ void __launch_bounds__(kSortThreads)
     }
     __syncthreads();
     if (warp == 0) {
+        // exclusive scan of this tile's digit counts; and, over the digits,
+        // of the digit totals (the last tile's inclusive prefixes)
         constexpr int PER = (RADIX + 31) / 32;
-        uint32_t v[PER], s = 0;
+        uint32_t v[PER], tv[PER], s = 0, ts = 0;
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
-            int d = lane * PER + j;
+            const int d = lane * PER + j;
             v[j] = d < RADIX ? dstart[d] : 0;
+            tv[j] = (!SINGLE_TILE && d < RADIX) ? hist[(size_t)d * tiles + tiles - 1] : 0;
             s += v[j];
+            ts += tv[j];
         }
-        uint32_t incl = s;
+        uint32_t incl = s, tincl = ts;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-            uint32_t y = __shfl_up_sync(kFull, incl, off);
-            if (lane >= off) incl += y;
+            const uint32_t y = __shfl_up_sync(kFull, incl, off), ty = __shfl_up_sync(kFull, tincl, off);
+            if (lane >= off) incl += y, tincl += ty;
         }
-        uint32_t run = incl - s;
+        uint32_t run = incl - s, trun = tincl - ts;
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
-            int d = lane * PER + j;
+            const int d = lane * PER + j;
             if (d < RADIX) {
                 dstart[d] = run;
+                // the run of digit d from this tile starts after the lower
+                // digits' totals and this digit's runs from earlier tiles
+                gbase[d] = SINGLE_TILE ? run : trun + hist[(size_t)d * tiles + tile] - v[j];
                 run += v[j];
+                trun += tv[j];
             }
         }
     }
     __syncthreads();
-    for (int d = threadIdx.x; d < RADIX; d += kSortThreads)
-        gbase[d] = SINGLE_TILE ? dstart[d] : hist[d * tiles + tile];
-    __syncthreads();
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
-        uint32_t i = base + warp * (32 * kSortItems) + k * 32 + lane;
+        const uint32_t i = base + warp * (32 * kSortItems) + k * 32 + lane;
         if (i < n) {
-            uint32_t d = (key[k] >> shift) & (RADIX - 1);
-            uint32_t lp = dstart[d] + wcnt[warp][d] + rank[k];
-            skeys[lp] = key[k];
-            if (WITH_VALS) svals[lp] = val[k];
+            const uint32_t key = kin[i];
+            const uint32_t d = (key >> shift) & (RADIX - 1);
+            const uint32_t lp = dstart[d] + wcnt[warp][d] + ((rank2[k >> 1] >> (16 * (k & 1))) & 0xffffu);
+            skeys[lp] = key;
+            if (WITH_VALS) svals[lp] = vin ? vin[i] : i;
         }
     }
     __syncthreads();
     const uint32_t tile_n = min((uint32_t)kSortTile, n - base);
     for (uint32_t j = threadIdx.x; j < tile_n; j += kSortThreads) {
-        uint32_t kk = skeys[j];
-        uint32_t d = (kk >> shift) & (RADIX - 1);
-        uint32_t o = gbase[d] + j - dstart[d];
+        const uint32_t kk = skeys[j];
+        const uint32_t d = (kk >> shift) & (RADIX - 1);
+        const uint32_t o = gbase[d] + j - dstart[d];
         kout[o] = kk;
         if (WITH_VALS) vout[o] = svals[j];
     }
@@ -252,7 +233,7 @@ cuco_status_t sort_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *kout
         *launches += 1;
     } else {
         k_sort_hist<RB><<<tiles, kSortThreads, 0, stream>>>(kin, n, shift, hist, tiles);
-        k_sort_scan<RB><<<1, 1024, 0, stream>>>(hist, tiles);
+        k_sort_scan<<<1u << RB, kSortThreads, 0, stream>>>(hist, tiles);
         if (with_vals)
             k_sort_scatter<RB, true, false><<<tiles, kSortThreads, 0, stream>>>(
                 kin, vin, kout, vout, n, shift, hist, tiles);
