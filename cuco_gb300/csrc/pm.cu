@@ -326,36 +326,46 @@ __device__ __forceinline__ void fft_z_r2c_reg(const unsigned long long *__restri
     float2 *x = sm, *tw_s = sm + M * pitch;
     const size_t r0 = (size_t)blk * 2 * P;
     load_twiddles(tw_s, tw, M);
-    for (int e0 = threadIdx.x; e0 < 2 * P * M; e0 += kLoadBatch * blockDim.x) {
-        float v[kLoadBatch];
+    // rows 2pr and 2pr+1 packed as one complex column, one float2 per thread
+    // and element (both reads coalesced along the rows)
+    for (int e0 = threadIdx.x; e0 < P * M; e0 += kLoadBatch * blockDim.x) {
+        float2 v[kLoadBatch];
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = e0 + u * blockDim.x;
-            v[u] = e < 2 * P * M ? __fmul_rn(__ull2float_rn(rho64[r0 * M + e]), mscale) : 0.f;
+            v[u] = make_float2(0.f, 0.f);
+            if (e < P * M) {
+                const int pr = e / M, m = e & (M - 1);
+                const size_t g = (r0 + 2 * pr) * M + m;
+                v[u] = make_float2(__fmul_rn(__ull2float_rn(rho64[g]), mscale),
+                                   __fmul_rn(__ull2float_rn(rho64[g + M]), mscale));
+            }
         }
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = e0 + u * blockDim.x;
-            if (e < 2 * P * M) {
-                const int row = e / M, m = e & (M - 1);
-                reinterpret_cast<float *>(&x[m * pitch + (row >> 1)])[row & 1] = v[u];
-            }
+            if (e < P * M) x[(e & (M - 1)) * pitch + e / M] = v[u];
         }
     }
     __syncthreads();
-    FT::template forward<-1>(x, tw_s, pitch, ilog2(P));
-    for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) {
-        const int row = e / Mh, k = e - row * Mh, pr = row >> 1;
+    const int ps = ilog2(P);
+    FT::template forward<-1>(x, tw_s, pitch, ps);
+    // Both rows of a pair from the same two transform values, columns
+    // fastest (consecutive banks), into the row-major block y (after the
+    // twiddles; 2P (M/2+1) <= M (P+1) points as P <= M/2); then the block
+    // goes out whole: the CTA's 2P spectrum rows are contiguous.
+    float2 *y = tw_s + M;
+    for (int e = threadIdx.x; e < P * Mh; e += blockDim.x) {
+        const int pr = e & (P - 1), k = e >> ps;
         const float2 z = x[FT::slot(k) * pitch + pr];
         float2 zc = x[FT::slot((M - k) & (M - 1)) * pitch + pr];
         zc.y = -zc.y;
-        float2 o;
-        if ((row & 1) == 0)
-            o = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
-        else  // (z - zc) / (2i)
-            o = make_float2(0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x));
-        spec[(r0 + row) * Mh + k] = o;
+        y[(2 * pr) * Mh + k] = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
+        // (z - zc) / (2i)
+        y[(2 * pr + 1) * Mh + k] = make_float2(0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x));
     }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 2 * P * Mh; e += blockDim.x) spec[r0 * Mh + e] = y[e];
 }
 
 template <typename FT>
@@ -367,40 +377,42 @@ __device__ __forceinline__ void fft_z_c2r_reg(const float2 *__restrict__ spec, f
     float2 *x = sm, *tw_s = sm + M * pitch;
     const size_t r0 = (size_t)blk * 2 * P;
     load_twiddles(tw_s, tw, M);
-    // row pair pr packed as one complex column a + i b (a, b the Hermitian
-    // rows 2pr and 2pr+1, imaginary parts at k = 0 and M/2 dropped), placed
-    // in the slot order the inverse transform starts from
-    for (int e0 = threadIdx.x; e0 < P * M; e0 += kLoadBatch * blockDim.x) {
-        float2 va[kLoadBatch], vb[kLoadBatch];
+    // the CTA's 2P spectrum rows, contiguous, into the row-major block y
+    float2 *y = tw_s + M;
+    for (int e0 = threadIdx.x; e0 < 2 * P * Mh; e0 += kLoadBatch * blockDim.x) {
+        float2 v[kLoadBatch];
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = e0 + u * blockDim.x;
-            va[u] = vb[u] = make_float2(0.f, 0.f);
-            if (e < P * M) {
-                const int pr = e / M, k = e & (M - 1);
-                const int kk = k <= M / 2 ? k : M - k;
-                va[u] = spec[(r0 + 2 * pr) * Mh + kk];
-                vb[u] = spec[(r0 + 2 * pr + 1) * Mh + kk];
-            }
+            v[u] = e < 2 * P * Mh ? spec[r0 * Mh + e] : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = e0 + u * blockDim.x;
-            if (e < P * M) {
-                const int pr = e / M, k = e & (M - 1);
-                float2 a = va[u], b = vb[u];
-                if (k == 0 || k == M / 2) a.y = b.y = 0.f;
-                if (k > M / 2) a.y = -a.y, b.y = -b.y;
-                x[FT::slot(k) * pitch + pr] = make_float2(a.x - b.y, a.y + b.x);  // a + i b
-            }
+            if (e < 2 * P * Mh) y[e] = v[u];
         }
     }
     __syncthreads();
+    // row pair pr packed as one complex column a + i b (a, b the Hermitian
+    // rows 2pr and 2pr+1, imaginary parts at k = 0 and M/2 dropped), placed
+    // in the slot order the inverse transform starts from; columns fastest
+    const int ps = ilog2(P);
+    for (int e = threadIdx.x; e < P * M; e += blockDim.x) {
+        const int pr = e & (P - 1), k = e >> ps;
+        const int kk = k <= M / 2 ? k : M - k;
+        float2 a = y[(2 * pr) * Mh + kk], b = y[(2 * pr + 1) * Mh + kk];
+        if (k == 0 || k == M / 2) a.y = b.y = 0.f;
+        if (k > M / 2) a.y = -a.y, b.y = -b.y;
+        x[FT::slot(k) * pitch + pr] = make_float2(a.x - b.y, a.y + b.x);  // a + i b
+    }
+    __syncthreads();
     FT::template inverse<+1>(x, tw_s, pitch, ilog2(P));
-    for (int e = threadIdx.x; e < 2 * P * M; e += blockDim.x) {
-        const int row = e / M, m = e & (M - 1);
-        const float2 z = x[m * pitch + (row >> 1)];
-        out[(r0 + row) * M + m] = (row & 1) ? z.y : z.x;
+    // the pair's two real rows from one transform value
+    for (int e = threadIdx.x; e < P * M; e += blockDim.x) {
+        const int pr = e / M, m = e & (M - 1);
+        const float2 z = x[m * pitch + pr];
+        out[(r0 + 2 * pr) * M + m] = z.x;
+        out[(r0 + 2 * pr + 1) * M + m] = z.y;
     }
 }
 
@@ -671,7 +683,10 @@ __global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
 template <int M1, int M2>
 cudaError_t fft_passes_reg(const PMPlan &plan, int P, int B, cudaStream_t stream) {
     constexpr int M = M1 * M2, Mh = M / 2 + 1;
-    const size_t smz = sizeof(float2) * ((size_t)M * (P + 1) + M), sma = sizeof(float2) * ((size_t)M * B + M);
+    // z passes: the transform buffer, the twiddles and the block of 2P
+    // spectrum rows; axis passes: the buffer and the twiddles
+    const size_t smz = sizeof(float2) * ((size_t)M * (P + 1) + M + (size_t)2 * P * Mh),
+                 sma = sizeof(float2) * ((size_t)M * B + M);
     static bool attr = [&] {
         cudaFuncSetAttribute(k_fft_z_r2c_r<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         cudaFuncSetAttribute(k_fft_z_c2r_r<M1, M2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
