@@ -164,6 +164,33 @@ __global__ void __launch_bounds__(kRecThreads) k_apply_staged(PARTICLE *__restri
     min_endstep(endstep, min_end);
 }
 
+// The same streaming from the records at src to those at dst (either may be
+// the host's P[] or the device mirror): every record is written to dst,
+// changed or not.  compute_accelerations reads P[] once into the mirror and,
+// after the forces, writes the mirror's records with their new fields back
+// whole, so the host link carries P[] once each way instead of reading it
+// again to merge the force fields.
+template <class Op>
+__global__ void __launch_bounds__(kRecThreads) k_apply_staged_to(const PARTICLE *__restrict__ src,
+                                                                PARTICLE *__restrict__ dst, uint32_t n, Op op) {
+    __shared__ uint4 buf[kRecBytes / 16];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t first = blockIdx.x * kRecThreads;
+    const uint32_t cnt = min(n - first, (uint32_t)kRecThreads);
+    const uint32_t bytes = cnt * (uint32_t)sizeof(PARTICLE);
+    const uint32_t words = bytes / 16, tail = (bytes % 16) / 4;
+    const uint4 *gs = reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(src) + (size_t)first * sizeof(PARTICLE));
+    uint4 *gd = reinterpret_cast<uint4 *>(reinterpret_cast<char *>(dst) + (size_t)first * sizeof(PARTICLE));
+    for (uint32_t w = tid; w < words; w += kRecThreads) buf[w] = gs[w];
+    if (tid < tail) reinterpret_cast<uint32_t *>(buf + words)[tid] = reinterpret_cast<const uint32_t *>(gs + words)[tid];
+    __syncthreads();
+    int endstep = INT_MAX;
+    if (tid < cnt) op(reinterpret_cast<PARTICLE *>(buf)[tid], first + tid, endstep);
+    __syncthreads();
+    for (uint32_t w = tid; w < words; w += kRecThreads) gd[w] = buf[w];
+    if (tid < tail) reinterpret_cast<uint32_t *>(gd + words)[tid] = reinterpret_cast<const uint32_t *>(buf + words)[tid];
+}
+
 // positions (and velocities) to the engine's float4 arrays
 struct UnpackOp {
     float4 *pos, *vel;
@@ -565,9 +592,26 @@ void move_particles(int time0, int time1) {
 void compute_accelerations(void) {
     set_softenings();
     PARTICLE *pp = particles_in();
+    const int pm = All.PM_Ti_endstep == All.Ti_Current;
+    if (pp == P && NumPart) {
+        // P[] in place: one read of the records into the mirror (wrapped,
+        // positions to the engine), the forces, one write of the records back
+        DropinState &s = ds();
+        BoxView v = view();
+        const unsigned blocks = (NumPart + kRecThreads - 1) / kRecThreads;
+        k_apply_staged_to<<<blocks, kRecThreads, 0, v.stream>>>(
+            P, (PARTICLE *)s.dP, NumPart, DriftWrapOp{0.0, (double)All.BoxSize, 0, 1, v.pos});
+        capi_check(cudaGetLastError(), "compute_accelerations");
+        cuco_box_mark_state(s.box);
+        capi_status(cuco_box_forces(s.box, pm, 1), "compute_accelerations");
+        k_apply_staged_to<<<blocks, kRecThreads, 0, v.stream>>>(
+            (const PARTICLE *)s.dP, P, NumPart, PackOp{v.pos, v.vel, v.acc_pp, v.acc_pm, kPackPP | (pm ? kPackPM : 0)});
+        capi_check(cudaGetLastError(), "compute_accelerations");
+        particles_out(pp);
+        return;
+    }
     drift_wrap(pp, 0.0, false, true, true);  // wrap, and the positions to the engine
     cuco_box_mark_state(ds().box);
-    int pm = All.PM_Ti_endstep == All.Ti_Current;
     capi_status(cuco_box_forces(ds().box, pm, 1), "compute_accelerations");
     pack(pp, kPackPP | (pm ? kPackPM : 0));
     particles_out(pp);
