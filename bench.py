@@ -619,10 +619,8 @@ def run_e2e(steps, ic, soft, device):
     dt = time.perf_counter() - t0
     if lib.cuco_dropin_host_access():
         # kernels stream whole 60-byte records of P[] over the host link:
-        # move_particles and advance_and_find_timesteps read and write each
-        # once; compute_accelerations reads twice (wrap, then the force write)
-        # and writes once (the wrap writes back only records that wrapped)
         # each of the three calls reads P[] once and writes it once
+        # (compute_accelerations through the device mirror)
         h2d, d2h, access = 3 * 60 * n, 3 * 60 * n, "kernels stream P[] records in place over the host link"
     else:
         h2d, d2h, access = 3 * 60 * n, 3 * 60 * n, "whole P[] copied in and out per call"
