@@ -188,6 +188,15 @@ class Box:
         check(self.lib.cuco_box_timings(self.h, ptr(ms)), "cuco_box_timings")
         return dict(zip(self.PHASES, ms.tolist()))
 
+    def count_pairs(self, enable: bool = True):
+        """Count in-range pairs in the short-range launches from now on."""
+        check(self.lib.cuco_box_count_pairs(self.h, int(enable)), "cuco_box_count_pairs")
+
+    def pair_count(self, reset: bool = True) -> int:
+        c = ctypes.c_uint64()
+        check(self.lib.cuco_box_pair_count(self.h, ctypes.byref(c), int(reset)), "cuco_box_pair_count")
+        return c.value
+
     def phase_totals(self, reset: bool = True) -> dict:
         """Per-phase device time summed over the timed steps since the last reset."""
         ms = np.zeros(8, dtype=np.float32)
