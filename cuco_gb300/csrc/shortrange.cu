@@ -8,28 +8,35 @@
 //
 // Work layout (GB300-first rather than one thread per particle over a full
 // cube of cells):
-//   * one CTA per z-segment of S consecutive cells (ix, iy, iz0..iz0+S-1); its
-//     targets are one contiguous range of the cell-sorted particles;
+//   * a segment is S consecutive cells along z (ix, iy, iz0..iz0+S-1); its
+//     targets are one contiguous range of the cell order.  A unit of work is a
+//     segment, or a slice of at most kTMax targets of a denser one; a plan
+//     kernel lists each segment's targets and the dense slices, and a
+//     persistent grid (the CTAs that fit on the GPU) pulls units from a
+//     counter, dense slices first;
 //   * the sources are the neighbour columns (dx, dy) within rcut of the
 //     segment in xy, over z-cells iz0-R .. iz0+S-1+R.  A column's cells are
-//     consecutive keys, so it is at most two contiguous runs of sorted
-//     particles (two when the z range wraps); warps copy the runs into shared
+//     consecutive keys, so it is at most two contiguous runs of the cell order
+//     (two when the z range wraps); the unit's threads find every cell's
+//     staged offset with one block scan, and warps copy the runs into shared
 //     memory relative to an integer origin at the segment corner, with the
-//     periodic image shift applied once per run;
+//     periodic image shift applied once per run (in chunks of kMaxStage
+//     sources; every target runs against each chunk, its sums carried in
+//     shared memory);
 //   * one target per warp: lane k culls column k by the target's xy distance
-//     and narrows it to the z-cells within sqrt(rcut^2 - d_xy^2) (each column
-//     is culled once, not once per lane); a ballot lists the non-empty
-//     columns, and all 32 lanes walk each range together on consecutive
-//     staged sources (conflict-free shared-memory reads, no lanes idling on
-//     ranges of different length);
-//   * the pair law runs without branches on the common path (a candidate
-//     beyond the cut gets a zero factor), two candidates per lane per
-//     iteration into two accumulator sets for instruction-level parallelism;
-//   * 256-thread CTAs over 8-cell segments keep 8+ warps per scheduler on the
-//     shared memory a segment needs;
-//   * the warp adds its lanes' partial sums with xor shuffles;
-//   * the epilogue scatters the force to original particle order and, in the
-//     engine's step, kicks the velocity (timestep.c:56-59,86-91).
+//     and narrows it to the z range sqrt(rcut^2 - d_xy^2) reaches, trimmed in
+//     the two end cells to the z slices it reaches (the cells' particles are
+//     ordered by slice, with per-cell slice counts); the column ranges,
+//     concatenated by a warp scan, are walked 64 candidates at a time, every
+//     lane on consecutive staged sources;
+//   * the pair law runs without branches on the common path and flags the
+//     rest (bin-edge and cut-edge pairs decided in double, the spline), which
+//     runs under one warp-uniform branch; two candidates per lane per window
+//     into two accumulator sets;
+//   * the warp adds its lanes' partial sums with xor shuffles (the precision
+//     form compensated by error-free splitting);
+//   * the warp's lanes scatter the forces to original particle order and, in
+//     the engine's step, kick the velocities (timestep.c:56-59,86-91).
 //
 // Precision of the plain path.  A float computation of asmthfac*r lands in the
 // neighbouring table bin for ~3e-5 of the pairs, and at high redshift (net
@@ -37,8 +44,8 @@
 // rms against the reference's double path.  Coordinates relative to an integer
 // origin make the image shift exact (origin -/+ L is an exact float for
 // L < 2^23) and dx exact for ~97% of pairs; pairs whose r^2 lies within
-// 4e-7 of rcut^2 or whose asmthfac*r lies within 4e-7 (relative) of a bin edge
-// are decided in double as gravlist.cpp:298-320 does.
+// 8e-7 (relative) of rcut^2 or whose asmthfac*r lies within 4e-7 (relative)
+// of a bin edge are decided in double as gravlist.cpp:298-320 does.
 #include <algorithm>
 #include <cstring>
 
