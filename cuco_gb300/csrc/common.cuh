@@ -127,6 +127,7 @@ struct KickArgs {
     const float4 *acc_pm_s;   // PM acceleration in sorted order (may be null)
     float4 *acc_pm_out;       // PM acceleration scattered to original order (may be null)
     double kick_pp, kick_pm;
+    const float4 *acc_pm_o;   // PM acceleration in original order (used when acc_pm_s is null)
 };
 
 // Device scratch of a launch's work plan: each segment's target count, the
@@ -172,6 +173,7 @@ struct PMPlan {
     float fd_fac;       // G/(pi L) * M/(2L) (pm_periodic.c:85-86)
     float *rho;         // M^3 real grid: the potential
     unsigned long long *rho64;  // M^3 deposited mass in units of m / 2^32
+    bool rho64_dirty;   // rho64 may hold sums (the z pass clears what it reads)
     float2 *spec;       // M*M*(M/2+1) complex grid
     float *green1d;     // M/2+1: exp(-k^2 a) / sinc(pi k/M)^4
     float2 *twiddle;    // M: exp(-2 pi i t / M)
@@ -183,7 +185,7 @@ cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, fl
                              double G, bool fixed = false);
 void pm_plan_destroy(PMPlan *plan);
 // Long-range acceleration of n positions (any order) into acc (same order).
-cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,
+cuco_status_t pm_forces(PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,
                         cudaStream_t stream, cudaEvent_t *ev_deposit_done,
                         cudaEvent_t *ev_fft_done, int *launches);
 

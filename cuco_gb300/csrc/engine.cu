@@ -281,6 +281,8 @@ void shortrange_table(float *t) {
 
 using namespace cuco;
 
+constexpr int kPhaseEvents = 9;
+
 struct cuco_box {
     cuco_config_t cfg;
     uint32_t n = 0;
@@ -289,8 +291,12 @@ struct cuco_box {
     int key_bits = 0;
     float gridfac = 0.f;
     cudaStream_t stream = nullptr;
+    // the PM runs on its own stream beside the sort and the cell order,
+    // forked after the positions are final and joined before the short range
+    cudaStream_t pm_stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr;
-    float4 *spos = nullptr, *acc_pm_s = nullptr;
+    float4 *spos = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr;
     uint32_t *hist = nullptr, *cell_off = nullptr;
     uint4 *cell_sl = nullptr;  // per cell: z-slice counts
@@ -304,8 +310,10 @@ struct cuco_box {
     bool count_pairs = false;
     // phase events, two sets: a step records into ev[ev_cur] and the set of
     // the step before is read then, so timing never waits on the step just
-    // enqueued
-    cudaEvent_t ev[2][8] = {};
+    // enqueued.  0 start, 1 positions and keys done (the PM fork), 2 sort
+    // done, 3 cell order done, 4/5/6 deposit/FFT/interpolation done (PM
+    // stream), 8 short range starts (after the join), 7 end.
+    cudaEvent_t ev[2][kPhaseEvents] = {};
     int ev_cur = 0;
     bool ev_pending = false;  // ev[ev_cur ^ 1] holds a recorded step not yet read
     float last_ms[8] = {};
@@ -358,12 +366,29 @@ cuco_status_t drift_keys(cuco_box *b, double drift, bool do_drift) {
                              b->stream);
 }
 
-void record(cuco_box *b, int i) {
-    if (b->timing) cudaEventRecord(b->ev[b->ev_cur][i], b->stream);
+void record(cuco_box *b, int i, cudaStream_t s = nullptr) {
+    if (b->timing) cudaEventRecord(b->ev[b->ev_cur][i], s ? s : b->stream);
 }
 
 // keys must already be in b->keys; runs sort, reorder, PM, short range (+kick)
 cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kick) {
+    // The PM reads the positions in original order and writes its
+    // accelerations in original order (its results do not depend on the
+    // order: integer deposit sums, one interpolation per particle), so it
+    // needs nothing from the sort and runs beside it.
+    if (pm) {
+        CUCO_TRY_CUDA(cudaEventRecord(b->fork, b->stream));
+        CUCO_TRY_CUDA(cudaStreamWaitEvent(b->pm_stream, b->fork, 0));
+        CUCO_TRY(pm_forces(b->pm, b->pos, b->n, b->acc_pm, b->pm_stream,
+                           b->timing ? &b->ev[b->ev_cur][4] : nullptr, b->timing ? &b->ev[b->ev_cur][5] : nullptr,
+                           &b->launches));
+        record(b, 6, b->pm_stream);
+        CUCO_TRY_CUDA(cudaEventRecord(b->join, b->pm_stream));
+    } else {
+        record(b, 4);
+        record(b, 5);
+        record(b, 6);
+    }
     bool in_alt = false;
     CUCO_TRY(sort_pairs(b->keys, b->perm, nullptr, b->keys_alt, b->perm_alt, b->hist, b->n,
                         b->key_bits, 8, b->stream, &in_alt, &b->launches));
@@ -382,27 +407,18 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
                                  nullptr, 1, b->cfg.mode == CUCO_MODE_FIXED, b->stream));
     b->launches += 2;
     record(b, 3);
-    if (pm) {
-        CUCO_TRY(pm_forces(b->pm, b->spos, b->n, b->acc_pm_s, b->stream,
-                           b->timing ? &b->ev[b->ev_cur][4] : nullptr, b->timing ? &b->ev[b->ev_cur][5] : nullptr,
-                           &b->launches));
-    } else {
-        record(b, 4);
-        record(b, 5);
-    }
-    record(b, 6);
+    if (pm) CUCO_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
+    record(b, 8);
     if (pp) {
         KickArgs k{};
         if (kick) k = *kick;
-        k.acc_pm_s = pm ? b->acc_pm_s : nullptr;
-        k.acc_pm_out = pm ? b->acc_pm : nullptr;
+        k.acc_pm_s = nullptr;
+        k.acc_pm_out = nullptr;
+        k.acc_pm_o = pm ? b->acc_pm : nullptr;
         CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, perm_s, b->cell_off,
                                    nullptr, kCellOffsets, b->table, b->acc_pp, k, b->work, b->stream,
                                    b->count_pairs ? b->pair_counter : nullptr));
         b->launches += 2;  // work plan + persistent short range
-    } else if (pm) {
-        CUCO_TRY(scatter4(b->acc_pm_s, perm_s, b->acc_pm, b->n, b->stream));
-        b->launches += 1;
     }
     record(b, 7);
     return CUCO_OK;
@@ -414,16 +430,16 @@ cuco_status_t read_pending(cuco_box *b) {
     b->ev_pending = false;
     cudaEvent_t *e = b->ev[b->ev_cur ^ 1];
     CUCO_TRY_CUDA(cudaEventSynchronize(e[7]));
-    for (int i = 0; i < 7; ++i) {
+    // drift+keys, sort, cell order; the PM's three phases from the fork (they
+    // overlap the sort and the cell order); the short range from the join;
+    // the whole pass
+    static const int from[8] = {0, 1, 2, 1, 4, 5, 8, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
+    for (int i = 0; i < 8; ++i) {
         float ms = 0.f;
-        cudaEventElapsedTime(&ms, e[i], e[i + 1]);
+        cudaEventElapsedTime(&ms, e[from[i]], e[to[i]]);
         b->last_ms[i] = ms;
         b->acc_ms[i] += ms;
     }
-    float tot = 0.f;
-    cudaEventElapsedTime(&tot, e[0], e[7]);
-    b->last_ms[7] = tot;
-    b->acc_ms[7] += tot;
     return CUCO_OK;
 }
 
@@ -485,14 +501,26 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         cuco_box_destroy(b);
         return st;
     };
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // The box's stream has the higher priority: while the PM runs beside the
+    // sort and the cell order, their CTAs are scheduled first and the PM
+    // takes the SMs they leave idle (measured faster than the reverse, whose
+    // sort passes waited behind the PM's transform CTAs).
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithPriority(&b->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
         set_error("cudaStreamCreate failed");
         delete b;
         return CUCO_ERR_CUDA;
     }
+    if (cudaStreamCreateWithPriority(&b->pm_stream, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        return fail(CUCO_ERR_CUDA);
+    }
     const size_t n = b->n;
     if ((s = alloc(&b->pos, n)) || (s = alloc(&b->vel, n)) || (s = alloc(&b->acc_pp, n)) ||
-        (s = alloc(&b->acc_pm, n)) || (s = alloc(&b->spos, n)) || (s = alloc(&b->acc_pm_s, n)) ||
+        (s = alloc(&b->acc_pm, n)) || (s = alloc(&b->spos, n)) ||
         (s = alloc(&b->keys, n)) || (s = alloc(&b->perm, n)) || (s = alloc(&b->keys_alt, n)) ||
         (s = alloc(&b->perm_alt, n)) ||
         (s = alloc(&b->hist, sort_hist_entries(b->n, b->key_bits, 8))) ||
@@ -518,7 +546,7 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
     cudaMemsetAsync(b->acc_pm, 0, sizeof(float4) * (n ? n : 1), b->stream);
     cudaMemsetAsync(b->vel, 0, sizeof(float4) * (n ? n : 1), b->stream);
     for (int k = 0; k < 2; ++k)
-        for (int i = 0; i < 8; ++i) cudaEventCreate(&b->ev[k][i]);
+        for (int i = 0; i < kPhaseEvents; ++i) cudaEventCreate(&b->ev[k][i]);
     cudaEventCreate(&b->tstart);
     cudaEventCreate(&b->tstop);
     *out = b;
@@ -533,7 +561,6 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     cudaFree(b->acc_pp);
     cudaFree(b->acc_pm);
     cudaFree(b->spos);
-    cudaFree(b->acc_pm_s);
     cudaFree(b->keys);
     cudaFree(b->perm);
     cudaFree(b->keys_alt);
@@ -551,8 +578,11 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     if (b->tstop) cudaEventDestroy(b->tstop);
     if (b->pm.rho) pm_plan_destroy(&b->pm);
     for (int k = 0; k < 2; ++k)
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < kPhaseEvents; ++i)
             if (b->ev[k][i]) cudaEventDestroy(b->ev[k][i]);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    if (b->pm_stream) cudaStreamDestroy(b->pm_stream);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return CUCO_OK;

@@ -318,7 +318,7 @@ __host__ __device__ inline bool reg_fft_ok(int M, int cols) {
 // The passes below with the register transforms (M = FT::M; one buffer of
 // M * pitch points, the twiddle table after it).
 template <typename FT>
-__device__ __forceinline__ void fft_z_r2c_reg(const unsigned long long *__restrict__ rho64, float mscale,
+__device__ __forceinline__ void fft_z_r2c_reg(unsigned long long *__restrict__ rho64, float mscale,
                                               float2 *__restrict__ spec, const float2 *tw, int P, int blk) {
     constexpr int M = FT::M, Mh = M / 2 + 1;
     extern __shared__ float2 sm[];
@@ -327,7 +327,8 @@ __device__ __forceinline__ void fft_z_r2c_reg(const unsigned long long *__restri
     const size_t r0 = (size_t)blk * 2 * P;
     load_twiddles(tw_s, tw, M);
     // rows 2pr and 2pr+1 packed as one complex column, one float2 per thread
-    // and element (both reads coalesced along the rows)
+    // and element (both reads coalesced along the rows); every sum read is
+    // cleared for the next deposit
     for (int e0 = threadIdx.x; e0 < P * M; e0 += kLoadBatch * blockDim.x) {
         float2 v[kLoadBatch];
 #pragma unroll
@@ -344,7 +345,13 @@ __device__ __forceinline__ void fft_z_r2c_reg(const unsigned long long *__restri
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = e0 + u * blockDim.x;
-            if (e < P * M) x[(e & (M - 1)) * pitch + e / M] = v[u];
+            if (e < P * M) {
+                const int pr = e / M, m = e & (M - 1);
+                const size_t g = (r0 + 2 * pr) * M + m;
+                rho64[g] = 0ull;
+                rho64[g + M] = 0ull;
+                x[m * pitch + pr] = v[u];
+            }
         }
     }
     __syncthreads();
@@ -484,7 +491,7 @@ __device__ __forceinline__ void fft_axis_reg(float2 *__restrict__ spec, const fl
 }
 
 // rows r0 .. r0+2P-1 of the M^3 real grid (row = x*M + y) -> spectrum rows
-__device__ __forceinline__ void fft_z_r2c(const unsigned long long *__restrict__ rho64, float mscale,
+__device__ __forceinline__ void fft_z_r2c(unsigned long long *__restrict__ rho64, float mscale,
                                           float2 *__restrict__ spec, const float2 *tw, int M, int P, int blk) {
     extern __shared__ float2 sm[];
     const int pitch = P + 1;
@@ -507,6 +514,7 @@ __device__ __forceinline__ void fft_z_r2c(const unsigned long long *__restrict__
         for (int u = 0; u < kLoadBatch; ++u) {
             int e = e0 + u * blockDim.x;
             if (e < 2 * P * M) {
+                rho64[r0 * M + e] = 0ull;  // cleared for the next deposit
                 const int row = (int)dM.div((uint32_t)e), m = e - row * M;
                 float *slot = reinterpret_cast<float *>(&x[m * pitch + (row >> 1)]);
                 slot[row & 1] = v[u];
@@ -641,7 +649,7 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
 }
 
 __global__ void __launch_bounds__(kFFTThreads)
-    k_fft_z_r2c(const unsigned long long *__restrict__ rho64, float mscale, float2 *__restrict__ spec,
+    k_fft_z_r2c(unsigned long long *__restrict__ rho64, float mscale, float2 *__restrict__ spec,
                 const float2 *tw, int M, int P) {
     fft_z_r2c(rho64, mscale, spec, tw, M, P, blockIdx.x);
 }
@@ -661,7 +669,7 @@ __global__ void __launch_bounds__(kFFTThreads)
 // instantiation per split (its registers sized for its DFT lengths).
 template <int M1, int M2>
 __global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
-    k_fft_z_r2c_r(const unsigned long long *__restrict__ rho64, float mscale, float2 *__restrict__ spec,
+    k_fft_z_r2c_r(unsigned long long *__restrict__ rho64, float mscale, float2 *__restrict__ spec,
                   const float2 *tw, int P) {
     fft_z_r2c_reg<RegFFT<M1, M2>>(rho64, mscale, spec, tw, P, blockIdx.x);
 }
@@ -1071,6 +1079,7 @@ cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, fl
     const size_t Mh = M / 2 + 1;
     CUCO_TRY_CUDA(cudaMalloc(&plan->rho, sizeof(float) * (size_t)M * M * M));
     CUCO_TRY_CUDA(cudaMalloc(&plan->rho64, sizeof(unsigned long long) * (size_t)M * M * M));
+    plan->rho64_dirty = true;
     CUCO_TRY_CUDA(cudaMalloc(&plan->spec, sizeof(float2) * (size_t)M * M * Mh));
     CUCO_TRY_CUDA(cudaMalloc(&plan->green1d, sizeof(float) * Mh));
     CUCO_TRY_CUDA(cudaMalloc(&plan->twiddle, sizeof(float2) * M));
@@ -1110,14 +1119,19 @@ void pm_plan_destroy(PMPlan *plan) {
     plan->spec = nullptr;
 }
 
-cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,
+cuco_status_t pm_forces(PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc,
                         cudaStream_t stream, cudaEvent_t *ev_deposit_done, cudaEvent_t *ev_fft_done,
                         int *launches) {
     const int M = plan.M, Mh = M / 2 + 1;
     const int P = fft_batch_z(M), B = fft_batch_axis(M);
     const size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
     const size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
-    CUCO_TRY_CUDA(cudaMemsetAsync(plan.rho64, 0, sizeof(unsigned long long) * (size_t)M * M * M, stream));
+    // The z r2c pass clears the sums it reads, so the grid is zero again when
+    // the previous call enqueued its passes; otherwise (first call, or a call
+    // that stopped at an error) it is cleared here.
+    if (plan.rho64_dirty)
+        CUCO_TRY_CUDA(cudaMemsetAsync(plan.rho64, 0, sizeof(unsigned long long) * (size_t)M * M * M, stream));
+    plan.rho64_dirty = true;
     if (n) {
         if (plan.fixed)
             k_deposit<true><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho64, M, plan.to_slab_fac);
@@ -1149,6 +1163,7 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
         k_fft_z_c2r<<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, M, P);
         CUCO_TRY_CUDA(cudaGetLastError());
     }
+    plan.rho64_dirty = false;
     if (ev_fft_done) CUCO_TRY_CUDA(cudaEventRecord(*ev_fft_done, stream));
     if (n) {
         if (plan.fixed)
@@ -1157,7 +1172,7 @@ cuco_status_t pm_forces(const PMPlan &plan, const float4 *pos, uint32_t n, float
             k_interp<false><<<(n + 255) / 256, 256, 0, stream>>>(pos, n, plan.rho, M, plan.to_slab_fac, plan.fd_fac, acc);
     }
     CUCO_TRY_CUDA(cudaGetLastError());
-    if (launches) *launches += 8;
+    if (launches) *launches += 5 + (n ? 2 : 0);  // five transform passes, deposit and interpolation
     return CUCO_OK;
 }
 

@@ -663,9 +663,12 @@ __device__ __forceinline__ void shortrange_segment(
         const uint32_t o = perm[i];
         acc_out[o] = a;
         float4 gpm = make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool with_pm = kick.acc_pm_s || kick.acc_pm_o;
         if (kick.acc_pm_s) {
             gpm = kick.acc_pm_s[i];
             if (kick.acc_pm_out) kick.acc_pm_out[o] = gpm;
+        } else if (kick.acc_pm_o) {
+            gpm = kick.acc_pm_o[o];
         }
         if (KICK) {
             float4 v = kick.vel[o];
@@ -675,7 +678,7 @@ __device__ __forceinline__ void shortrange_segment(
             v.x += __fmul_rn(a.x, kp);
             v.y += __fmul_rn(a.y, kp);
             v.z += __fmul_rn(a.z, kp);
-            if (kick.acc_pm_s) {
+            if (with_pm) {
                 v.x = __fmaf_rn(gpm.x, km, v.x);
                 v.y = __fmaf_rn(gpm.y, km, v.y);
                 v.z = __fmaf_rn(gpm.z, km, v.z);

@@ -241,8 +241,11 @@ cuco_status_t cuco_box_sync(cuco_box_t *box);
 cuco_status_t cuco_box_stream(cuco_box_t *box, void **stream);
 
 /* Device time (ms) of each phase of the last cuco_box_forces/cuco_box_step:
- * [0] drift+keys, [1] sort, [2] reorder, [3] PM deposit, [4] PM FFT+Green,
- * [5] PM gradient+interpolation, [6] short range (+kick), [7] total.
+ * [0] drift+keys, [1] sort, [2] reorder (cell bounds and z-slice order),
+ * [3] PM deposit, [4] PM FFT+Green, [5] PM gradient+interpolation,
+ * [6] short range (+kick), [7] total.  The PM runs on a second stream beside
+ * the sort and the reorder (from the end of [0] to the start of [6]), so
+ * [0] + max([1] + [2], [3] + [4] + [5]) + [6] is about [7].
  * Only filled when phase timing is enabled. */
 cuco_status_t cuco_box_enable_timing(cuco_box_t *box, int enable);
 cuco_status_t cuco_box_timings(cuco_box_t *box, float *ms /* 8 */);

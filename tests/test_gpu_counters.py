@@ -4,7 +4,8 @@ and the per-phase device times.
 The pair count (r^2 <= rcut^2, the self pair excluded) is compared with a
 brute-force count in double precision over all minimum-image pairs; the two
 may differ only for pairs within rounding of the cut.  The phase times of a
-run of steps are non-negative and add up to about the timed total.
+run of steps are non-negative and tile the timed total (the PM beside the
+sort and the reorder).
 """
 import numpy as np
 import pytest
@@ -65,5 +66,13 @@ def test_phase_totals_add_up():
     parts = [v for k, v in t.items() if k != "total"]
     assert all(v >= 0.0 for v in parts)
     assert t["total"] > 0.0
-    # the phases tile each step; the tolerance covers event granularity
-    assert abs(sum(parts) - t["total"]) <= 0.05 * t["total"] + 0.05
+    # Each step is drift+keys, then two branches side by side (sort and
+    # reorder; the PM on its own stream), then the short range.  Summed over
+    # steps, the longer branch lies between the larger branch total and the
+    # sum of both; the tolerance covers event granularity.
+    serial = t["drift+keys"] + t["shortrange"]
+    a = t["sort"] + t["reorder"]
+    b = t["pm_deposit"] + t["pm_fft"] + t["pm_interp"]
+    tol = 0.05 * t["total"] + 0.05
+    assert serial + max(a, b) <= t["total"] + tol
+    assert t["total"] <= serial + a + b + tol
