@@ -312,6 +312,10 @@ struct cuco_ensemble {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    // the PM's stream beside the sort (forked after the keys, joined before
+    // the short range; both branches are captured into the step's graph)
+    cudaStream_t pm_stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     // capacities (elements) of the grow-only arrays
     size_t cap_n = 0, cap_hist = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
            cap_green = 0, cap_tw = 0, cap_table = 0, cap_pbeg = 0, cap_segbase = 0, cap_drift = 0, cap_pm = 0,
@@ -334,6 +338,12 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
         CUCO_TRY_CUDA(cudaGetLastError());
         e->launches++;
     }
+    // The PM reads the positions and writes its accelerations in original
+    // order (order-independent results), beside the sort and the cell order.
+    CUCO_TRY_CUDA(cudaEventRecord(e->fork, e->stream));
+    CUCO_TRY_CUDA(cudaStreamWaitEvent(e->pm_stream, e->fork, 0));
+    CUCO_TRY(pm_forces_multi(e->pm, e->pos, e->n, e->acc_pm, e->pm_stream, &e->launches));
+    CUCO_TRY_CUDA(cudaEventRecord(e->join, e->pm_stream));
     bool in_alt = false;
     CUCO_TRY(sort_pairs(e->keys, e->perm, nullptr, e->keys_alt, e->perm_alt, e->hist, e->n, e->key_bits, 8,
                         e->stream, &in_alt, &e->launches));
@@ -347,11 +357,10 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
     CUCO_TRY(launch_cell_subsort(e->cell_off, e->sorted_perm, e->pos, e->spos, perm_s, e->cell_sl,
                                  (uint32_t)e->ncells, CellBox{}, e->d_drift, e->nbox, e->fixed, e->stream));
     e->launches += 2;
-    CUCO_TRY(pm_forces_multi(e->pm, e->spos, e->n, e->acc_pm_s, e->stream, &e->launches));
+    CUCO_TRY_CUDA(cudaStreamWaitEvent(e->stream, e->join, 0));
     KickArgs k{};
     k.vel = kick ? e->vel : nullptr;
-    k.acc_pm_s = e->acc_pm_s;
-    k.acc_pm_out = e->acc_pm;
+    k.acc_pm_o = e->acc_pm;
     SRWork w{e->sr_heavy, (uint32_t)e->cap_heavy, e->sr_segnt, (uint32_t)e->cap_segnt, e->sr_ctl};
     CUCO_TRY(launch_shortrange_multi(e->d_sr, e->d_kicks, e->d_segbase, e->nbox, e->segments, e->sr_smem, e->fixed,
                                      e->spos, perm_s, e->cell_off, e->table, e->acc_pp, k, w, e->stream,
@@ -641,9 +650,19 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
     cuco_ensemble *e = new cuco_ensemble();
     e->device = boxes[0].device;
     e->fixed = boxes[0].mode == CUCO_MODE_FIXED;
-    if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // the sort's stream first, the PM's on the SMs it leaves (as for one box)
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithPriority(&e->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess) {
         set_error("cudaStreamCreate failed");
         delete e;
+        return CUCO_ERR_CUDA;
+    }
+    if (cudaStreamCreateWithPriority(&e->pm_stream, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        cuco_ensemble_destroy(e);
         return CUCO_ERR_CUDA;
     }
     cudaEventCreate(&e->t0);
@@ -696,6 +715,9 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
     if (e->h_kicks) cudaFreeHost(e->h_kicks);
     if (e->t0) cudaEventDestroy(e->t0);
     if (e->t1) cudaEventDestroy(e->t1);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->join) cudaEventDestroy(e->join);
+    if (e->pm_stream) cudaStreamDestroy(e->pm_stream);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
     return CUCO_OK;
