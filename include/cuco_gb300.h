@@ -237,7 +237,10 @@ cuco_status_t cuco_box_run(cuco_box_t *box, int nsteps, const double *drift,
                            const double *kick_pp, const double *kick_pm);
 
 cuco_status_t cuco_box_sync(cuco_box_t *box);
-/* The box's CUDA stream (cudaStream_t). */
+/* The box's CUDA stream (cudaStream_t).  Every pass is ordered on it: the
+ * PM's second stream forks from it after the keys and joins it again before
+ * the short range, so work enqueued on this stream before or after a pass is
+ * ordered with all of the pass. */
 cuco_status_t cuco_box_stream(cuco_box_t *box, void **stream);
 
 /* Device time (ms) of each phase of the last cuco_box_forces/cuco_box_step:
