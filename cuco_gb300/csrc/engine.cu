@@ -556,6 +556,7 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
 cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     if (!b) return CUCO_OK;
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->pm_stream) cudaStreamSynchronize(b->pm_stream);  // a pass that stopped before its join
     cudaFree(b->pos);
     cudaFree(b->vel);
     cudaFree(b->acc_pp);

@@ -700,6 +700,7 @@ cuco_status_t cuco_ensemble_reshape(cuco_ensemble_t *e, const cuco_config_t *box
 cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
     if (!e) return CUCO_OK;
     if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->pm_stream) cudaStreamSynchronize(e->pm_stream);  // a pass that stopped before its join
     drop_graph(e);
     for (void *p : {(void *)e->pos, (void *)e->vel, (void *)e->acc_pp, (void *)e->acc_pm, (void *)e->spos,
                     (void *)e->acc_pm_s, (void *)e->keys, (void *)e->perm, (void *)e->keys_alt, (void *)e->perm_alt,
