@@ -157,7 +157,7 @@ __device__ float2 *fft_columns(float2 *x, float2 *y, const float2 *tw, int M, in
     return in;
 }
 
-__host__ __device__ __forceinline__ int ilog2(int v) {
+__host__ __device__ constexpr int ilog2(int v) {
     int l = 0;
     while ((1 << (l + 1)) <= v) ++l;
     return l;
@@ -666,6 +666,84 @@ __global__ void __launch_bounds__(kFFTThreads)
     fft_axis(spec, tw, green1d, M, B, axis, sign, green, blockIdx.x, blockIdx.y);
 }
 
+// fft_axis_reg for one box, with the batch B a compile-time constant
+// (B divides the block and M * B is a multiple of it): each thread keeps one
+// column b and visits the points m = r0 + j * (threads / B), so the index
+// arithmetic of the loads, stores and transforms folds to constants and the
+// Green's factor's column terms are computed once.  Same transforms and the
+// same operations per point as fft_axis_reg.
+template <typename FT, int B>
+__device__ __forceinline__ void fft_axis_reg_fixed(float2 *__restrict__ spec, const float2 *tw,
+                                                   const float *__restrict__ green1d, int axis, int sign,
+                                                   int green, int bx, int by) {
+    constexpr int M = FT::M, Mh = M / 2 + 1;
+    constexpr int bsh = ilog2(B), rs = kFFTThreads / B, per = M * B / kFFTThreads;
+    static_assert(kFFTThreads % B == 0 && (M * B) % kFFTThreads == 0, "batch layout");
+    extern __shared__ float2 sm[];
+    float2 *x = sm, *tw_s = sm + M * B;
+    const int o = by, kz0 = bx * B, nb = min(B, Mh - kz0);
+    const int b = threadIdx.x & (B - 1), r0 = threadIdx.x >> bsh;
+    const bool valid = b < nb;
+    const size_t sm_stride = axis == 1 ? (size_t)Mh : (size_t)M * Mh;
+    float2 *col = spec + (axis == 1 ? (size_t)o * M * Mh : (size_t)o * Mh) + kz0 + b;
+    // an inverse-only pass starts from the slot order
+    const bool to_slots = sign > 0;
+    load_twiddles(tw_s, tw, M);
+#pragma unroll
+    for (int j0 = 0; j0 < per; j0 += kLoadBatch) {
+        float2 v[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u)
+            if (j0 + u < per) v[u] = valid ? col[(size_t)(r0 + (j0 + u) * rs) * sm_stride] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u)
+            if (j0 + u < per) {
+                const int m = r0 + (j0 + u) * rs;
+                x[(to_slots ? FT::slot(m) : m) * B + b] = v[u];
+            }
+    }
+    __syncthreads();
+    bool natural = true;
+    if (sign < 0) {
+        FT::template forward<-1>(x, tw_s, B, bsh);
+        natural = false;
+        if (green) {
+            // slot s = M2 k1 + k2 holds X[k1 + M1 k2]
+            const int ky = o <= M / 2 ? o : M - o;
+            const float gy = green1d[ky];
+            const int kz = kz0 + b;
+            const float gz = valid ? green1d[kz] : 0.f;
+            const int c = ky * ky + kz * kz;
+#pragma unroll 4
+            for (int j = 0; j < per; ++j) {
+                const int sl = r0 + j * rs;
+                const int k1 = sl / FT::N2, k2 = sl - k1 * FT::N2;
+                const int m = k1 + FT::N1 * k2;  // the transform index along x
+                const int kx = m <= M / 2 ? m : M - m;
+                const float2 v = x[sl * B + b];
+                float g = 0.f;
+                if (valid) {
+                    const int k2s = kx * kx + c;
+                    if (k2s > 0) g = -green1d[kx] * gy * gz / (float)k2s;
+                }
+                x[sl * B + b] = make_float2(v.x * g, v.y * g);
+            }
+            __syncthreads();
+            FT::template inverse<+1>(x, tw_s, B, bsh);
+            natural = true;
+        }
+    } else {
+        FT::template inverse<+1>(x, tw_s, B, bsh);
+    }
+    if (valid) {
+#pragma unroll 4
+        for (int j = 0; j < per; ++j) {
+            const int m = r0 + j * rs;
+            col[(size_t)m * sm_stride] = x[(natural ? m : FT::slot(m)) * B + b];
+        }
+    }
+}
+
 // One box, power-of-two mesh M = M1 * M2: the register transforms, one
 // instantiation per split (its registers sized for its DFT lengths).
 template <int M1, int M2>
@@ -681,17 +759,21 @@ __global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
     fft_z_c2r_reg<RegFFT<M1, M2>>(spec, out, tw, P, blockIdx.x);
 }
 
+// the one-box batch of the axis passes, fft_batch_axis(M)
+__host__ __device__ constexpr int axis_batch(int M) { return 4096 / M > 16 ? 16 : 4096 / M; }
+
 template <int M1, int M2>
 __global__ void __launch_bounds__(kFFTThreads, M1 * M2 >= 512 ? 2 : 4)
-    k_fft_axis_r(float2 *__restrict__ spec, const float2 *tw, const float *__restrict__ green1d, int B, int axis,
+    k_fft_axis_r(float2 *__restrict__ spec, const float2 *tw, const float *__restrict__ green1d, int axis,
                  int sign, int green) {
-    fft_axis_reg<RegFFT<M1, M2>>(spec, tw, green1d, B, axis, sign, green, blockIdx.x, blockIdx.y);
+    fft_axis_reg_fixed<RegFFT<M1, M2>, axis_batch(M1 * M2)>(spec, tw, green1d, axis, sign, green, blockIdx.x,
+                                                            blockIdx.y);
 }
 
 // The five transform passes of one box with the register transforms.
 template <int M1, int M2>
-cudaError_t fft_passes_reg(const PMPlan &plan, int P, int B, cudaStream_t stream) {
-    constexpr int M = M1 * M2, Mh = M / 2 + 1;
+cudaError_t fft_passes_reg(const PMPlan &plan, int P, cudaStream_t stream) {
+    constexpr int M = M1 * M2, Mh = M / 2 + 1, B = axis_batch(M);
     // z passes: the transform buffer, the twiddles and the block of 2P
     // spectrum rows; axis passes: the buffer and the twiddles
     const size_t smz = sizeof(float2) * ((size_t)M * (P + 1) + M + (size_t)2 * P * Mh),
@@ -707,9 +789,9 @@ cudaError_t fft_passes_reg(const PMPlan &plan, int P, int B, cudaStream_t stream
     k_fft_z_r2c_r<M1, M2><<<zblocks, kFFTThreads, smz, stream>>>(plan.rho64, ldexpf(plan.mass, -32), plan.spec,
                                                                  plan.twiddle, P);
     dim3 ag((Mh + B - 1) / B, M);
-    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, B, 1, -1, 0);
-    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, B, 0, -1, 1);
-    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, B, 1, +1, 0);
+    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, 1, -1, 0);
+    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, 0, -1, 1);
+    k_fft_axis_r<M1, M2><<<ag, kFFTThreads, sma, stream>>>(plan.spec, plan.twiddle, plan.green1d, 1, +1, 0);
     k_fft_z_c2r_r<M1, M2><<<zblocks, kFFTThreads, smz, stream>>>(plan.spec, plan.rho, plan.twiddle, P);
     return cudaGetLastError();
 }
@@ -1146,13 +1228,13 @@ cuco_status_t pm_forces(PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc
     if (reg_fft_ok(M, P) && reg_fft_ok(M, B)) {
         cudaError_t e;
         switch (M) {
-            case 16: e = fft_passes_reg<4, 4>(plan, P, B, stream); break;
-            case 32: e = fft_passes_reg<4, 8>(plan, P, B, stream); break;
-            case 64: e = fft_passes_reg<8, 8>(plan, P, B, stream); break;
-            case 128: e = fft_passes_reg<8, 16>(plan, P, B, stream); break;
-            case 256: e = fft_passes_reg<16, 16>(plan, P, B, stream); break;
-            case 512: e = fft_passes_reg<16, 32>(plan, P, B, stream); break;
-            default: e = fft_passes_reg<32, 32>(plan, P, B, stream); break;
+            case 16: e = fft_passes_reg<4, 4>(plan, P, stream); break;
+            case 32: e = fft_passes_reg<4, 8>(plan, P, stream); break;
+            case 64: e = fft_passes_reg<8, 8>(plan, P, stream); break;
+            case 128: e = fft_passes_reg<8, 16>(plan, P, stream); break;
+            case 256: e = fft_passes_reg<16, 16>(plan, P, stream); break;
+            case 512: e = fft_passes_reg<16, 32>(plan, P, stream); break;
+            default: e = fft_passes_reg<32, 32>(plan, P, stream); break;
         }
         CUCO_TRY_CUDA(e);
     } else {
