@@ -948,31 +948,33 @@ __device__ __forceinline__ float4 interp_one(float4 p, const float *__restrict__
     int s[3][2];
     float d[3];
     cic_point<FIXED>(p, to_slab_fac, M, s, d);
-    const size_t Mz = M, Myz = (size_t)M * M;
     float wx[2] = {1.f - d[0], d[0]}, wy[2] = {1.f - d[1], d[1]}, wz[2] = {1.f - d[2], d[2]};
+    // Per dimension the six mesh planes s-2 .. s+3 (periodic), as offsets:
+    // the two corners are planes 2 and 3, and along each dimension the two
+    // corners' stencils (c-2, c-1, c+1, c+2) share one line of six points,
+    // so every potential value loaded is one sum of three offsets.
+    int off[3][6];
+#pragma unroll
+    for (int dim = 0; dim < 3; ++dim) {
+        const int scale = dim == 0 ? M * M : (dim == 1 ? M : 1);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) off[dim][q] = wrapi(s[dim][0] - 2 + q, M) * scale;
+    }
     float out[3];
 #pragma unroll
     for (int dim = 0; dim < 3; ++dim) {
-        // along dim the two corners' stencils (c-2, c-1, c+1, c+2) share one
-        // line of six points s-2 .. s+3: 4 lines x 6 loads instead of 32
+        // 4 lines x 6 loads instead of 32
         float F[2][2][2];
 #pragma unroll
         for (int u = 0; u < 2; ++u)
 #pragma unroll
             for (int v = 0; v < 2; ++v) {
-                // the two other dimensions' corner indices
-                int c[3];
-                c[dim] = 0;
-                c[(dim + 1) % 3] = s[(dim + 1) % 3][u];
-                c[(dim + 2) % 3] = s[(dim + 2) % 3][v];
-                const int s0 = s[dim][0];
+                // the two other dimensions' corner planes
+                const int d1 = (dim + 1) % 3, d2 = (dim + 2) % 3;
+                const int base = off[d1][2 + u] + off[d2][2 + v];
                 float f[6];
 #pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    int cc[3] = {c[0], c[1], c[2]};
-                    cc[dim] = wrapi(s0 - 2 + q, M);
-                    f[q] = __ldg(&phi[cc[0] * Myz + cc[1] * Mz + cc[2]]);
-                }
+                for (int q = 0; q < 6; ++q) f[q] = __ldg(&phi[base + off[dim][q]]);
                 // corner at s0 (f[2]) and at s0 + 1 (f[3])
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
@@ -981,8 +983,8 @@ __device__ __forceinline__ float4 interp_one(float4 p, const float *__restrict__
                     // F indexed by (cx, cy, cz)
                     int idx[3];
                     idx[dim] = h;
-                    idx[(dim + 1) % 3] = u;
-                    idx[(dim + 2) % 3] = v;
+                    idx[d1] = u;
+                    idx[d2] = v;
                     F[idx[0]][idx[1]][idx[2]] = Fv;
                 }
             }
