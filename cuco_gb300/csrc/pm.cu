@@ -6,13 +6,15 @@
 //   k_deposit      CIC mass assignment (pm_periodic.c:97-132): each weight as
 //                  the integer w * 2^32, added with 64-bit integer atomics into
 //                  an M^3 grid, so the grid is the same whatever order the
-//                  particles land in (float atomics are not associative); the
-//                  particles arrive cell-sorted, so a warp's atomics hit a few
-//                  neighbouring mesh cells.
+//                  particles land in (float atomics are not associative).  One
+//                  box deposits in original particle order (it runs beside the
+//                  sort), the ensemble cell-sorted.
 //   k_fft_z_r2c    real->complex along z; its load converts the integer sums to
-//                  mass (one rounding).  Two real rows are packed as the real
-//                  and imaginary parts of one complex row, transformed together
-//                  and separated (X1 = (Z + conj Z_-k)/2, X2 = (Z - conj Z_-k)/2i).
+//                  mass (one rounding) and writes zero back, so the grid is
+//                  clean for the next deposit.  Two real rows are packed as the
+//                  real and imaginary parts of one complex row, transformed
+//                  together and separated (X1 = (Z + conj Z_-k)/2,
+//                  X2 = (Z - conj Z_-k)/2i).
 //   k_fft_axis     complex transforms along y, and along x fused with the
 //                  Green's-function multiply and the inverse x transform: the
 //                  x pass is the last forward and the first inverse pass, so the
@@ -23,9 +25,12 @@
 //                  the 8 CIC corners of each particle and the CIC interpolation
 //                  (pm_periodic.c:272-309), fused: the three force grids the
 //                  reference builds are never materialised.
-// All transforms are unnormalised with cuFFT's sign conventions; each 1D
-// transform is a shared-memory Stockham FFT over a batch of columns with
-// radix-4/2/3/5 stages (M = 2^a 3^b 5^c), twiddles from an FP64-built table.
+// All transforms are unnormalised with cuFFT's sign conventions.  Power-of-two
+// meshes up to 1024 use a two-level transform with the points in registers
+// (RegFFT; the one-box axis passes with their column batch fixed at compile
+// time, fft_axis_reg_fixed); other meshes M = 2^a 3^b 5^c use a shared-memory
+// Stockham FFT over a batch of columns with radix-4/2/3/5 stages.  Twiddles
+// come from an FP64-built table.
 // The Green's function factorises: smth(k) = -g(kx) g(ky) g(kz) / k^2 with
 // g(k) = exp(-k^2 (2 pi asmth / L)^2) / sinc(pi k / M)^4, built in FP64.
 #include <algorithm>
