@@ -20,9 +20,10 @@ the reference's run loop (run.c:11-20) calling the drop-in move_particles,
 compute_accelerations and advance_and_find_timesteps on a host P[] array, with
 every P[] copy between host and device inside the timed region.
 
-`--impl reference` times the reference's own CPU force path (oracle/_ref, where
-it was compiled) or the oracle's C restatement of it, with all host threads, on
-a bounded sample of each step.
+`--impl reference` times full steps of the same run on the CPU force path,
+with all host threads: the oracle's C restatement of the reference's CPU code
+(bit-exact with the reference's gravlist.cpp + pm_periodic.c built from their
+sources; those sources are not on every host, so the restatement is what runs).
 """
 from __future__ import annotations
 
@@ -398,13 +399,34 @@ def dist_barrier(world):
 
 # ----------------------------------------------------------------- CPU arm
 
-class CpuStep:
-    """The CPU force path on a bounded sample of one step of the workload: the
-    short range for a seeded 1/64 of the targets (scaled to all N; the
-    reference's per-target cost does not depend on which targets are taken),
-    the full PM on the whole mesh, and the drift/kick of all particles."""
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
-    FRAC = 64
+
+class CpuStep:
+    """Full steps of the workload on the CPU force path: the oracle's C
+    restatement of the reference's CPU code (bit-exact with the reference's own
+    gravlist.cpp + pm_periodic.c built from its sources, which is only built
+    where those sources are; a host without them runs the restatement).  A step
+    is the reference's run-loop body for one global step: drift + wrap
+    (predict.c:10-41), the short range of every particle on the reference's
+    PMGRID^3 cell grid (gravlist.cpp:117-146,195-338), the full PM
+    (pm_periodic.c:67-314, FP64 FFT in place of cuFFT) and the kick
+    (timestep.c:56-91)."""
 
     def __init__(self, nthreads: int):
         import oracle
@@ -412,39 +434,64 @@ class CpuStep:
         self.ic = make_ic()
         soft = softening_h(self.ic)
         self.p = oracle.reference_params(self.ic.boxsize, self.ic.mass, ics.G_INTERNAL, PM_GRID, soft)
-        n = self.ic.n
-        rng = np.random.default_rng(7)
-        self.sub = np.sort(rng.choice(n, n // self.FRAC, replace=False))
         self.port = oracle.Port()
         self.kind = "port"
         self.nthreads = nthreads
-        self.vel = self.ic.canonical_velocity()
-        self.sample = (f"one z=49 step: short range for {len(self.sub)} of {n} targets (x{self.FRAC}), "
-                       f"on the reference's PMGRID^3 = {PM_GRID}^3 cell grid (gravlist.cpp:117-146), "
-                       f"full {PM_GRID}^3 PM (pm_periodic.c:67-314, FP64 FFT), drift+kick of all; "
-                       f"{nthreads} threads")
+        _, self.drift, self.kick = schedule(self.ic)
+        self.reset()
+        self.sample = (f"full steps of the {N_SIDE}^3 workload from z=49: drift+wrap, short range of all "
+                       f"{self.ic.n} particles on the reference's {PM_GRID}^3 cell grid, full {PM_GRID}^3 PM, "
+                       f"kick; {nthreads} threads")
 
-    def rate(self):
-        ic, p = self.ic, self.p
+    def reset(self):
+        self.pos = self.ic.pos.astype(np.float32).copy()
+        self.vel = self.ic.canonical_velocity().astype(np.float32)
+        self.s = 0
+
+    def step(self, targets=None):
+        """One step; with `targets`, the short range of those targets only
+        (the drift, PM and kick stay whole).  Returns the phase times (s)."""
+        s = self.s % (NSTEPS_RUN + 1)
+        L = np.float32(self.ic.boxsize)
         t0 = time.perf_counter()
-        acc = self.port.pp_targets(ic.pos, self.sub, p, PM_GRID, self.nthreads)
-        t_pp = (time.perf_counter() - t0) * self.FRAC
-        t0 = time.perf_counter()
-        apm = self.port.pm(ic.pos, p, PM_GRID, self.nthreads)
-        t_pm = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        x = (ic.pos.astype(np.float64) + self.vel.astype(np.float64) * 1e-3).astype(np.float32)
-        v = (self.vel.astype(np.float64) + apm.astype(np.float64) * 1e-3).astype(np.float32)
-        t_dk = time.perf_counter() - t0
-        del x, v, acc
-        step = t_pp + t_pm + t_dk
-        return self.ic.n / step, {"pp_s_all_targets": t_pp, "pm_s": t_pm, "drift_kick_s": t_dk}
+        if self.drift[s]:
+            x = self.pos.astype(np.float64) + self.vel.astype(np.float64) * self.drift[s]
+            self.pos = np.mod(x, float(L)).astype(np.float32)
+            self.pos[self.pos >= L] = 0
+        t1 = time.perf_counter()
+        if targets is None:
+            acc = self.port.pp(self.pos, self.p, PM_GRID, self.nthreads)
+        else:
+            acc = self.port.pp_targets(self.pos, targets, self.p, PM_GRID, self.nthreads)
+        t2 = time.perf_counter()
+        apm = self.port.pm(self.pos, self.p, PM_GRID, self.nthreads)
+        t3 = time.perf_counter()
+        if targets is None:
+            self.vel = (self.vel.astype(np.float64) + (acc.astype(np.float64) + apm) * self.kick[s]).astype(
+                np.float32)
+        t4 = time.perf_counter()
+        self.s += 1
+        return {"drift_s": t1 - t0, "pp_s": t2 - t1, "pm_s": t3 - t2, "kick_s": t4 - t3, "total_s": t4 - t0}
 
 
-def cpu_sample_rate(nthreads: int):
+def cpu_single_core(frac=32):
+    """A 1-thread figure on a bounded sample: the short range of a seeded
+    1/frac of the targets (scaled by frac) plus the full PM and drift/kick."""
+    cs = CpuStep(1)
+    rng = np.random.default_rng(7)
+    sub = np.sort(rng.choice(cs.ic.n, cs.ic.n // frac, replace=False))
+    t = cs.step(sub)
+    total = t["drift_s"] + t["pp_s"] * frac + t["pm_s"] + t["kick_s"]
+    return {"value": cs.ic.n / total, "unit": "particle-updates/s", "cores": 1,
+            "sample": f"one z=49 step on 1 thread: short range of {len(sub)} of {cs.ic.n} targets (x{frac}), "
+                      f"full PM and drift/kick"}
+
+
+def cpu_sample_rate(nthreads: int, steps: int = 2):
+    """The GPU arm's cpu_baseline: `steps` full steps from z=49."""
     cs = CpuStep(nthreads)
-    v, info = cs.rate()
-    return v, cs.kind, cs.sample, info
+    t = sum(cs.step()["total_s"] for _ in range(steps))
+    return cs.ic.n * steps / t, cs.kind, f"{steps} " + cs.sample, {}
 
 
 def run_reference_arm(args, world, rank):
@@ -452,24 +499,27 @@ def run_reference_arm(args, world, rank):
         return
     nthreads = os.cpu_count() or 1
     cs = CpuStep(nthreads)
-    kind, sample = cs.kind, cs.sample
-    vals = []
-    info = {}
-    for k in range(args.warmup + args.steps):
-        v, info = cs.rate()
-        if k >= args.warmup:
-            vals.append(v)
-    val = float(len(vals) / np.sum(1.0 / np.array(vals)))
+    for _ in range(args.warmup):
+        cs.step()
+    cs.reset()  # the timed steps are steps 0..K-1 of the run, as on the GPU arm
+    phases = {}
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for k, v in cs.step().items():
+            phases[k] = phases.get(k, 0.0) + v
+    wall = time.perf_counter() - t0
+    val = cs.ic.n * args.steps / wall
     line = {
         "impl": "reference", "metric": "particle-updates/s", "value": val, "unit": "particle-updates/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * (N_SIDE ** 3) / val, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(),
-        "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": nthreads, "kind": kind,
-                         "sample": sample},
+        "cpu_baseline": {"value": val, "unit": "particle-updates/s", "cores": nthreads, "kind": cs.kind,
+                         "sample": f"{args.steps} " + cs.sample, "cpu_model": cpu_model()},
         "e2e": {"value": val, "unit": "particle-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "detail": info,
+        "phase_s_per_step": {k: v / args.steps for k, v in phases.items()},
+        "single_core": cpu_single_core(),
     }
     print(json.dumps(line), flush=True)
 
@@ -522,6 +572,23 @@ def run_gpu_arm(args, world, rank, local):
         box.step(drift[s % (NSTEPS_RUN + 1)], kick[s % (NSTEPS_RUN + 1)])
     lib.cuco_box_pair_count(box.h, ctypes.byref(pairs), 1)
     lib.cuco_box_count_pairs(box.h, 0)
+    # the clustered end of the run: steps NSTEPS_RUN-19..NSTEPS_RUN timed after
+    # an untimed run from the ICs up to them
+    late = None
+    if K < NSTEPS_RUN:
+        box.set_state(ic.pos, vel0)
+        first = NSTEPS_RUN + 1 - 20
+        for s in range(first):
+            box.step(drift[s], kick[s])
+        box.sync()
+        lib.cuco_box_timer(box.h, 0, None)
+        for s in range(first, NSTEPS_RUN + 1):
+            box.step(drift[s], kick[s])
+        lm = ctypes.c_float()
+        lib.cuco_box_timer(box.h, 1, ctypes.byref(lm))
+        t_late = dist_max(lm.value / 1e3, world)
+        late = {"steps": f"{first}..{NSTEPS_RUN} of 0..{NSTEPS_RUN} (z = {1 / a[first - 1] - 1:.2f} -> 0)",
+                "value": world * ic.n * 20 / t_late, "ms_per_step": 1e3 * t_late / 20}
     value = world * ic.n * K / t_total
     pp_ms = phase[6] / K
     pair_flops = 20.0 * pairs.value / K
@@ -544,6 +611,7 @@ def run_gpu_arm(args, world, rank, local):
                                    "peak = measured FMA throughput"},
         "phase_ms_per_step": phases,
         "pairs_per_step": pairs.value / K,
+        "late_window": late,
         "clocks": clk,
         "gpu_launches": launches,
     }
@@ -556,7 +624,8 @@ def run_gpu_arm(args, world, rank, local):
         try:
             v, kind, sample, info = cpu_sample_rate(os.cpu_count() or 1)
             line["cpu_baseline"] = {"value": v, "unit": "particle-updates/s",
-                                    "cores": os.cpu_count(), "kind": kind, "sample": sample}
+                                    "cores": os.cpu_count(), "kind": kind, "sample": sample,
+                                    "cpu_model": cpu_model()}
         except Exception as e:  # the CPU baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     if rank == 0:

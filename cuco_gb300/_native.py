@@ -92,6 +92,9 @@ SIGNATURES = {
     "cudaForceEvaluateShortrange": (None, [_P, _P, _P, _P, _P, _U, _U]),
     "radixSort": (None, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
     "radixSortKeysOnly": (None, [_P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
+    "radixSortFloatKeys": (None, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
+    "radixSortFloatKeysOnly": (None, [_P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
+    "cuco_radixsort_overflow": (None, [_U, _U]),
     "initDeviceParameters": (None, []),
     "checkCudaError": (None, [ctypes.c_char_p]),
     # host force / integrator names

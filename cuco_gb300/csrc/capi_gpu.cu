@@ -180,6 +180,64 @@ void radixSortKeysOnly(uint *keys, uint *tempKeys, uint *counters, uint *counter
                    "radixSortKeysOnly");
 }
 
+// radixSortFloatKeys / radixSortFloatKeysOnly: order-preserving map of
+// signed floats to unsigned keys and back (an involution pair: sign bit set
+// -> all bits inverted, else sign bit set).
+}  // extern "C"
+
+namespace {
+__global__ void k_float_to_key(uint32_t *__restrict__ k, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t u = k[i];
+        k[i] = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    }
+}
+__global__ void k_key_to_float(uint32_t *__restrict__ k, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const uint32_t u = k[i];
+        k[i] = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    }
+}
+void float_keys(float *keys, uint32_t n, bool to_key, const char *where) {
+    if (n == 0) return;
+    const unsigned blocks = (n + 255) / 256;
+    if (to_key)
+        k_float_to_key<<<blocks, 256>>>(reinterpret_cast<uint32_t *>(keys), n);
+    else
+        k_key_to_float<<<blocks, 256>>>(reinterpret_cast<uint32_t *>(keys), n);
+    capi_check(cudaGetLastError(), where);
+}
+}  // namespace
+
+extern "C" {
+
+void radixSortFloatKeys(float *keys, uint *values, float *tempKeys, uint *tempValues, uint *counters,
+                        uint *countersSum, uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
+                        uint keyBits, bool negativeKeys) {
+    if (negativeKeys) float_keys(keys, numElements, true, "radixSortFloatKeys");
+    radixSort(reinterpret_cast<uint *>(keys), values, reinterpret_cast<uint *>(tempKeys), tempValues, counters,
+              countersSum, blockOffsets, scanPlan, numElements, keyBits, false);
+    if (negativeKeys) float_keys(keys, numElements, false, "radixSortFloatKeys");
+}
+
+void radixSortFloatKeysOnly(float *keys, float *tempKeys, uint *counters, uint *countersSum,
+                            uint *blockOffsets, CUDPPHandle scanPlan, uint numElements, uint keyBits,
+                            bool negativeKeys) {
+    if (negativeKeys) float_keys(keys, numElements, true, "radixSortFloatKeysOnly");
+    radixSortKeysOnly(reinterpret_cast<uint *>(keys), reinterpret_cast<uint *>(tempKeys), counters, countersSum,
+                      blockOffsets, scanPlan, numElements, keyBits, false);
+    if (negativeKeys) float_keys(keys, numElements, false, "radixSortFloatKeysOnly");
+}
+
+void cuco_radixsort_overflow(uint numElements, uint maxElements) {
+    char msg[128];
+    snprintf(msg, sizeof msg, "%u elements exceed the %u this RadixSort was created for", numElements,
+             maxElements);
+    capi_fail("RadixSort::sort", msg);
+}
+
 void initDeviceParameters(void) {}
 
 void checkCudaError(const char *msg) {

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "radixsort.h"
 
 extern "C" {
 __attribute__((weak)) unsigned int NumPart;
@@ -48,10 +49,12 @@ __attribute__((weak)) unsigned int *dGridParticleHash;
 __attribute__((weak)) unsigned int *dGridParticleIndex;
 __attribute__((weak)) unsigned int *dCellStart;
 __attribute__((weak)) unsigned int *dCellEnd;
-/* `RadixSort *sorter` (gravlist.cu:20); the drop-in sorts inside
- * gravity_linklist_cuda and leaves it null. */
-void *sorter;
 }
+
+/* gravlist.cu:20.  linklist_init creates it as gravlist.cpp:98 does, so a host
+ * that keeps the reference's gravlist.cpp finds it; the drop-in's own
+ * gravity_linklist_cuda sorts inside the engine and does not use it. */
+RadixSort *sorter;
 
 namespace cuco {
 void capi_set_grid(int G);
@@ -541,6 +544,8 @@ void linklist_init(void) {
     sim.G = (float)All.G;
     numParticles = NumPart;
     numGridCells = (unsigned)G * G * G;
+    delete sorter;
+    sorter = new RadixSort(numParticles);
     if (s.h <= 0) set_softenings();
     ensure_box();
     float4 *pos, *vel, *app, *apm, *spos;

@@ -25,7 +25,12 @@
 //     name is a host-side stand-in, not a device address).  The first call on
 //     each device, with that device current, looks the address up with
 //     cudaGetSymbolAddress and caches it; make that first call before
-//     capturing any work on that device into a stream capture.
+//     capturing any work on that device into a stream capture.  The cached
+//     address lives as long as the device's context: a cudaDeviceReset after
+//     the first call is not supported (the address would be stale);
+//   * keys must be below 2^key_bits: the passes split key_bits into equal
+//     digits of 4 to 8 bits, which may cover a few bits above key_bits, and
+//     bits set there would take part in the order.
 #include <mutex>
 
 #include "common.cuh"

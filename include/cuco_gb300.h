@@ -84,10 +84,14 @@ void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridP
                                  uint numCells);
 
 /* radixsort.h:47-58 / radixsort.cu:1048-1145.  Stable LSD sort of
- * (keys, values) by the low keyBits bits, in place.  tempKeys/tempValues hold
- * numElements entries each; `counters` holds at least 32*ceil(n/1024) entries
- * (the reference RadixSort's allocation, radixsort.h:271-275) and is used as
- * the per-tile digit histogram; countersSum, blockOffsets and scanPlan are not
+ * (keys, values) by the low keyBits bits, in place.  Every key must be below
+ * 2^keyBits: the passes split keyBits into equal digits of 4 to 6 bits
+ * (18 bits: three 6-bit passes; 1 bit: one 4-bit pass), which may cover a few
+ * bits above keyBits, and bits set there would take part in the order (the
+ * reference's CUDPP sort makes the same assumption).  tempKeys/tempValues hold numElements
+ * entries each; `counters` holds at least 32*ceil(n/1024) entries (the
+ * reference RadixSort's allocation, radixsort.h:271-275) and is used as the
+ * per-tile digit histogram; countersSum, blockOffsets and scanPlan are not
  * used.  flipBits must be false. */
 void radixSort(uint *keys, uint *values, uint *tempKeys, uint *tempValues, uint *counters,
                uint *countersSum, uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
@@ -96,6 +100,22 @@ void radixSort(uint *keys, uint *values, uint *tempKeys, uint *tempValues, uint 
 void radixSortKeysOnly(uint *keys, uint *tempKeys, uint *counters, uint *countersSum,
                        uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
                        uint keyBits, bool flipBits);
+/* radixsort.h:60-71, 83-92: float keys.  With negativeKeys the keys are
+ * mapped to order-preserving unsigned integers before the sort (sign bit set:
+ * all bits inverted; else the sign bit set) and mapped back after it; without
+ * it non-negative floats already order as their bit patterns.  The sort is
+ * radixSort's over the low keyBits bits of the mapped keys (32 for a full
+ * float order). */
+void radixSortFloatKeys(float *keys, uint *values, float *tempKeys, uint *tempValues, uint *counters,
+                        uint *countersSum, uint *blockOffsets, CUDPPHandle scanPlan, uint numElements,
+                        uint keyBits, bool negativeKeys);
+void radixSortFloatKeysOnly(float *keys, float *tempKeys, uint *counters, uint *countersSum,
+                            uint *blockOffsets, CUDPPHandle scanPlan, uint numElements, uint keyBits,
+                            bool negativeKeys);
+/* No counterpart in the reference (whose RadixSort::sort does not check its
+ * capacity): RadixSort::sort calls this, which prints a message and exits,
+ * when asked to sort more elements than the object was created for. */
+void cuco_radixsort_overflow(uint numElements, uint maxElements);
 /* radixsort.h:47: no device-specific tuning is needed on sm_103a; kept for linkage. */
 void initDeviceParameters(void);
 /* radixsort.h:46: aborts with `msg` if a CUDA error is pending. */
@@ -344,8 +364,10 @@ cuco_status_t cuco_ensemble_footprint(const cuco_config_t *boxes, int nbox, uint
  * rejected with CUCO_ERR_INVALID); 8.25 MiB held on every GPU that loads the
  * library, until exit.  All calls on a device share that array, so calls that
  * overlap on the GPU race; order them on one stream.  The first call on a
- * device (with it current) looks up the array's device address; make it
- * before any stream capture on that device.  values may be NULL (keys only);
+ * device (with it current) looks up the array's device address and keeps it
+ * for the life of the device's context; make it before any stream capture on
+ * that device, and do not reset the device afterwards.  Every key must be
+ * below 2^key_bits (as for radixSort).  values may be NULL (keys only);
  * stream is a cudaStream_t (NULL: legacy default stream). */
 cuco_status_t cuco_radix_sort_noalloc(uint32_t *keys, uint32_t *values, uint32_t n,
                                       uint32_t key_bits, void *stream);

@@ -23,7 +23,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_SOURCES = os.environ.get("CUCO_REFERENCE_DIR", "/root/reference")
+
+
+def reference_dir() -> str:
+    """Where the reference's sources lie: $CUCO_REFERENCE_DIR, else the
+    location the oracle recipe (oracle/Makefile, REF) names."""
+    env = os.environ.get("CUCO_REFERENCE_DIR")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
 
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
@@ -39,14 +49,15 @@ def build_port() -> str:
 
 
 def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REFERENCE_SOURCES, "gravlist.cpp"))
+    d = reference_dir()
+    return bool(d) and os.path.isfile(os.path.join(d, "gravlist.cpp"))
 
 
 def build_reference(pmgrids=(32, 64, 128, 256)) -> list[str]:
     """Compile the reference's CPU path (one library per PM mesh size)."""
     if not reference_available():
-        raise FileNotFoundError("reference sources not present at " + REFERENCE_SOURCES)
-    r = subprocess.run(["make", "-s", "-j4", "-C", HERE, "ref", "REF=" + REFERENCE_SOURCES,
+        raise FileNotFoundError("reference sources not present at " + repr(reference_dir()))
+    r = subprocess.run(["make", "-s", "-j4", "-C", HERE, "ref", "REF=" + reference_dir(),
                         "PMGRIDS=" + " ".join(str(m) for m in pmgrids)], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("reference oracle build failed:\n" + r.stdout + r.stderr)
@@ -96,9 +107,9 @@ class Port:
         lib.op_table_factor.argtypes = [_f64p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_int, ctypes.c_int]
         lib.op_table_factor.restype = ctypes.c_double
-        lib.op_ewald.argtypes = [_f64p, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
-                                 ctypes.c_double, ctypes.c_double, _f64p, ctypes.c_int64,
-                                 ctypes.c_int, _f64p]
+        lib.op_ewald_alpha.argtypes = [_f64p, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double, ctypes.c_double, _f64p, ctypes.c_int64,
+                                       ctypes.c_int, ctypes.c_double, _f64p]
         self.lib = lib
 
     def keys(self, pos, gridfac, G):
@@ -162,12 +173,14 @@ class Port:
         table = np.ascontiguousarray(table, dtype=np.float64)
         return self.lib.op_table_factor(table, table.size, loga0, loga1, tbi, t0, t1)
 
-    def ewald(self, src, mass, G, boxsize, softening_h, targets, nthreads=1):
+    def ewald(self, src, mass, G, boxsize, softening_h, targets, nthreads=1, alpha_l=0.0):
+        """FP64 Ewald-summed periodic force on `targets` from all `src`
+        (alpha_l = alpha * L of the split; 0 picks the cheapest)."""
         src = np.ascontiguousarray(src, dtype=np.float64)
         tg = np.ascontiguousarray(targets, dtype=np.float64)
         acc = np.empty_like(tg)
-        self.lib.op_ewald(src.reshape(-1), src.shape[0], mass, G, boxsize, softening_h,
-                          tg.reshape(-1), tg.shape[0], nthreads, acc.reshape(-1))
+        self.lib.op_ewald_alpha(src.reshape(-1), src.shape[0], mass, G, boxsize, softening_h,
+                                tg.reshape(-1), tg.shape[0], nthreads, alpha_l, acc.reshape(-1))
         return acc
 
 

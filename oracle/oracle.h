@@ -82,6 +82,14 @@ double op_table_factor(const double *table, int n, double loga0, double loga1,
 void op_ewald(const double *src, int64_t n, double mass, double G, double boxsize,
               double softening, const double *targets, int64_t nt, int nthreads, double *acc);
 
+/* op_ewald with the split parameter alpha = alpha_l / boxsize given (>= 11.5,
+ * so the real-space cut 5.5/alpha stays below L/2); alpha_l <= 0 picks the one
+ * that balances the real and Fourier work for n sources and nt targets.  The
+ * result does not depend on alpha beyond the ~1e-12 truncation of either sum. */
+void op_ewald_alpha(const double *src, int64_t n, double mass, double G, double boxsize,
+                    double softening, const double *targets, int64_t nt, int nthreads,
+                    double alpha_l, double *acc);
+
 #ifdef __cplusplus
 }
 #endif

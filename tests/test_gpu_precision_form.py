@@ -67,3 +67,16 @@ def test_forms_vs_fp64_path(port, states, when):
         print(f"{when} {name:9s}: pp {e_pp:.2e}  pm {e_pm:.2e}  total {e_tot:.2e}")
     assert max(errs["plain"]) < 1e-4
     assert max(errs["precision"]) < 1e-3
+
+
+@pytest.mark.parametrize("when", ["z49", "z0"])
+def test_forms_vs_ewald(port, states, when):
+    """Total force of both forms and of the reference method (the floor)
+    against the FP64 Ewald oracle on the same 4096-particle subsample."""
+    from test_gpu_ewald import check_against_floor, ewald_table
+    ic, soft, st = states
+    sub = np.sort(np.random.default_rng(4096).choice(ic.n, NSUB, replace=False))
+    t = ewald_table(port, st[when], ic, soft, M, sub)
+    print(f"EWALD 128^3 M=256 {when}: floor {t['floor']:.3e} plain {t['plain']:.3e} "
+          f"precision {t['precision']:.3e}")
+    check_against_floor(t)
