@@ -95,6 +95,10 @@ SIGNATURES = {
     "radixSortFloatKeys": (None, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
     "radixSortFloatKeysOnly": (None, [_P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
     "cuco_radixsort_overflow": (None, [_U, _U]),
+    "read_ic": (None, [ctypes.c_char_p]),
+    "savepositions": (None, [_I]),
+    "cuco_box_load_snapshot": (_I, [_P, ctypes.c_char_p, _I, _P]),
+    "cuco_box_save_snapshot": (_I, [_P, ctypes.c_char_p, _P]),
     "initDeviceParameters": (None, []),
     "checkCudaError": (None, [ctypes.c_char_p]),
     # host force / integrator names

@@ -488,6 +488,55 @@ void cuco_dropin_configure(int pmgrid, int cellgrid) {
     capi_set_grid(cell_grid());
 }
 
+// read_ic.c:9-45: HEADER then PARTICLE[NumPart] into the globals; exits on a
+// missing or short file as the reference does (it does not check fread).
+void read_ic(char *fname) {
+    FILE *fp = fopen(fname, "rb");
+    if (!fp) {
+        printf("Cannot open initial condition file %s!\n", fname);
+        exit(1);
+    }
+    HEADER h;
+    if (fread(&h, sizeof(HEADER), 1, fp) != 1 || h.NumPart < 0) {
+        printf("Initial condition file %s has no valid header!\n", fname);
+        exit(1);
+    }
+    header = h;
+    NumPart = (unsigned)h.NumPart;
+    P = (PARTICLE *)malloc(sizeof(PARTICLE) * (NumPart ? NumPart : 1));
+    if (!P || fread(P, sizeof(PARTICLE), NumPart, fp) != NumPart) {
+        printf("Initial condition file %s ends before its %u particles!\n", fname, NumPart);
+        exit(1);
+    }
+    fclose(fp);
+    All.NumPart = (int)NumPart;
+    All.BoxSize = header.BoxSize;
+    All.Mass = header.Mass;
+    printf("IC file %s: %u particles, box %g kpc/h, mass %g x 1e10 Msun/h, z = %g\n", fname, NumPart,
+           header.BoxSize, header.Mass, header.Redshift);
+}
+
+// io.c:9-40: <OutputDir>/<SnapshotFileBase>_<num>.cuco with the header's
+// time and redshift from All.Time.
+void savepositions(int num) {
+    char path[2 * CUCO_MAXLEN_FILENAME + 32];
+    snprintf(path, sizeof path, "%s/%s_%d.cuco", All.OutputDir, All.SnapshotFileBase, num);
+    FILE *fp = fopen(path, "wb");
+    if (!fp) {
+        printf("Cannot open snapshot file %d!\n", num);
+        exit(1);
+    }
+    HEADER h = header;
+    h.Time = All.Time;
+    h.Redshift = 1 / All.Time - 1;
+    if (fwrite(&h, sizeof(HEADER), 1, fp) != 1 || fwrite(P, sizeof(PARTICLE), NumPart, fp) != NumPart) {
+        printf("Cannot write snapshot file %d!\n", num);
+        exit(1);
+    }
+    fclose(fp);
+    printf("write output file %d: a = %g z = %g\n", num, All.Time, h.Redshift);
+}
+
 void pm_init_periodic(void) {
     All.Asmth = (float)(CUCO_ASMTH * (double)All.BoxSize / ds().pmgrid);
     All.Rcut = (float)(CUCO_RCUT * (double)All.Asmth);

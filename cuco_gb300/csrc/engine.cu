@@ -12,6 +12,7 @@
 // the permutation the sort produces is the reference's (stable sort of the keys
 // of P[] in index order).
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -879,6 +880,148 @@ __attribute__((visibility("hidden"))) cuco_status_t cuco_box_internal_arrays(
 
 __attribute__((visibility("hidden"))) cuco_status_t cuco_box_mark_state(cuco_box_t *b) {
     b->has_state = true;
+    return CUCO_OK;
+}
+
+}  // extern "C"
+
+// ---- .cuco snapshot / initial-conditions files (read_ic.c:9-45, io.c:9-40):
+// HEADER (32 bytes) then PARTICLE[NumPart] (60 bytes each), raw, host order.
+namespace snapshot_io {
+
+__global__ void k_records_to_state(const PARTICLE *__restrict__ rec, uint32_t n, float vscale,
+                                   float *__restrict__ pos3, float *__restrict__ vel3) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const PARTICLE r = rec[i];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        pos3[3 * (size_t)i + d] = r.Pos[d];
+        vel3[3 * (size_t)i + d] = vscale == 1.0f ? r.Vel[d] : __fmul_rn(r.Vel[d], vscale);
+    }
+}
+
+__global__ void k_state_to_records(const float *__restrict__ pos3, const float *__restrict__ vel3,
+                                   const float *__restrict__ app3, const float *__restrict__ apm3, float mass,
+                                   uint32_t n, PARTICLE *__restrict__ rec) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    PARTICLE r;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r.Pos[d] = pos3[3 * (size_t)i + d];
+        r.Vel[d] = vel3[3 * (size_t)i + d];
+        r.GravAccel[d] = app3[3 * (size_t)i + d];
+        r.GravPM[d] = apm3[3 * (size_t)i + d];
+    }
+    r.Mass = mass;
+    r.Ti_endstep = 0;
+    r.Ti_begstep = 0;
+    rec[i] = r;
+}
+
+struct DeviceScratch {
+    void *p[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    ~DeviceScratch() {
+        for (void *q : p) cudaFree(q);
+    }
+};
+
+struct HostFile {
+    FILE *f = nullptr;
+    ~HostFile() {
+        if (f) fclose(f);
+    }
+};
+
+}  // namespace snapshot_io
+
+using namespace snapshot_io;
+
+extern "C" {
+
+cuco_status_t cuco_box_load_snapshot(cuco_box_t *b, const char *path, int initial_conditions, HEADER *header) {
+    if (!b || !path) {
+        set_error("cuco_box_load_snapshot: null argument");
+        return CUCO_ERR_INVALID;
+    }
+    HostFile hf;
+    hf.f = fopen(path, "rb");
+    if (!hf.f) {
+        set_error(std::string("cuco_box_load_snapshot: cannot open ") + path);
+        return CUCO_ERR_INVALID;
+    }
+    HEADER h;
+    if (fread(&h, sizeof h, 1, hf.f) != 1) {
+        set_error("cuco_box_load_snapshot: short header");
+        return CUCO_ERR_INVALID;
+    }
+    if (h.NumPart < 0 || (int64_t)h.NumPart != b->n) {
+        set_error("cuco_box_load_snapshot: the file holds " + std::to_string(h.NumPart) +
+                  " particles, the box " + std::to_string(b->n));
+        return CUCO_ERR_INVALID;
+    }
+    const size_t n = (size_t)b->n;
+    std::vector<PARTICLE> rec(n);
+    if (n && fread(rec.data(), sizeof(PARTICLE), n, hf.f) != n) {
+        set_error("cuco_box_load_snapshot: the file ends before its " + std::to_string(n) + " particles");
+        return CUCO_ERR_INVALID;
+    }
+    if (header) *header = h;
+    if (!n) return CUCO_OK;
+    // init.c:30 scales an IC file's velocities by a^(3/2) into the
+    // integrator's variable; a snapshot stores that variable already
+    const float vscale = initial_conditions ? (float)(sqrt((double)h.Time) * (double)h.Time) : 1.0f;
+    DeviceScratch ds;
+    CUCO_TRY_CUDA(cudaMalloc(&ds.p[0], sizeof(PARTICLE) * n));
+    CUCO_TRY_CUDA(cudaMalloc(&ds.p[1], sizeof(float) * 3 * n));
+    CUCO_TRY_CUDA(cudaMalloc(&ds.p[2], sizeof(float) * 3 * n));
+    CUCO_TRY_CUDA(cudaMemcpyAsync(ds.p[0], rec.data(), sizeof(PARTICLE) * n, cudaMemcpyHostToDevice, b->stream));
+    k_records_to_state<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(
+        static_cast<const PARTICLE *>(ds.p[0]), (uint32_t)n, vscale, static_cast<float *>(ds.p[1]),
+        static_cast<float *>(ds.p[2]));
+    CUCO_TRY_CUDA(cudaGetLastError());
+    CUCO_TRY(cuco_box_set_state(b, static_cast<float *>(ds.p[1]), static_cast<float *>(ds.p[2]), 1));
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    return CUCO_OK;
+}
+
+cuco_status_t cuco_box_save_snapshot(cuco_box_t *b, const char *path, const HEADER *header) {
+    if (!b || !path || !header) {
+        set_error("cuco_box_save_snapshot: null argument");
+        return CUCO_ERR_INVALID;
+    }
+    if (!b->has_state) {
+        set_error("cuco_box_save_snapshot: the box has no state");
+        return CUCO_ERR_STATE;
+    }
+    const size_t n = (size_t)b->n;
+    HEADER h = *header;
+    h.NumPart = (int)b->n;
+    std::vector<PARTICLE> rec(n);
+    if (n) {
+        DeviceScratch ds;
+        CUCO_TRY_CUDA(cudaMalloc(&ds.p[0], sizeof(PARTICLE) * n));
+        for (int k = 1; k <= 4; ++k) CUCO_TRY_CUDA(cudaMalloc(&ds.p[k], sizeof(float) * 3 * n));
+        float *f[4] = {static_cast<float *>(ds.p[1]), static_cast<float *>(ds.p[2]), static_cast<float *>(ds.p[3]),
+                       static_cast<float *>(ds.p[4])};
+        CUCO_TRY(cuco_box_get_state(b, f[0], f[1], f[2], f[3], 1));
+        k_state_to_records<<<(unsigned)((n + 255) / 256), 256, 0, b->stream>>>(
+            f[0], f[1], f[2], f[3], header->Mass, (uint32_t)n, static_cast<PARTICLE *>(ds.p[0]));
+        CUCO_TRY_CUDA(cudaGetLastError());
+        CUCO_TRY_CUDA(cudaMemcpyAsync(rec.data(), ds.p[0], sizeof(PARTICLE) * n, cudaMemcpyDeviceToHost, b->stream));
+        CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    }
+    HostFile hf;
+    hf.f = fopen(path, "wb");
+    if (!hf.f) {
+        set_error(std::string("cuco_box_save_snapshot: cannot create ") + path);
+        return CUCO_ERR_INVALID;
+    }
+    if (fwrite(&h, sizeof h, 1, hf.f) != 1 || (n && fwrite(rec.data(), sizeof(PARTICLE), n, hf.f) != n)) {
+        set_error(std::string("cuco_box_save_snapshot: write failed on ") + path);
+        return CUCO_ERR_INVALID;
+    }
     return CUCO_OK;
 }
 

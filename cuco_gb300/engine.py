@@ -16,7 +16,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native
-from ._native import CucoConfig, check, ptr
+from ._native import CucoConfig, Header, check, ptr
 
 HUBBLE = 0.1  # H0 in internal units, km/s per kpc/h (begrun.c:70)
 ASMTH = 1.25  # allvars.h:24
@@ -161,6 +161,18 @@ class Box:
         out = [np.empty((self.n, 3), dtype=np.float32) for _ in range(4)]
         check(self.lib.cuco_box_get_state(self.h, *[ptr(o) for o in out], 0), "cuco_box_get_state")
         return out  # pos, vel, acc_pp, acc_pm
+
+    def load_snapshot(self, path: str, initial_conditions: bool = True) -> Header:
+        """State from a .cuco IC or snapshot file (read_ic.c:9-45); returns its header."""
+        hdr = Header()
+        check(self.lib.cuco_box_load_snapshot(self.h, path.encode(), int(initial_conditions),
+                                              ctypes.byref(hdr)), "cuco_box_load_snapshot")
+        return hdr
+
+    def save_snapshot(self, path: str, header: Header):
+        """The state and last forces as a .cuco snapshot (io.c:9-40)."""
+        check(self.lib.cuco_box_save_snapshot(self.h, path.encode(), ctypes.byref(header)),
+              "cuco_box_save_snapshot")
 
     def set_softening(self, h: float):
         check(self.lib.cuco_box_set_softening(self.h, h), "cuco_box_set_softening")

@@ -170,6 +170,13 @@ int cuco_dropin_min_ti_endstep(void);
  * coherently, e.g. a Grace host over NVLink-C2C, and CUCO_DROPIN_MIRROR is not
  * "1"); 0 when each call copies P[] whole to a device mirror and back. */
 int cuco_dropin_host_access(void);
+/* read_ic.c:9-45: HEADER then PARTICLE[NumPart] of an IC file into header, P
+ * (malloc'ed here), NumPart and All.NumPart/BoxSize/Mass; exits on a missing
+ * or short file. */
+void read_ic(char *fname);
+/* io.c:9-40: header (with Time = All.Time, Redshift = 1/All.Time - 1) and
+ * P[0..NumPart) to <All.OutputDir>/<All.SnapshotFileBase>_<num>.cuco. */
+void savepositions(int num);
 /* driftfac.c:14-42 (tables integrated in FP64; the float tables DriftTable /
  * GravKickTable are filled too) */
 void init_drift_table(void);
@@ -238,6 +245,21 @@ cuco_status_t cuco_box_get_state(cuco_box_t *box, float *pos, float *vel, float 
 cuco_status_t cuco_box_set_state_fixed(cuco_box_t *box, const uint32_t *pos, const float *vel,
                                        int on_device);
 cuco_status_t cuco_box_get_state_fixed(cuco_box_t *box, uint32_t *pos, int on_device);
+/* The reference's IC/snapshot file format (read_ic.c:9-45, io.c:9-40): HEADER
+ * then PARTICLE[NumPart], raw.  load: the file's NumPart must equal the box's
+ * n; positions and velocities become the box's state (with
+ * initial_conditions != 0 the velocities are scaled by Time^(3/2) into the
+ * integrator's variable, as init.c:30 does for an IC file; a snapshot stores
+ * that variable already); the header is returned when `header` is not NULL.
+ * save: writes `header` (NumPart set to n) and one record per particle with
+ * Pos, Vel, Mass = header->Mass, GravAccel = the last short-range force,
+ * GravPM = the last PM force, Ti_endstep = Ti_begstep = 0 (the engine keeps
+ * no individual timeline).  Both go through device memory they allocate for
+ * the call. */
+cuco_status_t cuco_box_load_snapshot(cuco_box_t *box, const char *path, int initial_conditions,
+                                     HEADER *header);
+cuco_status_t cuco_box_save_snapshot(cuco_box_t *box, const char *path, const HEADER *header);
+
 /* Spline softening length h (changes with time when softening is physical). */
 cuco_status_t cuco_box_set_softening(cuco_box_t *box, float h);
 

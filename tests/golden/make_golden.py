@@ -11,6 +11,8 @@ Zel'dovich box (L = 50 Mpc/h, z = 49, PMGRID = 32) and stores:
   run_*           state after 3 passes of the reference run loop with the CPU
                   short range (run.c:11-20, accel.c, timestep.c)
   asmth, rcut, G, softening, mass, boxsize, timebase_interval: the constants
+and, in ref_n16_pm32_mixed.npz, eight passes of the run loop on a box whose
+particles take different individual timesteps (see mixed() below).
 The keys/permutation fixture uses the oracle's restatement of calcHashD plus
 a stable sort (the reference computes keys only on the GPU, which does not
 build on CUDA 13); it is pinned by tests/test_oracle_ref.py.
@@ -67,6 +69,33 @@ def main():
                run_pm_ti=pm, run_ti_current=np.array(ti))
     np.savez_compressed(os.path.join(HERE, "ref_n16_pm32.npz"), **out)
     print("wrote", os.path.join(HERE, "ref_n16_pm32.npz"), "Ti:", ti, "steps:", np.unique(e - b))
+    mixed()
+
+
+# A box clustered enough (z = 4) and a tolerance tight enough (ErrTolIntAccuracy
+# = 0.005) that the particles take three different power-of-two steps below the
+# PM step: eight passes of the run loop exercise the individual timesteps
+# (timestep.c:11-94) - which particles are kicked, when the PM kick comes, and
+# the drift of inactive particles between their kicks.
+MIXED_Z, MIXED_ERRTOL, MIXED_SEED, MIXED_PASSES = 4.0, 0.005, 7, 8
+
+
+def mixed():
+    ic = ics.zeldovich(N_SIDE, BOX_MPC, MIXED_Z, MIXED_SEED)
+    eps = float(np.float32(0.03 * ic.boxsize / N_SIDE))
+    ref = oracle.Reference(PMGRID)
+    ref.begrun(ic, a_max=1.0, soft_comoving=eps, max_dloga=0.03, errtol=MIXED_ERRTOL)
+    pos0, vel0, _, _ = ref.get()
+    ti = [ref.step(1) for _ in range(MIXED_PASSES)]
+    rp, rv, rpp, rpm = ref.get()
+    b, e, pm = ref.timeline()
+    out = dict(pos=pos0, vel=vel0, mass=ic.mass, boxsize=ic.boxsize, a_begin=np.float32(ic.a), pmgrid=PMGRID,
+               eps=eps, errtol=MIXED_ERRTOL, max_dloga=0.03, run_pos=rp, run_vel=rv, run_acc_pp=rpp,
+               run_acc_pm=rpm, run_ti_beg=b, run_ti_end=e, run_pm_ti=pm, run_ti_current=np.array(ti))
+    path = os.path.join(HERE, "ref_n16_pm32_mixed.npz")
+    np.savez_compressed(path, **out)
+    steps, counts = np.unique(e - b, return_counts=True)
+    print("wrote", path, "Ti:", ti, "steps:", dict(zip(steps.tolist(), counts.tolist())))
 
 
 if __name__ == "__main__":

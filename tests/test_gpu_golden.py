@@ -60,3 +60,39 @@ def test_dropin_run_loop_vs_reference(gold, mirror, monkeypatch):
     dx = np.abs(d.field("Pos") - gold["run_pos"])
     dx = np.minimum(dx, float(gold["boxsize"]) - dx)
     assert dx.max() < 1e-4 * float(gold["boxsize"])
+
+
+@pytest.fixture(scope="module")
+def gold_mixed():
+    return dict(np.load(os.path.join(os.path.dirname(FIX), "ref_n16_pm32_mixed.npz")))
+
+
+def test_dropin_run_loop_individual_timesteps(gold_mixed):
+    """Eight passes of the reference's run loop on a box whose particles take
+    three different power-of-two steps (timestep.c:11-94): the integer
+    timeline of every particle and of the PM step, the velocities (kicked
+    only when a particle is active), the positions (drifted every pass), and
+    the short-range force of the particles active at the last pass.  The
+    reference's CPU loop computes the short range for active particles only
+    (gravlist.cpp:208) and the GPU path for all (as gravity_linklist_cuda
+    does); an inactive particle's stored force is not used before it is
+    recomputed, so only the active ones are compared."""
+    g = gold_mixed
+    M = int(g["pmgrid"])
+    d = DropIn(g["pos"], g["vel"], float(g["mass"]), float(g["boxsize"]), float(g["a_begin"]), M, 0,
+               float(g["eps"]), errtol=float(g["errtol"]), max_dloga=float(g["max_dloga"]))
+    tis = [d.run_pass() for _ in range(len(g["run_ti_current"]))]
+    assert tis == list(g["run_ti_current"])
+    beg, end = d.timeline()
+    steps = np.unique(g["run_ti_end"] - g["run_ti_beg"])
+    assert steps.size >= 3  # the fixture really mixes step sizes
+    assert np.array_equal(beg, g["run_ti_beg"]) and np.array_equal(end, g["run_ti_end"])
+    assert [d.All.PM_Ti_begstep, d.All.PM_Ti_endstep, d.All.Ti_Current] == list(g["run_pm_ti"])
+    active = beg == tis[-1]
+    assert 0 < active.sum() < d.n
+    assert rms_rel(d.field("GravAccel")[active], g["run_acc_pp"][active]) < 1e-4
+    assert rms_rel(d.field("GravPM"), g["run_acc_pm"]) < 1e-4
+    assert rms_rel(d.field("Vel"), g["run_vel"]) < 1e-4
+    dx = np.abs(d.field("Pos") - g["run_pos"])
+    dx = np.minimum(dx, float(g["boxsize"]) - dx)
+    assert dx.max() < 1e-4 * float(g["boxsize"])
