@@ -9,8 +9,10 @@
 // is one launch over all boxes' meshes (a per-CTA (box, block) map), and the
 // short range is one launch over all boxes' segments (a segment prefix
 // table).  The per-step factors of every box (drift, kicks) sit in a small
-// device array refreshed from pinned host memory at the start of the step, so
-// a whole step is one CUDA graph.
+// device array refreshed from pinned host memory by a copy queued before each
+// step, so the rest of the step is one CUDA graph; the pinned factors have two
+// slots used in turn, and the host waits only for the copy of two steps back,
+// never for the step in flight.
 //
 // Autotuning.  A box's short-range cell grid G (cell_grid = 0) and its FFT
 // batching (columns per CTA) are chosen by timing candidates on a scratch box
@@ -300,8 +302,16 @@ struct cuco_ensemble {
     uint2 *d_mapz = nullptr, *d_mapa = nullptr;
     char *d_sr = nullptr;
     double2 *d_kicks = nullptr;
-    StepFactors *d_factors = nullptr, *h_factors = nullptr;  // h_factors: pinned
-    double2 *h_kicks = nullptr;                               // pinned
+    StepFactors *d_factors = nullptr;
+    // per-step factors in pinned host memory, two slots used in turn: a step
+    // fills one slot while the copy from the other may still be queued, and
+    // waits only for the copy of two steps back (up_done), so the host
+    // prepares step t+1 while the GPU runs step t
+    StepFactors *h_factors[2] = {nullptr, nullptr};
+    double2 *h_kicks[2] = {nullptr, nullptr};
+    cudaEvent_t up_done[2] = {nullptr, nullptr};
+    bool up_pending[2] = {false, false};
+    int slot = 0;
     PMMulti pm{};
     uint32_t segments = 0;
     size_t sr_smem = 0;
@@ -319,7 +329,8 @@ struct cuco_ensemble {
     // capacities (elements) of the grow-only arrays
     size_t cap_n = 0, cap_hist = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
            cap_green = 0, cap_tw = 0, cap_table = 0, cap_pbeg = 0, cap_segbase = 0, cap_drift = 0, cap_pm = 0,
-           cap_kicks = 0, cap_factors = 0, cap_counter = 0, cap_sr = 0, cap_hfactors = 0, cap_hkicks = 0,
+           cap_kicks = 0, cap_factors = 0, cap_counter = 0, cap_sr = 0, cap_hfactors[2] = {0, 0},
+           cap_hkicks[2] = {0, 0},
            cap_mapz = 0, cap_mapa = 0, cap_heavy = 0, cap_segnt = 0, cap_ctl = 0, cap_cellsl = 0;
     // the short range's work-plan scratch
     uint2 *sr_heavy = nullptr;
@@ -369,11 +380,15 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
     return CUCO_OK;
 }
 
-cuco_status_t upload_factors(cuco_ensemble *e) {
-    CUCO_TRY_CUDA(cudaMemcpyAsync(e->d_factors, e->h_factors, sizeof(StepFactors) * e->nbox,
+// The factors of slot k to the device, stream-ordered before the step that
+// reads them; up_done[k] marks when slot k may be written again.
+cuco_status_t upload_factors(cuco_ensemble *e, int k) {
+    CUCO_TRY_CUDA(cudaMemcpyAsync(e->d_factors, e->h_factors[k], sizeof(StepFactors) * e->nbox,
                                   cudaMemcpyHostToDevice, e->stream));
-    CUCO_TRY_CUDA(cudaMemcpyAsync(e->d_kicks, e->h_kicks, sizeof(double2) * e->nbox, cudaMemcpyHostToDevice,
+    CUCO_TRY_CUDA(cudaMemcpyAsync(e->d_kicks, e->h_kicks[k], sizeof(double2) * e->nbox, cudaMemcpyHostToDevice,
                                   e->stream));
+    CUCO_TRY_CUDA(cudaEventRecord(e->up_done[k], e->stream));
+    e->up_pending[k] = true;
     return CUCO_OK;
 }
 
@@ -563,7 +578,10 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
         (s = grow(e->d_pm, e->cap_pm, nbc, st)) || (s = grow(e->d_kicks, e->cap_kicks, nbc, st)) ||
         (s = grow(e->d_factors, e->cap_factors, nbc, st)) || (s = grow(e->pair_counter, e->cap_counter, 1, st)) ||
         (s = grow(e->d_sr, e->cap_sr, shortrange_desc_bytes() * nbc, st)) ||
-        (s = grow_pinned(e->h_factors, e->cap_hfactors, nbc)) || (s = grow_pinned(e->h_kicks, e->cap_hkicks, nbc)))
+        (s = grow_pinned(e->h_factors[0], e->cap_hfactors[0], nbc)) ||
+        (s = grow_pinned(e->h_kicks[0], e->cap_hkicks[0], nbc)) ||
+        (s = grow_pinned(e->h_factors[1], e->cap_hfactors[1], nbc)) ||
+        (s = grow_pinned(e->h_kicks[1], e->cap_hkicks[1], nbc)))
         return s;
     // tables and descriptors
     std::vector<float> tab(kNTab);
@@ -617,8 +635,10 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
         set_error("ensemble: descriptor upload failed");
         return CUCO_ERR_CUDA;
     }
-    memset(e->h_factors, 0, sizeof(StepFactors) * nbox);
-    memset(e->h_kicks, 0, sizeof(double2) * nbox);
+    for (int k = 0; k < 2; ++k) {
+        memset(e->h_factors[k], 0, sizeof(StepFactors) * nbox);
+        memset(e->h_kicks[k], 0, sizeof(double2) * nbox);
+    }
     e->nbox = nbox;
     e->cfg = cfg;
     e->P = P;
@@ -667,6 +687,12 @@ cuco_status_t cuco_ensemble_create(const cuco_config_t *boxes, int nbox, cuco_en
     }
     cudaEventCreate(&e->t0);
     cudaEventCreate(&e->t1);
+    for (int k = 0; k < 2; ++k)
+        if (cudaEventCreateWithFlags(&e->up_done[k], cudaEventDisableTiming) != cudaSuccess) {
+            set_error("cudaEventCreate failed");
+            cuco_ensemble_destroy(e);
+            return CUCO_ERR_CUDA;
+        }
     pool_keep_memory(e->device);
     cuco_status_t s = ensemble_layout(e, boxes, nbox, nullptr);
     if (s != CUCO_OK) {
@@ -712,8 +738,11 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
                     (void *)e->sr_segnt, (void *)e->sr_ctl})
         if (p && e->stream) cudaFreeAsync(p, e->stream);
     if (e->stream) cudaStreamSynchronize(e->stream);
-    if (e->h_factors) cudaFreeHost(e->h_factors);
-    if (e->h_kicks) cudaFreeHost(e->h_kicks);
+    for (int k = 0; k < 2; ++k) {
+        if (e->h_factors[k]) cudaFreeHost(e->h_factors[k]);
+        if (e->h_kicks[k]) cudaFreeHost(e->h_kicks[k]);
+        if (e->up_done[k]) cudaEventDestroy(e->up_done[k]);
+    }
     if (e->t0) cudaEventDestroy(e->t0);
     if (e->t1) cudaEventDestroy(e->t1);
     if (e->fork) cudaEventDestroy(e->fork);
@@ -793,22 +822,28 @@ cuco_status_t cuco_ensemble_step(cuco_ensemble_t *e, const double *drift, const 
         set_error("cuco_ensemble_step: no state uploaded or null factors");
         return CUCO_ERR_STATE;
     }
-    // the previous replay may still read the pinned factors
-    if (e->exec) CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
+    // slot k was last copied two steps ago: wait for that copy only, not for
+    // the steps in flight
+    const int k = e->slot;
+    if (e->up_pending[k]) {
+        CUCO_TRY_CUDA(cudaEventSynchronize(e->up_done[k]));
+        e->up_pending[k] = false;
+    }
     for (int b = 0; b < e->nbox; ++b) {
         const double L = e->cfg[b].boxsize;
-        e->h_factors[b].units_per_time = (float)(e->fixed ? drift[b] * 4294967296.0 / L : drift[b]);
-        e->h_kicks[b] = make_double2(kick_pp[b], kick_pm[b]);
+        e->h_factors[k][b].units_per_time = (float)(e->fixed ? drift[b] * 4294967296.0 / L : drift[b]);
+        e->h_kicks[k][b] = make_double2(kick_pp[b], kick_pm[b]);
     }
+    e->slot ^= 1;
+    CUCO_TRY(upload_factors(e, k));
     if (!e->exec) {
         // first step: run once outside capture (one-time kernel attributes),
-        // then capture the step as a graph for the following ones
-        CUCO_TRY(upload_factors(e));
+        // then capture the step (without the factor upload, which precedes
+        // every launch) as a graph for the following ones
         CUCO_TRY(ensemble_pass(e, 1, true));
         CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
         CUCO_TRY_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        cuco_status_t s1 = upload_factors(e);
-        cuco_status_t s2 = s1 == CUCO_OK ? ensemble_pass(e, 1, true) : s1;
+        cuco_status_t s2 = ensemble_pass(e, 1, true);
         cudaGraph_t g = nullptr;
         cudaError_t ce = cudaStreamEndCapture(e->stream, &g);
         if (s2 != CUCO_OK) {

@@ -359,7 +359,9 @@ cuco_status_t cuco_ensemble_get_state(cuco_ensemble_t *ensemble, int box, float 
 /* forces at the current positions (synchronous) */
 cuco_status_t cuco_ensemble_forces(cuco_ensemble_t *ensemble);
 /* one step of every box: drift[b], kick_pp[b], kick_pm[b] as cuco_box_step
- * (asynchronous; the first call also captures the graph) */
+ * (asynchronous; the first call also captures the graph).  The factors are
+ * copied from one of two pinned slots used in turn, so a call waits at most
+ * for the copy queued two calls back, not for the steps in flight. */
 cuco_status_t cuco_ensemble_step(cuco_ensemble_t *ensemble, const double *drift, const double *kick_pp,
                                  const double *kick_pm);
 cuco_status_t cuco_ensemble_sync(cuco_ensemble_t *ensemble);
