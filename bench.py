@@ -36,6 +36,7 @@ import subprocess
 import sys
 import threading
 import time
+from types import SimpleNamespace
 
 import numpy as np
 
@@ -94,7 +95,9 @@ def run_batched(args, world, rank, local):
     from cuco_gb300 import Box, BoxConfig, ics
     from cuco_gb300.engine import MODE_FIXED
     from cuco_gb300.ensemble import Ensemble
-    specs = batched_specs()
+    # boxes are independent: rank r takes every world-th box (no exchange)
+    all_specs = batched_specs()
+    specs = all_specs[rank::world]
     ic_list, cfgs, sched = [], [], None
     for n_side, M, L, seed in specs:
         ic = ics.zeldovich(n_side, L, Z_INIT, seed)
@@ -133,7 +136,8 @@ def run_batched(args, world, rank, local):
     dist_barrier(world)
     clk = clocks.stop()
     t_total = dist_max(ms / 1e3, world)
-    value = world * ntot * K / t_total
+    ntot_all = dist_sum(float(ntot), world)
+    value = ntot_all * K / t_total
     launches = ens.launches()
     plans = [ens.plan(b) for b in range(len(cfgs))]
     ens.close()
@@ -156,14 +160,15 @@ def run_batched(args, world, rank, local):
         lib.cuco_box_timer(box.h, 1, ctypes.byref(m))
         t_plain += m.value / 1e3
         box.close()
-    plain_rate = ntot * Kb / t_plain
-    sizes = [sp[0] for sp in specs]
+    plain_rate = ntot_all * Kb / dist_max(t_plain, world)
+    sizes = [sp[0] for sp in all_specs]
     line = {
         "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": K, "warmup": W, "ms_per_step": 1e3 * t_total / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic",
-        "config": {"workload": "batched-64boxes-N16to96-M2N-L50to400-z49", "boxes": len(specs),
-                   "particles": ntot, "n_side_min": min(sizes), "n_side_max": max(sizes),
+        "config": {"workload": "batched-64boxes-N16to96-M2N-L50to400-z49", "boxes": len(all_specs),
+                   "particles": int(ntot_all), "n_side_min": min(sizes), "n_side_max": max(sizes),
+                   "sharding": f"boxes split by rank ({world} rank(s)), no exchange",
                    "positions": "uint32 fixed point (L/2^32)", "timed_steps": "steps 0..K-1 from z=49",
                    "graph": "one CUDA graph per step, one launch per phase over all boxes"},
         "one_at_a_time_plain": {"value": plain_rate, "unit": "particle-updates/s", "steps": Kb,
@@ -229,7 +234,11 @@ def run_serving(args, world, rank, local):
     # the served form in either precision: both meet the rms force error of
     # 1e-3 the serving workload asks for (the plain form 1e-4)
     mode = MODE_FIXED if args.serving_mode == "fixed" else 0
+    from cuco_gb300.serve import shard_jobs
     stream = serving_stream(args.jobs)
+    # jobs are independent: rank r serves every world-th job (no exchange)
+    stream_all = stream
+    stream = [vars(sp) for sp in shard_jobs([SimpleNamespace(**sp) for sp in stream_all], rank, world)]
     jobs = serving_jobs(stream, local, mode)
     # autotune every size once (cached), outside the timed stream
     sizes_seen = {}
@@ -245,7 +254,14 @@ def run_serving(args, world, rank, local):
     clk = clocks.stop()
     lat = np.array([j.done - j.arrival for j in done])
     updates = sum(j.config.n * (j.steps + 1) for j in done)
-    served_rate = updates / wall
+    wall = dist_max(wall, world)
+    updates_all = dist_sum(float(updates), world)
+    served_rate = updates_all / wall
+    if world > 1:  # latencies of every rank's jobs
+        import torch.distributed as dist
+        parts = [None] * world
+        dist.all_gather_object(parts, lat.tolist())
+        lat = np.array([x for p in parts for x in p])
     # one at a time, plain path: a sample of the jobs run alone (their full
     # runs), and a FIFO queue of all jobs at that rate with the same arrivals
     sample = jobs[:: max(1, len(jobs) // args.baseline_jobs)][: args.baseline_jobs]
@@ -264,24 +280,25 @@ def run_serving(args, world, rank, local):
         box.close()
     plain_rate = plain_u / plain_t
     free, fifo = 0.0, []
-    for sp in stream:
+    for sp in stream_all:
         free = max(free, sp["arrival"]) + sp["n_side"] ** 3 * (sp["steps"] + 1) / plain_rate
         fifo.append(free - sp["arrival"])
     fifo = np.array(fifo)
-    sizes = [sp["n_side"] for sp in stream]
+    sizes = [sp["n_side"] for sp in stream_all]
     line = {
         "metric": "particle-updates/s", "value": served_rate, "unit": "particle-updates/s", "n_gpus": world,
-        "steps": int(sum(sp["steps"] + 1 for sp in stream)), "warmup": 0, "ms_per_step": None,
+        "steps": int(sum(sp["steps"] + 1 for sp in stream_all)), "warmup": 0, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32+f32" if mode else "f32", "data": "synthetic",
-        "config": {"workload": f"serving-{len(stream)}jobs-poisson20-N32to192-M2N-L50to500-50to200steps",
-                   "jobs": len(stream), "arrival_rate_per_s": 20.0, "hbm_budget_gb": args.hbm_budget_gb,
+        "config": {"workload": f"serving-{len(stream_all)}jobs-poisson20-N32to192-M2N-L50to500-50to200steps",
+                   "jobs": len(stream_all), "arrival_rate_per_s": 20.0, "hbm_budget_gb": args.hbm_budget_gb,
+                   "sharding": f"jobs split by rank ({world} rank(s)), no exchange",
                    "n_side_min": min(sizes), "n_side_max": max(sizes),
                    "positions": "uint32 fixed point (L/2^32)" if mode else "float32",
                    "clock": "host wall time"},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},
-        "wall_s": wall, "particle_updates": updates, "max_concurrent_jobs": srv.peak_active,
+        "wall_s": wall, "particle_updates": int(updates_all), "max_concurrent_jobs": srv.peak_active,
         "rebuilds": srv.rebuilds, "rebuild_s": srv.rebuild_s,
         "one_at_a_time_plain": {"value": plain_rate, "unit": "particle-updates/s", "sample_jobs": len(sample),
                                 "fifo_latency_s": {"p50": float(np.percentile(fifo, 50)),
@@ -388,6 +405,16 @@ def dist_max(x: float, world: int) -> float:
     import torch.distributed as dist
     t = torch.tensor([x], dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
     return float(t.item())
 
 

@@ -17,11 +17,25 @@ interpolation, a short range that visits candidates in a fixed order), and a
 job's result is bit-identical alone and in the mix.
 
 Time comes from a clock callable: wall time for measurements, a tick counter
-for tests.  A job's latency is its completion time minus its arrival time.
+for tests.  A job's latency is its completion time minus its arrival time;
+the completion time is taken after the GPU has finished the job's last step
+(the server waits for the ensemble's stream only when a job finishes, not
+every tick, so the host prepares the next step while the GPU runs this one).
+
+Output times (run.c:49-59, 75-104; the reference reads them from a list such
+as output_32/list_32.txt): a job may list scale factors at which it writes a
+snapshot in the reference's .cuco format.  As in the reference, an output
+between two steps is a drift of the positions from the last step to the
+output time with the velocities as they stand (the last kick), written
+without changing the run: the trajectory is the same with or without outputs.
+
+Several processes (one per GPU) share a stream by job: shard_jobs gives each
+rank every world-th job in arrival order, with no exchange between ranks.
 """
 from __future__ import annotations
 
 import ctypes
+import os
 import time
 from dataclasses import dataclass, field
 
@@ -29,8 +43,9 @@ import numpy as np
 
 from . import _native
 from ._native import check
-from .engine import MODE_FIXED, BoxConfig, fixed_step_schedule
+from .engine import MODE_FIXED, BoxConfig, cosmo_factors, fixed_step_schedule
 from .ensemble import Ensemble
+from .ics import HEADER_DTYPE, PARTICLE_DTYPE
 
 
 @dataclass
@@ -42,6 +57,11 @@ class Job:
     a_begin: float
     steps: int                   # fixed log-a steps to a = 1
     arrival: float = 0.0         # in the server clock's units
+    outputs: tuple = ()          # scale factors of snapshot outputs (ascending)
+    output_dir: str | None = None
+    omega0: float = 0.3          # for the snapshot header and the drift to an output
+    omega_lambda: float = 0.7
+    hubble_param: float = 0.7
     # filled in by the server
     drift: np.ndarray = field(default=None, repr=False)
     kick: np.ndarray = field(default=None, repr=False)
@@ -50,10 +70,49 @@ class Job:
     done: float | None = None
     result_pos: np.ndarray = field(default=None, repr=False)
     result_vel: np.ndarray = field(default=None, repr=False)
+    a: np.ndarray = field(default=None, repr=False)   # scale factor after each step
+    snapshots: list = field(default_factory=list)     # paths written, in order
+    next_output: int = 0
 
     @property
     def finished(self) -> bool:
         return self.next_step > self.steps
+
+
+def shard_jobs(jobs: list, rank: int, world: int) -> list:
+    """This rank's share of a job stream: every world-th job in arrival order
+    (jobs are independent; no data crosses ranks)."""
+    order = sorted(range(len(jobs)), key=lambda k: (jobs[k].arrival, k))
+    return [jobs[k] for k in order[rank::world]]
+
+
+def output_positions(pos: np.ndarray, vel: np.ndarray, drift: float, boxsize: float) -> np.ndarray:
+    """Positions drifted from the last step to an output time and wrapped into
+    [0, L) (predict.c:10-41: Pos += Vel * drift, then the box wrapping)."""
+    x = (pos.astype(np.float64) + vel.astype(np.float64) * drift).astype(np.float32)
+    L = np.float32(boxsize)
+    x = np.where(x < 0, (x.astype(np.float64) + float(L)).astype(np.float32), x)
+    x = np.where(x >= L, (x.astype(np.float64) - float(L)).astype(np.float32), x)
+    return x
+
+
+def write_snapshot(path: str, job: Job, a_out: float, pos, vel, acc_pp, acc_pm):
+    """HEADER + PARTICLE[] as io.c:9-40 writes them (Ti fields 0: the jobs run
+    global steps)."""
+    c = job.config
+    hdr = np.zeros(1, dtype=HEADER_DTYPE)
+    hdr["NumPart"] = c.n
+    hdr["Mass"] = c.mass
+    hdr["Time"] = a_out
+    hdr["Redshift"] = np.float32(1) / np.float32(a_out) - np.float32(1)
+    hdr["BoxSize"] = c.boxsize
+    hdr["Omega0"], hdr["OmegaLambda"], hdr["HubbleParam"] = job.omega0, job.omega_lambda, job.hubble_param
+    parts = np.zeros(c.n, dtype=PARTICLE_DTYPE)
+    parts["Pos"], parts["Vel"], parts["Mass"] = pos, vel, c.mass
+    parts["GravAccel"], parts["GravPM"] = acc_pp, acc_pm
+    with open(path, "wb") as fh:
+        fh.write(hdr.tobytes())
+        fh.write(parts.tobytes())
 
 
 def footprint(configs: list[BoxConfig]) -> int:
@@ -91,7 +150,9 @@ class Server:
     def submit(self, job: Job):
         if job.config.mode != self.mode:
             raise ValueError("job mode differs from the server's")
-        _, job.drift, job.kick = fixed_step_schedule(job.a_begin, 1.0, job.steps)
+        job.a, job.drift, job.kick = fixed_step_schedule(job.a_begin, 1.0, job.steps)
+        if job.outputs and not job.output_dir:
+            raise ValueError("a job with output times needs an output directory")
         self.queue.append(job)
 
     def _admit(self) -> list[Job]:
@@ -131,7 +192,12 @@ class Server:
 
     def _retire(self):
         """Collect finished jobs' results (their boxes stay in the ensemble,
-        frozen, until the next rebuild)."""
+        frozen, until the next rebuild).  A job is done when the GPU has run
+        its last step: the ensemble's stream is waited for before the time is
+        taken, only on ticks where a job finishes."""
+        if not any(j.finished and j.done is None for j in self.active):
+            return
+        self.ens.sync()
         now = self.clock()
         for k, j in enumerate(self.active):
             if j.finished and j.done is None:
@@ -152,6 +218,7 @@ class Server:
             self._rebuild(running, new)
         if not self.active:
             return bool(self.queue)
+        self._outputs()
         nb = len(self.active)
         d = np.zeros(nb)
         kp = np.zeros(nb)
@@ -165,6 +232,26 @@ class Server:
                 self.updates += j.config.n
         self.ticks += 1
         return True
+
+    def _outputs(self):
+        """Snapshots of running jobs whose next step passes an output time:
+        step s (s >= 1) drifts a[s-1] -> a[s]; an output a_out in (a[s-1],
+        a[s]] is the state after step s-1 drifted to a_out (run.c:49-59).
+        Output times at or before the start are skipped."""
+        for k, j in enumerate(self.active):
+            s = j.next_step
+            if j.finished or not j.outputs or s == 0:
+                continue
+            while j.next_output < len(j.outputs) and j.outputs[j.next_output] <= j.a[s]:
+                a_out = j.outputs[j.next_output]
+                if a_out > j.a[0]:
+                    pos, vel, app, apm = self.ens.get_state(k)
+                    drift = cosmo_factors(j.a[s - 1], a_out, j.omega0, j.omega_lambda)[0]
+                    path = os.path.join(j.output_dir, f"job{j.job_id}_{j.next_output:03d}.cuco")
+                    write_snapshot(path, j, a_out, output_positions(pos, vel, drift, j.config.boxsize), vel,
+                                   app, apm)
+                    j.snapshots.append(path)
+                j.next_output += 1
 
     def drain(self):
         self.ens and self.ens.sync()

@@ -88,3 +88,44 @@ def test_job_larger_than_the_budget_is_refused():
     jobs = make_jobs()[:1]
     with pytest.raises(RuntimeError):
         serve(jobs, budget=footprint([jobs[0].config]) - 1)
+
+
+def test_output_times_write_snapshots_without_changing_the_run(tmp_path):
+    """A job with output times (run.c:49-59) served in a mix: its snapshots are
+    the state after the step before each output time, drifted to it, in the
+    reference's .cuco format; the run itself is the same as without outputs."""
+    from cuco_gb300 import fixed_step_schedule
+    from cuco_gb300.engine import cosmo_factors
+    from cuco_gb300.ensemble import Ensemble
+    from cuco_gb300.ics import read_cuco
+    from cuco_gb300.serve import output_positions
+    jobs = make_jobs()
+    target = jobs[3]
+    a_sched = fixed_step_schedule(target.a_begin, 1.0, target.steps)[0]
+    # between steps, exactly on a step, and the end of the run
+    target.outputs = (0.5 * (a_sched[2] + a_sched[3]), float(a_sched[5]), 1.0)
+    target.output_dir = str(tmp_path)
+    mix, _, _ = serve(jobs)
+    j = mix[target.job_id]
+    assert len(j.snapshots) == 3
+    plain, _, _ = serve(make_jobs())
+    assert np.array_equal(j.result_pos, plain[target.job_id].result_pos)
+    assert np.array_equal(j.result_vel, plain[target.job_id].result_vel)
+    # the same snapshots from the job run alone, step by step
+    ref = make_jobs()[3]
+    a, drift, kick = fixed_step_schedule(ref.a_begin, 1.0, ref.steps)
+    box = Ensemble([ref.config])
+    box.set_state(0, ref.pos, ref.vel)
+    s = 0
+    for path, a_out in zip(j.snapshots, target.outputs):
+        while a[s] < a_out:  # run up to the step before the output (states at a[0..s])
+            box.step(np.array([drift[s]]), np.array([kick[s]]))
+            s += 1
+        pos, vel, app, apm = box.get_state(0)
+        d = cosmo_factors(float(a[s - 1]), a_out)[0]
+        hdr, parts = read_cuco(path)
+        assert hdr["Time"] == np.float32(a_out) and int(hdr["NumPart"]) == ref.config.n
+        assert np.array_equal(parts["Pos"], output_positions(pos, vel, d, ref.config.boxsize))
+        assert np.array_equal(parts["Vel"], vel)
+        assert np.array_equal(parts["GravAccel"], app) and np.array_equal(parts["GravPM"], apm)
+    box.close()
