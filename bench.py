@@ -62,10 +62,15 @@ PRESETS = {
     "precision-128": (128, 256.0, 256, 64, 1, "precision-128^3-L256-M256-G64-z49to0-200steps"),
     "plain-512": (512, 1000.0, 1024, 256, 0, "plain-512^3-L1000-M1024-G256-z49to0-200steps"),
     "precision-512": (512, 1000.0, 1024, 256, 1, "precision-512^3-L1000-M1024-G256-z49to0-200steps"),
+    "plain-256": (256, 512.0, 512, 128, 0, "plain-256^3-L512-M512-G128-z49to0-200steps"),
+    "precision-256": (256, 512.0, 512, 128, 1, "precision-256^3-L512-M512-G128-z49to0-200steps"),
 }
 
 
 BATCHED = "batched-64"
+# 256^3 particles as eight 128^3 boxes (L = 256 Mpc/h, M = 256, own seeds): the
+# batched fixed-point form against the same boxes on the plain path
+BATCHED_256 = "batched-8x128"
 
 
 def smooth5(n):
@@ -89,14 +94,18 @@ def batched_specs(nbox=64, seed=2024):
     return out
 
 
-def run_batched(args, world, rank, local):
+def batched_256_specs(seed=4096):
+    return [(128, 256, 256.0, seed + 1 + i) for i in range(8)]
+
+
+def run_batched(args, world, rank, local, all_specs=None, workload="batched-64boxes-N16to96-M2N-L50to400-z49"):
     """Many boxes per launch (fixed-point form) against the same boxes stepped
     one at a time on the plain path."""
     from cuco_gb300 import Box, BoxConfig, ics
     from cuco_gb300.engine import MODE_FIXED
     from cuco_gb300.ensemble import Ensemble
     # boxes are independent: rank r takes every world-th box (no exchange)
-    all_specs = batched_specs()
+    all_specs = batched_specs() if all_specs is None else all_specs
     specs = all_specs[rank::world]
     ic_list, cfgs, sched = [], [], None
     for n_side, M, L, seed in specs:
@@ -166,7 +175,7 @@ def run_batched(args, world, rank, local):
         "metric": "particle-updates/s", "value": value, "unit": "particle-updates/s", "n_gpus": world,
         "steps": K, "warmup": W, "ms_per_step": 1e3 * t_total / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32", "data": "synthetic",
-        "config": {"workload": "batched-64boxes-N16to96-M2N-L50to400-z49", "boxes": len(all_specs),
+        "config": {"workload": workload, "boxes": len(all_specs),
                    "particles": int(ntot_all), "n_side_min": min(sizes), "n_side_max": max(sizes),
                    "sharding": f"boxes split by rank ({world} rank(s)), no exchange",
                    "positions": "uint32 fixed point (L/2^32)", "timed_steps": "steps 0..K-1 from z=49",
@@ -738,7 +747,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS) + [BATCHED, SERVING])
+    ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS) + [BATCHED, BATCHED_256, SERVING])
     ap.add_argument("--baseline-steps", type=int, default=20)
     ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")
     ap.add_argument("--baseline-jobs", type=int, default=8, help="serving: jobs run alone on the plain path")
@@ -750,10 +759,13 @@ def main():
         world, rank, local = dist_setup()
         run_serving(args, world, rank, local)
         return
-    if args.workload == BATCHED:
+    if args.workload in (BATCHED, BATCHED_256):
         args.warmup = max(args.warmup, 3)
         world, rank, local = dist_setup()
-        run_batched(args, world, rank, local)
+        if args.workload == BATCHED:
+            run_batched(args, world, rank, local)
+        else:
+            run_batched(args, world, rank, local, batched_256_specs(), "batched-8x128^3-L256-M256-z49")
         return
     apply_preset(args.workload)
     args.warmup = max(args.warmup, 3)

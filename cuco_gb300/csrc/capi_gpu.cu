@@ -133,13 +133,15 @@ void cudaForceEvaluateShortrange(float *gravAccel, float *sortedPos, uint *gridP
         const uint32_t hc = shortrange_heavy_cap(numParticles);
         capi_check(cudaMalloc(&w.heavy, sizeof(uint2) * hc), "cudaForceEvaluateShortrange");
         capi_check(cudaMalloc(&w.seg_nt, sizeof(uint32_t) * numCells), "cudaForceEvaluateShortrange");
-        capi_check(cudaMalloc(&w.ctl, 2 * sizeof(uint32_t)), "cudaForceEvaluateShortrange");
+        capi_check(cudaMalloc(&w.ctl, kSRCtlWords * sizeof(uint32_t)), "cudaForceEvaluateShortrange");
+        capi_check(cudaMemset(w.ctl, 0, kSRCtlWords * sizeof(uint32_t)), "cudaForceEvaluateShortrange");
         w.heavy_cap = hc;
         w.seg_cap = numCells;
     }
     capi_status(launch_shortrange(p, (const float4 *)sortedPos, gridParticleIndex, cellStart, cellEnd,
                                   kCellStartEnd, s.table, (float4 *)gravAccel, k, w, 0),
                 "cudaForceEvaluateShortrange");
+    capi_status(shortrange_check(w.ctl, 0), "cudaForceEvaluateShortrange");
 }
 
 void radixSort(uint *keys, uint *values, uint *tempKeys, uint *tempValues, uint *counters,

@@ -139,9 +139,14 @@ struct SRWork {
     uint32_t heavy_cap;
     uint32_t *seg_nt;
     uint32_t seg_cap;
-    uint32_t *ctl;  // [0] dense slices listed, [1] next unit
+    uint32_t *ctl;  // kSRCtlWords: [0] dense slices listed, [1] next unit (both reset per
+                    // launch), [2] nonzero once a staging wait gave up (kept until read)
 };
 uint32_t shortrange_heavy_cap(uint32_t n);
+constexpr int kSRCtlWords = 4;
+// Reads and clears the short range's timeout word (ctl[2]) after the work on
+// `stream` is done: CUCO_ERR_TIMEOUT when a staging wait gave up.
+cuco_status_t shortrange_check(uint32_t *ctl, cudaStream_t stream);
 
 // pair_counter: when non-null, the launch adds its in-range pair count to it.
 cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,

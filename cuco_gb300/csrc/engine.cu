@@ -529,8 +529,9 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         (s = alloc(&b->table, kNTab)) ||
         (s = alloc(&b->stage3, 3 * n)) || (s = alloc(&b->pair_counter, 1)) ||
         (s = alloc(&b->work.heavy, shortrange_heavy_cap(b->n))) || (s = alloc(&b->work.seg_nt, b->ncells)) ||
-        (s = alloc(&b->work.ctl, 2)))
+        (s = alloc(&b->work.ctl, kSRCtlWords)))
         return fail(s);
+    cudaMemset(b->work.ctl, 0, sizeof(uint32_t) * kSRCtlWords);
     b->work.heavy_cap = shortrange_heavy_cap(b->n);
     b->work.seg_cap = b->ncells;  // G^3 covers every segment length
     cudaMemset(b->pair_counter, 0, sizeof(unsigned long long));
@@ -629,7 +630,7 @@ cuco_status_t cuco_box_get_state(cuco_box_t *b, float *pos, float *vel, float *a
         CUCO_TRY_CUDA(cudaMemcpyAsync(dst[k], b->stage3, bytes, kind, b->stream));
     }
     CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
-    return CUCO_OK;
+    return shortrange_check(b->work.ctl, b->stream);
 }
 
 cuco_status_t cuco_box_set_state_fixed(cuco_box_t *b, const uint32_t *pos, const float *vel, int on_device) {
@@ -718,7 +719,7 @@ cuco_status_t cuco_box_run(cuco_box_t *b, int nsteps, const double *drift, const
 cuco_status_t cuco_box_sync(cuco_box_t *b) {
     if (!b) return CUCO_ERR_INVALID;
     CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
-    return CUCO_OK;
+    return shortrange_check(b->work.ctl, b->stream);
 }
 
 cuco_status_t cuco_box_stream(cuco_box_t *b, void **stream) {

@@ -618,7 +618,7 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
     }
     if ((s = grow(e->d_mapz, e->cap_mapz, mapz.size(), st)) || (s = grow(e->d_mapa, e->cap_mapa, mapa.size(), st)) ||
         (s = grow(e->sr_heavy, e->cap_heavy, (size_t)shortrange_heavy_cap((uint32_t)n) + 16u * nbox, st)) ||
-        (s = grow(e->sr_segnt, e->cap_segnt, (size_t)segbase[nbox], st)) || (s = grow(e->sr_ctl, e->cap_ctl, 2, st)))
+        (s = grow(e->sr_segnt, e->cap_segnt, (size_t)segbase[nbox], st)) || (s = grow(e->sr_ctl, e->cap_ctl, kSRCtlWords, st)))
         return s;
     if (cudaStreamSynchronize(st) != cudaSuccess ||
         cudaMemcpy(e->table, tab.data(), sizeof(float) * kNTab, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -631,7 +631,8 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
         cudaMemcpy(e->d_sr, srd.data(), srd.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_mapz, mapz.data(), sizeof(uint2) * mapz.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(e->d_mapa, mapa.data(), sizeof(uint2) * mapa.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(e->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaMemset(e->pair_counter, 0, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(e->sr_ctl, 0, sizeof(uint32_t) * kSRCtlWords) != cudaSuccess) {
         set_error("ensemble: descriptor upload failed");
         return CUCO_ERR_CUDA;
     }
@@ -862,7 +863,7 @@ cuco_status_t cuco_ensemble_step(cuco_ensemble_t *e, const double *drift, const 
 cuco_status_t cuco_ensemble_sync(cuco_ensemble_t *e) {
     if (!e) return CUCO_ERR_INVALID;
     CUCO_TRY_CUDA(cudaStreamSynchronize(e->stream));
-    return CUCO_OK;
+    return e->sr_ctl ? shortrange_check(e->sr_ctl, e->stream) : CUCO_OK;
 }
 
 cuco_status_t cuco_ensemble_timer(cuco_ensemble_t *e, int op, float *ms) {

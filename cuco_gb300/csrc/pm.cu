@@ -479,7 +479,7 @@ __device__ __forceinline__ void fft_axis_reg(float2 *__restrict__ spec, const fl
                 float g = 0.f;
                 if (b < nb) {
                     const int k2s = kx * kx + ky * ky + kz * kz;
-                    if (k2s > 0) g = -green1d[kx] * gy * green1d[kz] / (float)k2s;
+                    if (k2s > 0) g = -green1d[kx] * gy * green1d[kz] * __frcp_rn((float)k2s);
                 }
                 x[sl * pitch + b] = make_float2(v.x * g, v.y * g);
             }
@@ -640,7 +640,7 @@ __device__ __forceinline__ void fft_axis(float2 *__restrict__ spec, const float2
             float g = 0.f;
             if (b < nb) {
                 int k2 = kx * kx + ky * ky + kz * kz;
-                if (k2 > 0) g = -green1d[kx] * gy * green1d[kz] / (float)k2;
+                if (k2 > 0) g = -green1d[kx] * gy * green1d[kz] * __frcp_rn((float)k2);
             }
             res[m * pitch + b] = make_float2(v.x * g, v.y * g);
         }
@@ -729,7 +729,7 @@ __device__ __forceinline__ void fft_axis_reg_fixed(float2 *__restrict__ spec, co
                 float g = 0.f;
                 if (valid) {
                     const int k2s = kx * kx + c;
-                    if (k2s > 0) g = -green1d[kx] * gy * gz / (float)k2s;
+                    if (k2s > 0) g = -green1d[kx] * gy * gz * __frcp_rn((float)k2s);
                 }
                 x[sl * B + b] = make_float2(v.x * g, v.y * g);
             }
@@ -918,11 +918,29 @@ __device__ __forceinline__ void cic_point(const float4 &p, float to_slab_fac, in
     }
 }
 
-// CIC weight w in [0, 1] as the integer w * 2^32 (rounded once): integer
-// atomics are associative, so the deposited grid does not depend on the order
-// in which particles land, and it is the exact sum of the rounded weights.
-__device__ __forceinline__ void deposit_w(unsigned long long *a, float w) {
-    atomicAdd(a, __float2ull_rn(__fmul_rn(w, 4294967296.0f)));
+// CIC weights w in [0, 1] are added as the integers w * 2^32 (rounded once):
+// integer atomics are associative, so the deposited grid does not depend on
+// the order in which particles land, and it is the exact sum of the rounded
+// weights.
+//
+// The eight CIC corners of a particle, warp-aggregated: lanes whose corner is
+// the same mesh cell (__match_any_sync on the address) add their integer
+// weights with shuffles and the lowest of them issues one atomic.  When no two
+// active lanes share a cell (a warp of lattice-ordered particles at high
+// redshift) every lane adds its own weight directly.  Integer sums are
+// associative, so the grid is the same either way, bit for bit.  Called by
+// every active lane of the warp together.
+__device__ __forceinline__ void deposit_corner(unsigned long long *a, float w, unsigned active, unsigned lane) {
+    const unsigned long long v = __float2ull_rn(__fmul_rn(w, 4294967296.0f));
+    const unsigned peers = __match_any_sync(active, (unsigned long long)a);
+    if (__all_sync(active, peers == (1u << lane))) {
+        atomicAdd(a, v);
+        return;
+    }
+    unsigned long long sum = 0;
+    for (unsigned rest = peers; rest; rest &= rest - 1)
+        sum += __shfl_sync(peers, v, __ffs(rest) - 1);
+    if (lane == (unsigned)__ffs(peers) - 1) atomicAdd(a, sum);
 }
 
 template <bool FIXED>
@@ -935,14 +953,15 @@ __device__ __forceinline__ void deposit_one(float4 p, unsigned long long *__rest
     const float dx = d[0], dy = d[1], dz = d[2];
     const size_t Mz = M, Myz = (size_t)M * M;
     const float m0 = 1.f - dx, m1 = dx;
-    deposit_w(&rho64[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz));
-    deposit_w(&rho64[sx * Myz + syy * Mz + sz], m0 * dy * (1.f - dz));
-    deposit_w(&rho64[sx * Myz + sy * Mz + szz], m0 * (1.f - dy) * dz);
-    deposit_w(&rho64[sx * Myz + syy * Mz + szz], m0 * dy * dz);
-    deposit_w(&rho64[sxx * Myz + sy * Mz + sz], m1 * (1.f - dy) * (1.f - dz));
-    deposit_w(&rho64[sxx * Myz + syy * Mz + sz], m1 * dy * (1.f - dz));
-    deposit_w(&rho64[sxx * Myz + sy * Mz + szz], m1 * (1.f - dy) * dz);
-    deposit_w(&rho64[sxx * Myz + syy * Mz + szz], m1 * dy * dz);
+    const unsigned active = __activemask(), lane = threadIdx.x & 31;
+    deposit_corner(&rho64[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz), active, lane);
+    deposit_corner(&rho64[sx * Myz + syy * Mz + sz], m0 * dy * (1.f - dz), active, lane);
+    deposit_corner(&rho64[sx * Myz + sy * Mz + szz], m0 * (1.f - dy) * dz, active, lane);
+    deposit_corner(&rho64[sx * Myz + syy * Mz + szz], m0 * dy * dz, active, lane);
+    deposit_corner(&rho64[sxx * Myz + sy * Mz + sz], m1 * (1.f - dy) * (1.f - dz), active, lane);
+    deposit_corner(&rho64[sxx * Myz + syy * Mz + sz], m1 * dy * (1.f - dz), active, lane);
+    deposit_corner(&rho64[sxx * Myz + sy * Mz + szz], m1 * (1.f - dy) * dz, active, lane);
+    deposit_corner(&rho64[sxx * Myz + syy * Mz + szz], m1 * dy * dz, active, lane);
 }
 
 __device__ __forceinline__ int wrapi(int a, int M) { return a < 0 ? a + M : (a >= M ? a - M : a); }

@@ -169,16 +169,71 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
     return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
 }
 
+// ---- Bulk copies of contiguous source runs into shared memory (the tensor
+// memory accelerator's untiled global -> shared copy, completing on an
+// mbarrier).  One barrier per CTA, reused phase after phase; its waits are
+// bounded (kWaitCycles), after which the CTA reports a timeout and stops.
+constexpr long long kWaitCycles = 1ll << 31;  // ~1 s at 2 GHz
+__shared__ __align__(8) uint64_t g_stage_bar;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void bar_init(uint64_t *bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// one arrival that also expects `bytes` of copies in this phase
+__device__ __forceinline__ void bar_arrive_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool bar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Wait for the phase with parity `parity` to complete, at most kWaitCycles.
+__device__ __forceinline__ bool bar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    for (;;) {
+        if (bar_try_wait(bar, parity)) return true;
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+}
+
+// bytes (a multiple of 16) from global src to shared dst, both 16-byte aligned
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// orders this thread's earlier shared-memory accesses (and, after a CTA
+// barrier, the CTA's) before later bulk copies into shared memory
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // The body for one unit: the targets [slice_lo, slice_hi) (counted from the
 // segment's first target) of segment `seg` of one box (p, cs); kick_pp/kick_pm
 // are that box's kick factors.  A unit has at most kTMax targets.
+// Returns false when a staging wait gave up (the error word is set; the CTA
+// must stop).  `phase` is the parity of the CTA's staging barrier.
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
-__device__ __forceinline__ void shortrange_segment(
+__device__ __forceinline__ bool shortrange_segment(
     const ShortRangeParams &p, const ColumnSet &cs, const int seg, const uint32_t slice_lo,
     const uint32_t slice_hi, const double kick_pp, const double kick_pm, const float4 *__restrict__ spos,
     const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
     const float *__restrict__ table_g, float4 *__restrict__ acc_out, const KickArgs &kick,
-    unsigned long long *__restrict__ pair_counter) {
+    unsigned long long *__restrict__ pair_counter, uint32_t &phase, uint32_t *__restrict__ err) {
     extern __shared__ float4 smem_f4[];
     __shared__ uint32_t s_total, s_tbegin, s_tend;
     __shared__ uint32_t s_wdelta[kWarps][32];
@@ -236,7 +291,7 @@ __device__ __forceinline__ void shortrange_segment(
         const uint32_t t_seg = cst[e00], t_seg_end = cst[e00 + S - 1] + ccn[e00 + S - 1];
         t_begin = t_seg + min(slice_lo, t_seg_end - t_seg);
         t_end = t_seg + min(slice_hi, t_seg_end - t_seg);
-        if (t_begin >= t_end) return;  // uniform over the CTA
+        if (t_begin >= t_end) return true;  // uniform over the CTA
         // staged offsets: an exclusive scan of the cell counts in (column,
         // z-cell) order, each thread over a run of consecutive entries
         const int ne = ncols * nz;
@@ -319,7 +374,7 @@ __device__ __forceinline__ void shortrange_segment(
         const uint32_t t_seg = s_tbegin, t_seg_end = s_tend;
         t_begin = t_seg + min(slice_lo, t_seg_end - t_seg);
         t_end = t_seg + min(slice_hi, t_seg_end - t_seg);
-        if (t_begin >= t_end) return;
+        if (t_begin >= t_end) return true;
 
         // per column: staged offsets of its z-cells, runs of consecutive cells with one shift
         for (int col = tid; col < ncols; col += kThreads) {
@@ -687,35 +742,49 @@ __device__ __forceinline__ void shortrange_segment(
         }
     };
 
-    // stage [c0, c1): warp per run
-    auto stage = [&](uint32_t c0, uint32_t c1) {
+    // stage [c0, c1): each run's part is one bulk copy into shared memory,
+    // issued by lane 0 of the warp that owns the run; after the barrier's
+    // phase completes, the warp shifts its runs in place to the origin (the
+    // periodic image shift once per run; fixed point: the int32 offsets from
+    // the corner).  Entered by all threads after a CTA barrier.
+    auto stage = [&](uint32_t c0, uint32_t c1) -> bool {
+        if (tid == 0) bar_arrive_expect(&g_stage_bar, (c1 - c0) * (uint32_t)sizeof(float4));
+        __syncthreads();
+        if (lane == 0) {
+            fence_async_smem();
+            for (int rr = warp; rr < ncols * 2; rr += kWarps) {
+                const Run &r = runs[rr];
+                const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
+                if (r.cnt && hi > lo)
+                    bulk_copy_g2s(src + (lo - c0), spos + r.gsrc + (lo - r.soff), (hi - lo) * (uint32_t)sizeof(float4),
+                                  &g_stage_bar);
+            }
+        }
+        bool ok = bar_wait_bounded(&g_stage_bar, phase);
+        if (!ok) ok = bar_wait_bounded(&g_stage_bar, phase);  // the copies still in flight, bounded again
+        phase ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(err, 1u);
+            return false;
+        }
         for (int rr = warp; rr < ncols * 2; rr += kWarps) {
             const Run r = runs[rr];
             if (r.cnt == 0) continue;
             const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
-            uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
-            for (uint32_t s0 = lo + lane; s0 < hi; s0 += 64) {
-                const uint32_t s1 = s0 + 32;
-                const float4 a0 = spos[r.gsrc + (s0 - r.soff)];
-                float4 a1 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (s1 < hi) a1 = spos[r.gsrc + (s1 - r.soff)];
-                if (FIXED) {
-                    src[s0 - c0] = rel(a0);
-                    if (s1 < hi) src[s1 - c0] = rel(a1);
-                } else {
-                    src[s0 - c0] = make_float4(a0.x - cx, a0.y - cy, a0.z - cz, 0.f);
-                    if (s1 < hi) src[s1 - c0] = make_float4(a1.x - cx, a1.y - cy, a1.z - cz, 0.f);
-                }
-
+            const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
+            for (uint32_t s0 = lo + lane; s0 < hi; s0 += 32) {
+                const float4 a = src[s0 - c0];
+                src[s0 - c0] = FIXED ? rel(a) : make_float4(a.x - cx, a.y - cy, a.z - cz, 0.f);
             }
         }
+        return true;
     };
 
     // the unit's targets, read by every round (and chunk) from shared memory
     for (uint32_t t = tid; t < nt; t += kThreads) s_tpos[t] = spos[t_begin + t];
 
     if (single_chunk) {
-        stage(0, total);
+        if (!stage(0, total)) return false;
         __syncthreads();
         for (uint32_t round = 0; round < rounds; ++round) {
             const uint32_t t = round * kWarps + warp;
@@ -744,7 +813,7 @@ __device__ __forceinline__ void shortrange_segment(
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
             __syncthreads();  // the previous chunk is no longer read; s_acc zeroed
-            stage(c0, c1);
+            if (!stage(c0, c1)) return false;
             __syncthreads();
             for (uint32_t round = 0; round < rounds; ++round) {
                 const uint32_t t = round * kWarps + warp;
@@ -786,6 +855,7 @@ __device__ __forceinline__ void shortrange_segment(
         for (int off = 16; off > 0; off >>= 1) wsum += __shfl_xor_sync(kFull, wsum, off);
         if (lane == 0 && wsum) atomicAdd(pair_counter, (unsigned long long)wsum);
     }
+    return true;
 }
 
 // The work plan of one launch: each segment's target count, and the kTMax
@@ -857,7 +927,10 @@ __device__ __forceinline__ void load_table(const float *__restrict__ table_g) {
     extern __shared__ float4 smem_f4[];
     float *tab = reinterpret_cast<float *>(smem_f4 + kMaxStage + 1);
     for (int i = threadIdx.x; i < kTabPad; i += kThreads) tab[i] = table_g[min(i, kNTab - 1)];
-    if (threadIdx.x == 0) smem_f4[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
+    if (threadIdx.x == 0) {
+        smem_f4[kMaxStage] = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
+        bar_init(&g_stage_bar);
+    }
 }
 
 // Persistent: as many CTAs as fit on the GPU, each taking units until none
@@ -870,13 +943,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                  const uint32_t *__restrict__ cb, const float *__restrict__ table_g,
                  float4 *__restrict__ acc_out, const __grid_constant__ KickArgs kick,
                  unsigned long long *__restrict__ pair_counter) {
-    uint32_t seg, lo;
+    uint32_t seg, lo, phase = 0;
     bool skip;
     load_table(table_g);
     while (next_unit(w, nseg, &seg, &lo, &skip)) {
         if (skip) continue;
-        shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, (int)seg, lo, lo + kTMax, kick.kick_pp, kick.kick_pm,
-                                                    spos, perm, ca, cb, table_g, acc_out, kick, pair_counter);
+        if (!shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, (int)seg, lo, lo + kTMax, kick.kick_pp,
+                                                         kick.kick_pm, spos, perm, ca, cb, table_g, acc_out, kick,
+                                                         pair_counter, phase, w.ctl + 2))
+            return;
     }
 }
 
@@ -901,7 +976,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
                        const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cell_off,
                        const float *__restrict__ table_g, float4 *__restrict__ acc_out,
                        const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
-    uint32_t seg, lo;
+    uint32_t seg, lo, phase = 0;
     bool skip;
     load_table(table_g);
     while (next_unit(w, nseg, &seg, &lo, &skip)) {
@@ -909,9 +984,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const int b = find_box(seg_base, nbox, seg);
         const SRBoxDesc &d = boxes[b];
         const double2 k = KICK ? kicks[b] : make_double2(0.0, 0.0);
-        shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, d.cs, (int)(seg - seg_base[b]), lo, lo + kTMax,
-                                                             k.x, k.y, spos, perm, cell_off, nullptr, table_g,
-                                                             acc_out, kick, pair_counter);
+        if (!shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, d.cs, (int)(seg - seg_base[b]), lo,
+                                                                  lo + kTMax, k.x, k.y, spos, perm, cell_off, nullptr,
+                                                                  table_g, acc_out, kick, pair_counter, phase,
+                                                                  w.ctl + 2))
+            return;
     }
 }
 
@@ -988,6 +1065,18 @@ void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const Colum
 }
 
 uint32_t shortrange_heavy_cap(uint32_t n) { return 2u * (n / kTMax) + 16u; }
+
+cuco_status_t shortrange_check(uint32_t *ctl, cudaStream_t stream) {
+    uint32_t flag = 0;
+    CUCO_TRY_CUDA(cudaMemcpyAsync(&flag, ctl + 2, sizeof flag, cudaMemcpyDeviceToHost, stream));
+    CUCO_TRY_CUDA(cudaStreamSynchronize(stream));
+    if (flag) {
+        CUCO_TRY_CUDA(cudaMemsetAsync(ctl + 2, 0, sizeof(uint32_t), stream));
+        set_error("short range: a bulk-copy wait into shared memory gave up after ~1 s; forces are invalid");
+        return CUCO_ERR_TIMEOUT;
+    }
+    return CUCO_OK;
+}
 
 // The pair-law bounds the kernel reads from its parameters.
 static void finish_pair_law(ShortRangeParams &p) {
