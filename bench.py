@@ -617,14 +617,19 @@ def run_gpu_arm(args, world, rank, local):
         for s in range(first):
             box.step(drift[s], kick[s])
         box.sync()
+        box.enable_timing(True)
+        box.phase_totals(reset=True)
         lib.cuco_box_timer(box.h, 0, None)
         for s in range(first, NSTEPS_RUN + 1):
             box.step(drift[s], kick[s])
         lm = ctypes.c_float()
         lib.cuco_box_timer(box.h, 1, ctypes.byref(lm))
+        late_phase = box.phase_totals()
+        box.enable_timing(False)
         t_late = dist_max(lm.value / 1e3, world)
         late = {"steps": f"{first}..{NSTEPS_RUN} of 0..{NSTEPS_RUN} (z = {1 / a[first - 1] - 1:.2f} -> 0)",
-                "value": world * ic.n * 20 / t_late, "ms_per_step": 1e3 * t_late / 20}
+                "value": world * ic.n * 20 / t_late, "ms_per_step": 1e3 * t_late / 20,
+                "phase_ms_per_step": {k: round(v / 20, 4) for k, v in late_phase.items()}}
     value = world * ic.n * K / t_total
     pp_ms = phase[6] / K
     pair_flops = 20.0 * pairs.value / K

@@ -922,27 +922,18 @@ __device__ __forceinline__ void cic_point(const float4 &p, float to_slab_fac, in
 // integer atomics are associative, so the deposited grid does not depend on
 // the order in which particles land, and it is the exact sum of the rounded
 // weights.
-//
-// The eight CIC corners of a particle, warp-aggregated: lanes whose corner is
-// the same mesh cell (__match_any_sync on the address) add their integer
-// weights with shuffles and the lowest of them issues one atomic.  When no two
-// active lanes share a cell (a warp of lattice-ordered particles at high
-// redshift) every lane adds its own weight directly.  Integer sums are
-// associative, so the grid is the same either way, bit for bit.  Called by
-// every active lane of the warp together.
-__device__ __forceinline__ void deposit_corner(unsigned long long *a, float w, unsigned active, unsigned lane) {
-    const unsigned long long v = __float2ull_rn(__fmul_rn(w, 4294967296.0f));
-    const unsigned peers = __match_any_sync(active, (unsigned long long)a);
-    if (__all_sync(active, peers == (1u << lane))) {
-        atomicAdd(a, v);
-        return;
-    }
-    unsigned long long sum = 0;
-    for (unsigned rest = peers; rest; rest &= rest - 1)
-        sum += __shfl_sync(peers, v, __ffs(rest) - 1);
-    if (lane == (unsigned)__ffs(peers) - 1) atomicAdd(a, sum);
+__device__ __forceinline__ unsigned long long weight_u64(float w) {
+    return __float2ull_rn(__fmul_rn(w, 4294967296.0f));
 }
 
+// The eight CIC corners of a particle, warp-aggregated: particles of one warp
+// in the same mesh cell share all eight corners, so one __match_any_sync on
+// the cell finds them; each group adds its members' integer weights with
+// shuffles and its lowest lane issues the eight atomics.  When no two active
+// lanes share a cell (lattice-ordered particles at high redshift) every lane
+// adds its own weights directly.  Integer sums are associative, so the grid
+// is the same either way, bit for bit.  Called by every active lane of the
+// warp together.
 template <bool FIXED>
 __device__ __forceinline__ void deposit_one(float4 p, unsigned long long *__restrict__ rho64, int M,
                                             float to_slab_fac) {
@@ -953,15 +944,38 @@ __device__ __forceinline__ void deposit_one(float4 p, unsigned long long *__rest
     const float dx = d[0], dy = d[1], dz = d[2];
     const size_t Mz = M, Myz = (size_t)M * M;
     const float m0 = 1.f - dx, m1 = dx;
+    unsigned long long w[8] = {weight_u64(m0 * (1.f - dy) * (1.f - dz)), weight_u64(m0 * dy * (1.f - dz)),
+                               weight_u64(m0 * (1.f - dy) * dz),        weight_u64(m0 * dy * dz),
+                               weight_u64(m1 * (1.f - dy) * (1.f - dz)), weight_u64(m1 * dy * (1.f - dz)),
+                               weight_u64(m1 * (1.f - dy) * dz),        weight_u64(m1 * dy * dz)};
     const unsigned active = __activemask(), lane = threadIdx.x & 31;
-    deposit_corner(&rho64[sx * Myz + sy * Mz + sz], m0 * (1.f - dy) * (1.f - dz), active, lane);
-    deposit_corner(&rho64[sx * Myz + syy * Mz + sz], m0 * dy * (1.f - dz), active, lane);
-    deposit_corner(&rho64[sx * Myz + sy * Mz + szz], m0 * (1.f - dy) * dz, active, lane);
-    deposit_corner(&rho64[sx * Myz + syy * Mz + szz], m0 * dy * dz, active, lane);
-    deposit_corner(&rho64[sxx * Myz + sy * Mz + sz], m1 * (1.f - dy) * (1.f - dz), active, lane);
-    deposit_corner(&rho64[sxx * Myz + syy * Mz + sz], m1 * dy * (1.f - dz), active, lane);
-    deposit_corner(&rho64[sxx * Myz + sy * Mz + szz], m1 * (1.f - dy) * dz, active, lane);
-    deposit_corner(&rho64[sxx * Myz + syy * Mz + szz], m1 * dy * dz, active, lane);
+    const unsigned cell = ((unsigned)sx * (unsigned)M + (unsigned)sy) * (unsigned)M + (unsigned)sz;
+    const unsigned peers = __match_any_sync(active, cell);
+    bool lead = true;
+    if (!__all_sync(active, peers == (1u << lane))) {
+        // sum the group's weights into its lowest lane (every member runs the
+        // same number of shuffles, named by the group's own mask)
+        const unsigned first = (unsigned)__ffs(peers) - 1;
+        lead = lane == first;
+        unsigned long long sum[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (unsigned rest = peers; rest; rest &= rest - 1) {
+            const int src = __ffs(rest) - 1;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) sum[c] += __shfl_sync(peers, w[c], src);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) w[c] = sum[c];
+    }
+    if (lead) {
+        atomicAdd(&rho64[sx * Myz + sy * Mz + sz], w[0]);
+        atomicAdd(&rho64[sx * Myz + syy * Mz + sz], w[1]);
+        atomicAdd(&rho64[sx * Myz + sy * Mz + szz], w[2]);
+        atomicAdd(&rho64[sx * Myz + syy * Mz + szz], w[3]);
+        atomicAdd(&rho64[sxx * Myz + sy * Mz + sz], w[4]);
+        atomicAdd(&rho64[sxx * Myz + syy * Mz + sz], w[5]);
+        atomicAdd(&rho64[sxx * Myz + sy * Mz + szz], w[6]);
+        atomicAdd(&rho64[sxx * Myz + syy * Mz + szz], w[7]);
+    }
 }
 
 __device__ __forceinline__ int wrapi(int a, int M) { return a < 0 ? a + M : (a >= M ? a - M : a); }

@@ -459,7 +459,6 @@ __device__ __forceinline__ bool shortrange_segment(
     uint32_t npairs = 0;
     uint32_t *wdelta = s_wdelta[warp];
     const uint32_t lt_mask = (1u << lane) - 1u, le_mask = lt_mask | (1u << lane);
-    float tx = 0.f, ty = 0.f, tz = 0.f;  // the current target, origin-relative
 
     // Kernel parameters used per candidate, held in registers.
 
@@ -478,7 +477,7 @@ __device__ __forceinline__ bool shortrange_segment(
     // table is padded to kTabPad entries with its last value, so a bin index
     // masked to the padding is the clamped one (fast pairs have bins below
     // kNTab; others read a padding value they do not use).
-    auto pair_fast = [&](float4 s, float &ax, float &ay, float &az) -> bool {
+    auto pair_fast = [&](float4 s, float tx, float ty, float tz, float &ax, float &ay, float &az) -> bool {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
         // r2 = 0 gives rinv = inf and r = NaN: not fast (r2 < hmin2), not flagged
@@ -497,7 +496,7 @@ __device__ __forceinline__ bool shortrange_segment(
         // not flagged, so the rare-case branch is not taken once per target
         return r2 <= p.rc2_hi && r2 != 0.f && !fast;
     };
-    auto pair_slow = [&](float4 s, float &ax, float &ay, float &az) {
+    auto pair_slow = [&](float4 s, float tx, float ty, float tz, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
         bool ok = r2 <= p.rc2_hi && r2 != 0.f;
@@ -529,27 +528,35 @@ __device__ __forceinline__ bool shortrange_segment(
         if (COUNT) npairs += ok;
     };
 
-    // One target per warp: lane k culls columns k, k+32, ...; the warp then
-    // walks each non-empty column range with all lanes on consecutive sources.
+    // Two targets per warp: the warp culls the columns once for the pair
+    // (lane k takes column k, k+32, ...: the column against the pair's bounding
+    // box), concatenates the surviving column ranges into one candidate list,
+    // and walks it 32 candidates at a time, every lane on one staged source
+    // that it evaluates against both targets.  The pair shares the cull, the
+    // list mapping and the source loads; each target keeps its own sums.
     // Chunk-major: each chunk of staged sources is staged once, and every
     // target of the unit runs against it; with more than one chunk the
     // targets' sums are carried in shared memory from chunk to chunk.
-    const uint32_t rounds = (nt + kWarps - 1) / kWarps;
+    const uint32_t npair = (nt + 1) / 2;
+    const uint32_t rounds = (npair + kWarps - 1) / kWarps;
     const float mg = p.mass * p.G;
 
-    // The target's force from the sources of chunk [c0, c1), warp-reduced
-    // (lane 0 holds it); FIXED: compensated, with the error terms in e*.
-    auto target_chunk = [&](float4 pt, uint32_t c0, uint32_t c1, float &ax, float &ay, float &az, float &ex,
-                            float &ey, float &ez, bool reduce) {
-        float bx = 0.f, by = 0.f, bz = 0.f;
-        ax = ay = az = 0.f;
+    // The forces on targets A and B from the sources of chunk [c0, c1),
+    // warp-reduced (lane 0 holds them); FIXED: compensated, with the error
+    // terms in e*.  lo/hi: the pair's bounding box (absolute), ta/tb: the
+    // targets origin-relative (a missing B sits at the sentinel: it adds and
+    // counts nothing).
+    auto pair_chunk = [&](float4 lo, float4 hi, float4 ta, float4 tb, uint32_t c0, uint32_t c1, float &ax,
+                          float &ay, float &az, float &eax, float &eay, float &eaz, float &bx, float &by, float &bz,
+                          float &ebx, float &eby, float &ebz) {
+        ax = ay = az = bx = by = bz = 0.f;
         for (int cb = 0; cb < ncols; cb += 32) {
             const int col = cb + lane;
             uint32_t b = 0, e = 0;
             if (col < ncols) {
                 const float4 g = cgeo[col];
-                const float ddx = fmaxf(fmaxf(g.x - pt.x, pt.x - g.y), 0.f);
-                const float ddy = fmaxf(fmaxf(g.z - pt.y, pt.y - g.w), 0.f);
+                const float ddx = fmaxf(fmaxf(g.x - hi.x, lo.x - g.y), 0.f);
+                const float ddy = fmaxf(fmaxf(g.z - hi.y, lo.y - g.w), 0.f);
                 // explicit roundings: the candidate set (hence the lane each
                 // candidate lands on) must not depend on how the compiler
                 // contracts this expression in a given instantiation
@@ -559,7 +566,7 @@ __device__ __forceinline__ bool shortrange_segment(
                     // approximate square root: the margin covers it), in
                     // cells from the column's first z-cell
                     const float hz = __fmul_rn(q, rsqrt_ftz(fmaxf(q, 1e-30f)));
-                    const float ul = __fmaf_rn(pt.z - hz, winv, -zbase), uh = __fmaf_rn(pt.z + hz, winv, -zbase);
+                    const float ul = __fmaf_rn(lo.z - hz, winv, -zbase), uh = __fmaf_rn(hi.z + hz, winv, -zbase);
                     const int fl = __float2int_rd(ul), fh = __float2int_rd(uh);
                     const int zlo = max(fl, 0), zhi = min(fh, nz - 1);
                     if (zlo <= zhi) {
@@ -606,76 +613,56 @@ __device__ __forceinline__ bool shortrange_segment(
             if (len > 0) wdelta[__popc(nonempty & lt_mask)] = b - c0 - ps;
             if (len == 0) ps = 0xffffffffu;  // marks no start
             __syncwarp();
-            // Each window of 64 candidates: one bit per column start, so a
+            // Each window of 32 candidates: one bit per column start, so a
             // lane's column is (columns started before the window) +
             // (starts at or below its position) - 1.  Positions at or past
             // T read the sentinel.  The rare-case law runs under a
             // warp-uniform branch.
-            uint32_t before = 0, base = 0;
-            for (; base + 32u < T; base += 64) {
-                const uint32_t r0 = ps - base, r1 = r0 - 32u;
-                const uint32_t m0 = __reduce_or_sync(kFull, bit_at(r0));
-                const uint32_t m1 = __reduce_or_sync(kFull, bit_at(r1));
-                const uint32_t n0 = before + __popc(m0);
-                const uint32_t k0 = base + lane, k1 = k0 + 32;
-                const uint32_t i0 = k0 + wdelta[before + __popc(m0 & le_mask) - 1];
-                const uint32_t d1 = wdelta[n0 + __popc(m1 & le_mask) - 1];
-                const uint32_t i1 = k1 < T ? k1 + d1 : (uint32_t)kMaxStage;
-                const float4 s0 = src[i0], s1 = src[i1];
-                const bool x0 = pair_fast(s0, ax, ay, az);
-                const bool x1 = pair_fast(s1, bx, by, bz);
-                if (__any_sync(kFull, x0 || x1)) {
-                    if (x0) pair_slow(s0, ax, ay, az);
-                    if (x1) pair_slow(s1, bx, by, bz);
-                }
-                before = n0 + __popc(m1);
-            }
-            if (base < T) {
-                const uint32_t r0 = ps - base;
-                const uint32_t m0 = __reduce_or_sync(kFull, bit_at(r0));
+            uint32_t before = 0;
+            for (uint32_t base = 0; base < T; base += 32) {
+                const uint32_t m0 = __reduce_or_sync(kFull, bit_at(ps - base));
                 const uint32_t k0 = base + lane;
                 const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
                 const float4 s0 = src[k0 < T ? k0 + d0 : (uint32_t)kMaxStage];
-                const bool x0 = pair_fast(s0, ax, ay, az);
-                if (__any_sync(kFull, x0)) {
-                    if (x0) pair_slow(s0, ax, ay, az);
+                const bool xa = pair_fast(s0, ta.x, ta.y, ta.z, ax, ay, az);
+                const bool xb = pair_fast(s0, tb.x, tb.y, tb.z, bx, by, bz);
+                if (__any_sync(kFull, xa || xb)) {
+                    if (xa) pair_slow(s0, ta.x, ta.y, ta.z, ax, ay, az);
+                    if (xb) pair_slow(s0, tb.x, tb.y, tb.z, bx, by, bz);
                 }
+                before += __popc(m0);
             }
             __syncwarp();
         }
-        // the warp's sum of the lanes' two accumulator sets
-        ex = ey = ez = 0.f;
-        if (FIXED) {
-            // Compensated by error-free splitting: with V a power of two above
-            // every lane's partial sums, each is split against the quantum
-            // q = V / 2^17 into a multiple of q (h = (v + C) - C, C = 1.5 *
-            // 2^23 q) and an exact remainder l = v - h (|l| <= q/2).  The 64
-            // multiples of q add exactly in any order (|sum| <= 64 V = 2^23 q);
-            // the remainders add in float, their error far below q.  The
-            // result is the pair (sum of the h, sum of the l).
-            const float m = fmaxf(fmaxf(fmaxf(fabsf(ax), fabsf(bx)), fmaxf(fabsf(ay), fabsf(by))),
-                                  fmaxf(fabsf(az), fabsf(bz)));
-            const uint32_t eb = __reduce_max_sync(kFull, __float_as_uint(m) >> 23);  // V = 2^(eb - 126)
-            const float C = __uint_as_float(((eb + 7u) << 23) | 0x400000u);      // 1.5 * 2^6 V
-            auto split2 = [&](float a, float b, float &h, float &l) {
-                const float ha = __fsub_rn(__fadd_rn(a, C), C), hb = __fsub_rn(__fadd_rn(b, C), C);
-                h = __fadd_rn(ha, hb);
-                l = __fadd_rn(__fsub_rn(a, ha), __fsub_rn(b, hb));
-            };
-            split2(ax, bx, ax, ex);
-            split2(ay, by, ay, ey);
-            split2(az, bz, az, ez);
-        } else {
-            ax += bx;
-            ay += by;
-            az += bz;
-        }
-        if (reduce) {
+        // the warp's sums, one target at a time
+        auto reduce = [&](float &x, float &y, float &z, float &ex, float &ey, float &ez) {
+            ex = ey = ez = 0.f;
+            if (FIXED) {
+                // Compensated by error-free splitting: with V a power of two
+                // above every lane's partial sum, each is split against the
+                // quantum q = V / 2^18 into a multiple of q (h = (v + C) - C,
+                // C = 1.5 * 2^23 q) and an exact remainder l = v - h
+                // (|l| <= q/2).  The 32 multiples of q add exactly in any
+                // order (|sum| <= 32 V = 2^23 q); the remainders add in float,
+                // their error far below q.  The result is the pair (sum of the
+                // h, sum of the l).
+                const float m = fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z));
+                const uint32_t eb = __reduce_max_sync(kFull, __float_as_uint(m) >> 23);  // V = 2^(eb - 126)
+                const float C = __uint_as_float(((eb + 6u) << 23) | 0x400000u);       // 1.5 * 2^5 V
+                auto split = [&](float &v, float &l) {
+                    const float h = __fsub_rn(__fadd_rn(v, C), C);
+                    l = __fsub_rn(v, h);
+                    v = h;
+                };
+                split(x, ex);
+                split(y, ey);
+                split(z, ez);
+            }
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
-                ax = __fadd_rn(ax, __shfl_xor_sync(kFull, ax, off));
-                ay = __fadd_rn(ay, __shfl_xor_sync(kFull, ay, off));
-                az = __fadd_rn(az, __shfl_xor_sync(kFull, az, off));
+                x = __fadd_rn(x, __shfl_xor_sync(kFull, x, off));
+                y = __fadd_rn(y, __shfl_xor_sync(kFull, y, off));
+                z = __fadd_rn(z, __shfl_xor_sync(kFull, z, off));
                 if (FIXED) {
                     ex = __fadd_rn(ex, __shfl_xor_sync(kFull, ex, off));
                     ey = __fadd_rn(ey, __shfl_xor_sync(kFull, ey, off));
@@ -684,32 +671,42 @@ __device__ __forceinline__ bool shortrange_segment(
             }
             if (FIXED) {
                 // (sum, error) as a normalised pair for the callers
-                two_sum(ax, ex, ax, ex);
-                two_sum(ay, ey, ay, ey);
-                two_sum(az, ez, az, ez);
+                two_sum(x, ex, x, ex);
+                two_sum(y, ey, y, ey);
+                two_sum(z, ez, z, ez);
             }
-        }
+        };
+        reduce(ax, ay, az, eax, eay, eaz);
+        reduce(bx, by, bz, ebx, eby, ebz);
     };
 
-    // the target's coordinates: pt absolute float (for the culling; fixed
-    // point rounded to float, which the culling margin covers), tx..tz
-    // origin-relative (for the pair law)
-    auto load_target = [&](float4 praw) {
+    // a target's coordinates: absolute float (for the culling; fixed point
+    // rounded to float, which the culling margin covers) and origin-relative
+    // (for the pair law)
+    auto load_target = [&](float4 praw, float4 &rel_out) {
         float4 pt = praw;
         if (FIXED) {
             pt = make_float4(__fmul_rn((float)__float_as_uint(praw.x), fs),
                              __fmul_rn((float)__float_as_uint(praw.y), fs),
                              __fmul_rn((float)__float_as_uint(praw.z), fs), 0.f);
-            const float4 tr = rel(praw);
-            tx = tr.x;
-            ty = tr.y;
-            tz = tr.z;
+            rel_out = rel(praw);
         } else {
-            tx = pt.x - ox;
-            ty = pt.y - oy;
-            tz = pt.z - oz;
+            rel_out = make_float4(pt.x - ox, pt.y - oy, pt.z - oz, 0.f);
         }
         return pt;
+    };
+
+    // the pair (2q, 2q + 1) of round `round`: bounding box and relative
+    // coordinates; a missing second target sits at the sentinel
+    auto load_pair = [&](uint32_t q, float4 &lo, float4 &hi, float4 &ta, float4 &tb, bool &has_b) {
+        const uint32_t t = 2 * q;
+        has_b = t + 1 < nt;
+        const float4 pa = load_target(s_tpos[t], ta);
+        float4 pb = pa;
+        tb = make_float4(kSentinel, kSentinel, kSentinel, 0.f);
+        if (has_b) pb = load_target(s_tpos[t + 1], tb);
+        lo = make_float4(fminf(pa.x, pb.x), fminf(pa.y, pb.y), fminf(pa.z, pb.z), 0.f);
+        hi = make_float4(fmaxf(pa.x, pb.x), fmaxf(pa.y, pb.y), fmaxf(pa.z, pb.z), 0.f);
     };
 
     // force (already scaled by m G) to original order, PM scatter and kick
@@ -787,55 +784,72 @@ __device__ __forceinline__ bool shortrange_segment(
         if (!stage(0, total)) return false;
         __syncthreads();
         for (uint32_t round = 0; round < rounds; ++round) {
-            const uint32_t t = round * kWarps + warp;
-            if (t >= nt) break;  // warp-uniform
-            const float4 pt = load_target(s_tpos[t]);
-            float ax, ay, az, ex, ey, ez;
-            target_chunk(pt, 0, total, ax, ay, az, ex, ey, ez, true);
+            const uint32_t q = round * kWarps + warp;
+            if (q >= npair) break;  // warp-uniform
+            float4 lo, hi, ta, tb;
+            bool has_b;
+            load_pair(q, lo, hi, ta, tb, has_b);
+            float ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz;
+            pair_chunk(lo, hi, ta, tb, 0, total, ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz);
             if (FIXED) {
-                ax = __fadd_rn(ax, ex);
-                ay = __fadd_rn(ay, ey);
-                az = __fadd_rn(az, ez);
+                ax = __fadd_rn(ax, eax);
+                ay = __fadd_rn(ay, eay);
+                az = __fadd_rn(az, eaz);
+                bx = __fadd_rn(bx, ebx);
+                by = __fadd_rn(by, eby);
+                bz = __fadd_rn(bz, ebz);
             }
             if (lane == 0) {
-                s_acc[0][t] = ax * mg;
-                s_acc[1][t] = ay * mg;
-                s_acc[2][t] = az * mg;
+                s_acc[0][2 * q] = ax * mg;
+                s_acc[1][2 * q] = ay * mg;
+                s_acc[2][2 * q] = az * mg;
+                if (has_b) {
+                    s_acc[0][2 * q + 1] = bx * mg;
+                    s_acc[1][2 * q + 1] = by * mg;
+                    s_acc[2][2 * q + 1] = bz * mg;
+                }
             }
         }
-        // the warp's epilogues side by side: lane r takes its round r target
+        // the warp's epilogues side by side: lane 2r + j takes target j of
+        // its round r pair
         __syncwarp();
-        const uint32_t t = lane * kWarps + warp;
-        if (lane < rounds && t < nt) epilogue(t, make_float4(s_acc[0][t], s_acc[1][t], s_acc[2][t], 0.f));
+        const uint32_t t = 2 * ((lane >> 1) * kWarps + warp) + (lane & 1);
+        if ((lane >> 1) < rounds && t < nt) epilogue(t, make_float4(s_acc[0][t], s_acc[1][t], s_acc[2][t], 0.f));
     } else {
         for (uint32_t t = tid; t < nt; t += kThreads)
             for (int k = 0; k < 6; ++k) s_acc[k][t] = 0.f;
+        // target t's running sums (only the warp of t's pair touches them)
+        auto carry = [&](uint32_t t, float x, float y, float z, float ex, float ey, float ez) {
+            if (FIXED) {
+                float e;
+                two_sum(s_acc[0][t], x, s_acc[0][t], e);
+                s_acc[3][t] = __fadd_rn(s_acc[3][t], __fadd_rn(ex, e));
+                two_sum(s_acc[1][t], y, s_acc[1][t], e);
+                s_acc[4][t] = __fadd_rn(s_acc[4][t], __fadd_rn(ey, e));
+                two_sum(s_acc[2][t], z, s_acc[2][t], e);
+                s_acc[5][t] = __fadd_rn(s_acc[5][t], __fadd_rn(ez, e));
+            } else {
+                s_acc[0][t] += x;
+                s_acc[1][t] += y;
+                s_acc[2][t] += z;
+            }
+        };
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
             const uint32_t c1 = min(total, c0 + (uint32_t)kMaxStage);
             __syncthreads();  // the previous chunk is no longer read; s_acc zeroed
             if (!stage(c0, c1)) return false;
             __syncthreads();
             for (uint32_t round = 0; round < rounds; ++round) {
-                const uint32_t t = round * kWarps + warp;
-                if (t >= nt) break;
-                const float4 pt = load_target(s_tpos[t]);
-                float ax, ay, az, ex, ey, ez;
-                target_chunk(pt, c0, c1, ax, ay, az, ex, ey, ez, true);
+                const uint32_t q = round * kWarps + warp;
+                if (q >= npair) break;
+                float4 lo, hi, ta, tb;
+                bool has_b;
+                load_pair(q, lo, hi, ta, tb, has_b);
+                float ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz;
+                pair_chunk(lo, hi, ta, tb, c0, c1, ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz);
                 if (lane == 0) {
-                    // only this warp touches target t's accumulators
-                    if (FIXED) {
-                        float e;
-                        two_sum(s_acc[0][t], ax, s_acc[0][t], e);
-                        s_acc[3][t] = __fadd_rn(s_acc[3][t], __fadd_rn(ex, e));
-                        two_sum(s_acc[1][t], ay, s_acc[1][t], e);
-                        s_acc[4][t] = __fadd_rn(s_acc[4][t], __fadd_rn(ey, e));
-                        two_sum(s_acc[2][t], az, s_acc[2][t], e);
-                        s_acc[5][t] = __fadd_rn(s_acc[5][t], __fadd_rn(ez, e));
-                    } else {
-                        s_acc[0][t] += ax;
-                        s_acc[1][t] += ay;
-                        s_acc[2][t] += az;
-                    }
+                    carry(2 * q, ax, ay, az, eax, eay, eaz);
+                    if (has_b) carry(2 * q + 1, bx, by, bz, ebx, eby, ebz);
                 }
             }
         }

@@ -212,13 +212,15 @@ class Server:
         """Admit/retire, then advance every running job one step.  Returns
         False when nothing is running or waiting."""
         self._retire()
+        # before any re-layout: the boxes' last forces are only in place until
+        # the ensemble is rebuilt (a rebuild carries positions and velocities)
+        self._outputs()
         running = [j for j in self.active if not j.finished]
         new = self._admit() if self.queue else []
         if new or len(running) != len(self.active):
             self._rebuild(running, new)
         if not self.active:
             return bool(self.queue)
-        self._outputs()
         nb = len(self.active)
         d = np.zeros(nb)
         kp = np.zeros(nb)

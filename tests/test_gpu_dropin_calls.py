@@ -95,9 +95,12 @@ def test_long_range_force_vs_oracle(dropin, port):
 def _get_timestep_reference(al, acc_pp, acc_pm):
     """timestep.c:96-138 with the factors advance_and_find_timesteps sets (11-24)."""
     a = al.Time
-    fac1 = 1.0 / (a * a)
-    hubble_a = al.Hubble * math.sqrt(al.Omega0 / a ** 3 + (1 - al.Omega0 - al.OmegaLambda) / a ** 2 +
-                                     al.OmegaLambda)
+    f32 = np.float32
+    # C's float arithmetic where timestep.c mixes only floats and ints:
+    # 1 / (All.Time * All.Time) and 1 - Omega0 - OmegaLambda
+    fac1 = float(f32(1) / (f32(a) * f32(a)))
+    curv = float(f32(1) - f32(al.Omega0) - f32(al.OmegaLambda))
+    hubble_a = al.Hubble * math.sqrt(al.Omega0 / (a * a * a) + curv / (a * a) + al.OmegaLambda)
     acc = fac1 * acc_pp.astype(np.float64) + fac1 * acc_pm.astype(np.float64)
     ac = np.sqrt((acc ** 2).sum(axis=1))
     ac[ac == 0] = 1e-30
