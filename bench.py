@@ -58,6 +58,8 @@ MODE = 0  # 0 plain (float32 positions, the reference's arithmetic), 1 fixed poi
 # default is the plain method at mid size; the others are the precision form
 # (uint32 fixed-point positions) at the same size and both forms at 512^3.
 PRESETS = {
+    "plain-32": (32, 100.0, 64, 16, 0, "plain-32^3-L100-M64-G16-z49to0-200steps"),
+    "precision-32": (32, 100.0, 64, 16, 1, "precision-32^3-L100-M64-G16-z49to0-200steps"),
     "plain-128": (128, 256.0, 256, 64, 0, "plain-128^3-L256-M256-G64-z49to0-200steps"),
     "precision-128": (128, 256.0, 256, 64, 1, "precision-128^3-L256-M256-G64-z49to0-200steps"),
     "plain-512": (512, 1000.0, 1024, 256, 0, "plain-512^3-L1000-M1024-G256-z49to0-200steps"),
@@ -325,15 +327,22 @@ def run_serving(args, world, rank, local):
 SR_TRAFFIC = {"plain-128^3-L256-M256-G64-z49to0-200steps": 148.7e6}
 
 
+# softening (fraction of the mean spacing) of the small box: 0.03, the others 0.025
+SOFT_FRACS = {"plain-32": 0.03, "precision-32": 0.03}
+
+
 def apply_preset(name):
-    global N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD
+    global N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD, SOFT_FRAC
     N_SIDE, BOX_MPC, PM_GRID, CELL_GRID, MODE, WORKLOAD = PRESETS[name]
+    SOFT_FRAC = SOFT_FRACS.get(name, SOFT_FRAC)
 
 
 def workload_config():
     return {"workload": WORKLOAD, "particles": N_SIDE ** 3, "box_mpc_h": BOX_MPC, "pm_grid": PM_GRID,
             "cell_grid": CELL_GRID, "z_init": Z_INIT, "log_a_steps": NSTEPS_RUN, "seed": SEED,
-            "softening": f"{SOFT_FRAC} mean spacing", "l2": "working set > L2 (no flush)",
+            "softening": f"{SOFT_FRAC} mean spacing",
+            "l2": "working set > L2 (no flush)" if N_SIDE >= 128 else
+                  "working set < L2, not flushed between steps (a secondary workload, not the headline)",
             "positions": "uint32 fixed point (L/2^32)" if MODE else "float32"}
 
 
