@@ -11,6 +11,7 @@
 // Particle state (pos, vel, forces) is kept in original particle order so that
 // the permutation the sort produces is the reference's (stable sort of the keys
 // of P[] in index order).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -591,6 +592,44 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     return CUCO_OK;
 }
 
+}  // extern "C"
+
+namespace state_check {
+__global__ void k_count_nonfinite(const float *__restrict__ v, size_t n, uint32_t *__restrict__ count) {
+    uint32_t bad = 0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        bad += !isfinite(v[i]);
+    bad = __reduce_add_sync(0xffffffffu, bad);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(count, bad);
+}
+
+// The staged triplets (b->stage3) must all be finite: a state with a NaN or
+// an infinity is refused before it reaches the box (CUCO_ERR_INVALID).
+cuco_status_t check_finite(cuco_box_t *b, const char *what) {
+    uint32_t *count = b->work.ctl + 3;  // the plan's spare control word
+    CUCO_TRY_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), b->stream));
+    const size_t n = 3 * (size_t)b->n;
+    if (n) {
+        const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+        k_count_nonfinite<<<blocks, 256, 0, b->stream>>>(b->stage3, n, count);
+        CUCO_TRY_CUDA(cudaGetLastError());
+    }
+    uint32_t bad = 0;
+    CUCO_TRY_CUDA(cudaMemcpyAsync(&bad, count, sizeof bad, cudaMemcpyDeviceToHost, b->stream));
+    CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));
+    if (bad) {
+        set_error(std::string("cuco_box_set_state: ") + std::to_string(bad) + " " + what +
+                  " components are not finite");
+        return CUCO_ERR_INVALID;
+    }
+    return CUCO_OK;
+}
+}  // namespace state_check
+
+using state_check::check_finite;
+
+extern "C" {
+
 cuco_status_t cuco_box_set_state(cuco_box_t *b, const float *pos, const float *vel, int on_device) {
     if (!b || !pos) {
         set_error("cuco_box_set_state: null argument");
@@ -599,12 +638,14 @@ cuco_status_t cuco_box_set_state(cuco_box_t *b, const float *pos, const float *v
     const size_t bytes = sizeof(float) * 3 * b->n;
     cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, pos, bytes, kind, b->stream));
+    CUCO_TRY(check_finite(b, "position"));
     if (b->cfg.mode == CUCO_MODE_FIXED)
         CUCO_TRY(to_fixed(b->stage3, b->pos, b->n, b->cfg.boxsize, b->stream));
     else
         CUCO_TRY(pack3to4(b->stage3, b->pos, b->n, b->stream));
     if (vel) {
         CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, vel, bytes, kind, b->stream));
+        CUCO_TRY(check_finite(b, "velocity"));
         CUCO_TRY(pack3to4(b->stage3, b->vel, b->n, b->stream));
     }
     b->has_state = true;
@@ -645,6 +686,7 @@ cuco_status_t cuco_box_set_state_fixed(cuco_box_t *b, const uint32_t *pos, const
     CUCO_TRY(pack3to4(b->stage3, b->pos, b->n, b->stream));
     if (vel) {
         CUCO_TRY_CUDA(cudaMemcpyAsync(b->stage3, vel, bytes, kind, b->stream));
+        CUCO_TRY(check_finite(b, "velocity"));
         CUCO_TRY(pack3to4(b->stage3, b->vel, b->n, b->stream));
     }
     b->has_state = true;

@@ -73,6 +73,7 @@ class Job:
     a: np.ndarray = field(default=None, repr=False)   # scale factor after each step
     snapshots: list = field(default_factory=list)     # paths written, in order
     next_output: int = 0
+    cancelled: bool = False
 
     @property
     def finished(self) -> bool:
@@ -145,15 +146,52 @@ class Server:
         self.rebuild_s = 0.0             # host time spent rebuilding ensembles
         self.peak_active = 0             # most jobs running at once
         self.updates = 0                 # particle-updates done
+        self.cancelled_ids: set = set()  # cancelled before they arrived
+        self.refused: list[Job] = []     # refused at submission (invalid initial state)
 
     # -------------------------------------------------------------- intake
     def submit(self, job: Job):
+        """Queue a job.  A job whose initial positions or velocities are not
+        all finite, or do not match its particle count, is refused (ValueError)
+        and recorded in `refused`; nothing already queued or running is
+        touched."""
         if job.config.mode != self.mode:
             raise ValueError("job mode differs from the server's")
+        n = job.config.n
+        pos, vel = np.asarray(job.pos), np.asarray(job.vel)
+        if pos.shape != (n, 3) or vel.shape != (n, 3) or not (np.isfinite(pos).all() and np.isfinite(vel).all()):
+            job.cancelled = True
+            self.refused.append(job)
+            raise ValueError(f"job {job.job_id}: initial state is not {n} finite positions and velocities")
+        if job.job_id in self.cancelled_ids:
+            job.cancelled = True
+            job.done = self.clock()
+            self.finished.append(job)
+            return
         job.a, job.drift, job.kick = fixed_step_schedule(job.a_begin, 1.0, job.steps)
         if job.outputs and not job.output_dir:
             raise ValueError("a job with output times needs an output directory")
         self.queue.append(job)
+
+    def cancel(self, job_id) -> None:
+        """Cancel a job: a waiting job leaves the queue, a running one stops
+        after the step in flight and leaves the ensemble at the next tick (no
+        result), a job not yet submitted is dropped when it arrives.  The other
+        jobs' trajectories do not change (each job's result is independent of
+        the mix)."""
+        for j in self.queue:
+            if j.job_id == job_id:
+                self.queue.remove(j)
+                j.cancelled = True
+                j.done = self.clock()
+                self.finished.append(j)
+                return
+        for j in self.active:
+            if j.job_id == job_id and not j.finished:
+                j.cancelled = True
+                j.next_step = j.steps + 1  # finished: retired without a result
+                return
+        self.cancelled_ids.add(job_id)
 
     def _admit(self) -> list[Job]:
         new = []
@@ -201,7 +239,7 @@ class Server:
         now = self.clock()
         for k, j in enumerate(self.active):
             if j.finished and j.done is None:
-                if self.keep_results:
+                if self.keep_results and not j.cancelled:
                     pos, vel, _, _ = self.ens.get_state(k)
                     j.result_pos, j.result_vel = pos, vel
                 j.done = now
@@ -270,7 +308,10 @@ class Server:
         while i < len(pending) or self.queue or any(not j.finished for j in self.active):
             now = self.clock()
             while i < len(pending) and pending[i].arrival <= now:
-                self.submit(pending[i])
+                try:
+                    self.submit(pending[i])
+                except ValueError:
+                    pass  # refused (recorded in self.refused); the stream goes on
                 i += 1
             if not self.tick() and i < len(pending):
                 # idle: nothing to run until the next arrival

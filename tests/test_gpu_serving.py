@@ -129,3 +129,36 @@ def test_output_times_write_snapshots_without_changing_the_run(tmp_path):
         assert np.array_equal(parts["Vel"], vel)
         assert np.array_equal(parts["GravAccel"], app) and np.array_equal(parts["GravPM"], apm)
     box.close()
+
+
+def test_faults_on_the_host_leave_the_other_jobs_unchanged():
+    """Failures made on the host (no GPU fault): a job whose initial state
+    carries a NaN is refused at submission, and a running job is cancelled
+    mid-run.  Every other job finishes with the result it has alone, bit for
+    bit; the cancelled job leaves without a result."""
+    jobs = make_jobs()
+    bad = jobs[2]
+    bad.pos = bad.pos.copy()
+    bad.pos[17, 1] = np.nan  # injected into the host-side copy of the state
+    srv = Server(1 << 40, clock=None)
+    srv.clock = lambda: float(srv.ticks)
+    tick = srv.tick
+
+    ran = {}
+
+    def cancelling_tick():
+        if srv.ticks == 5:
+            ran["steps"] = jobs[1].next_step
+            srv.cancel(1)  # job 1 arrived at tick 1 and is running
+        return tick()
+
+    srv.tick = cancelling_tick
+    done = {j.job_id: j for j in srv.run(jobs)}
+    assert [j.job_id for j in srv.refused] == [2] and 2 not in done
+    assert done[1].cancelled and done[1].result_pos is None
+    assert 0 < ran["steps"] < jobs[1].steps  # it was running and stopped early
+    for k in (0, 3, 4):
+        alone, _, _ = serve([make_jobs()[k]])
+        assert not done[k].cancelled
+        assert np.array_equal(done[k].result_pos, alone[k].result_pos)
+        assert np.array_equal(done[k].result_vel, alone[k].result_vel)

@@ -104,3 +104,50 @@ def test_box_snapshot_load_save(tmp_path, mode):
     for b in (box, box2, box3):
         b.close()
     os.remove(snap)
+
+
+def test_read_ic_exits_on_a_truncated_file(tmp_path):
+    """read_ic.c:12-15 exits with a message on a missing file; the library's
+    read_ic does the same for a file that ends before its particles."""
+    import subprocess
+    import sys
+    ic = _ic()
+    src = tmp_path / "ic.cuco"
+    write_cuco(str(src), ic)
+    raw = np.fromfile(src, dtype=np.uint8)
+    (tmp_path / "short.cuco").write_bytes(raw[: 32 + 60 * (ic.n // 2)].tobytes())
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for name in ("short.cuco", "missing.cuco"):
+        code = ("import sys; sys.path.insert(0, %r); from cuco_gb300 import _native; "
+                "_native.load().read_ic(%r)" % (root, str(tmp_path / name).encode()))
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+        assert r.returncode == 1, (r.returncode, r.stdout, r.stderr)
+        assert "initial condition file" in r.stdout.lower()
+
+
+@pytest.mark.gpu
+def test_invalid_state_and_files_are_refused(tmp_path):
+    """An invalid IC file (truncated) and a state with a NaN injected into the
+    host-side copy are refused with an error status; the box keeps working."""
+    ic = _ic(16, 9)
+    soft = 2.8 * 0.03 * ic.boxsize / 16
+    box = Box(BoxConfig(n=ic.n, pm_grid=32, boxsize=ic.boxsize, mass=ic.mass, G=ics.G_INTERNAL, softening=soft))
+    src = tmp_path / "ic.cuco"
+    write_cuco(str(src), ic)
+    raw = np.fromfile(src, dtype=np.uint8)
+    (tmp_path / "short.cuco").write_bytes(raw[:-60].tobytes())
+    with pytest.raises(Exception, match="ends before"):
+        box.load_snapshot(str(tmp_path / "short.cuco"))
+    pos = ic.pos.copy()
+    pos[123, 2] = np.nan
+    with pytest.raises(Exception, match="not finite"):
+        box.set_state(pos, ic.canonical_velocity())
+    vel = ic.canonical_velocity().copy()
+    vel[5, 0] = np.inf
+    with pytest.raises(Exception, match="not finite"):
+        box.set_state(ic.pos, vel)
+    box.set_state(ic.pos, ic.canonical_velocity())
+    box.forces()
+    _, _, app, apm = box.get_state()
+    assert np.isfinite(app).all() and np.isfinite(apm).all()
+    box.close()
