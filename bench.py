@@ -665,6 +665,15 @@ def run_gpu_arm(args, world, rank, local):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    if args.step_log:
+        # an untimed pass of the whole run with every step timed by phase and
+        # written as one JSON line (each step waits for the one before)
+        from cuco_gb300.steplog import StepLog
+        box.set_state(ic.pos, vel0)
+        log = StepLog(args.step_log)
+        box.run(drift, kick, a=a, log=log)
+        log.close()
+        line["step_log"] = args.step_log
     box.close()
     if args.e2e_steps and MODE == 0:
         line["e2e"] = run_e2e(min(args.e2e_steps, K), ic, soft, local)
@@ -761,6 +770,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--step-log", default=None,
+                    help="write an untimed pass of the whole run, one JSON line per step with phase times")
     ap.add_argument("--workload", default="plain-128", choices=sorted(PRESETS) + [BATCHED, BATCHED_256, SERVING])
     ap.add_argument("--baseline-steps", type=int, default=20)
     ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")

@@ -184,6 +184,26 @@ class Box:
         check(self.lib.cuco_box_step(self.h, drift, kick_pp, kick_pp if kick_pm is None else kick_pm),
               "cuco_box_step")
 
+    def run(self, drift, kick_pp, kick_pm=None, a=None, log=None, first_step: int = 0):
+        """Steps with the given factors (arrays).  With `log` (a
+        steplog.StepLog) every step is timed by phase and logged - each step
+        then waits for the one before, so a logged run is not a timed one."""
+        n = len(drift)
+        if log is not None:
+            self.enable_timing(True)
+        for k in range(n):
+            self.step(drift[k], kick_pp[k], None if kick_pm is None else kick_pm[k])
+            if log is not None:
+                self.sync()
+                t = self.timings()
+                rec = {"step": first_step + k, "phase_ms": {p: round(v, 5) for p, v in t.items()},
+                       "particle_updates_per_s": self.n / (t["total"] * 1e-3) if t["total"] > 0 else None}
+                if a is not None:
+                    rec["a"] = float(a[k])
+                log.write("box_step", **rec)
+        if log is not None:
+            self.enable_timing(False)
+
     def sync(self):
         check(self.lib.cuco_box_sync(self.h), "cuco_box_sync")
 

@@ -35,6 +35,7 @@ rank every world-th job in arrival order, with no exchange between ranks.
 from __future__ import annotations
 
 import ctypes
+import json
 import os
 import time
 from dataclasses import dataclass, field
@@ -74,6 +75,20 @@ class Job:
     snapshots: list = field(default_factory=list)     # paths written, in order
     next_output: int = 0
     cancelled: bool = False
+    start_step: int = 0          # a job resumed from a checkpoint starts here
+
+    @classmethod
+    def from_checkpoint(cls, path: str, arrival: float = 0.0) -> "Job":
+        """A job resumed from `checkpoint` files: the state of the snapshot,
+        the schedule continuing at the step after it."""
+        from .ics import read_cuco
+        with open(path + ".json") as fh:
+            meta = json.load(fh)
+        _, parts = read_cuco(path)
+        cfg = BoxConfig(**meta["config"])
+        return cls(meta["job_id"], cfg, np.ascontiguousarray(parts["Pos"]), np.ascontiguousarray(parts["Vel"]),
+                   meta["a_begin"], meta["steps"], arrival=arrival, outputs=tuple(meta["outputs"]),
+                   output_dir=meta["output_dir"], start_step=meta["next_step"])
 
     @property
     def finished(self) -> bool:
@@ -131,12 +146,13 @@ def footprint(configs: list[BoxConfig]) -> int:
 
 class Server:
     def __init__(self, hbm_budget: int, max_active: int = 1 << 30, mode: int = MODE_FIXED,
-                 clock=time.perf_counter, keep_results: bool = True):
+                 clock=time.perf_counter, keep_results: bool = True, log=None):
         self.budget = hbm_budget
         self.max_active = max_active
         self.mode = mode
         self.clock = clock
         self.keep_results = keep_results
+        self.log = log                   # a steplog.StepLog: one record per tick and per finished job
         self.queue: list[Job] = []       # arrived, waiting
         self.active: list[Job] = []      # resident, in the ensemble's box order
         self.finished: list[Job] = []
@@ -169,6 +185,9 @@ class Server:
             self.finished.append(job)
             return
         job.a, job.drift, job.kick = fixed_step_schedule(job.a_begin, 1.0, job.steps)
+        job.next_step = job.start_step
+        while job.next_output < len(job.outputs) and job.outputs[job.next_output] <= job.a[max(job.start_step - 1, 0)]:
+            job.next_output += 1  # outputs before a resumed job's state were written before it stopped
         if job.outputs and not job.output_dir:
             raise ValueError("a job with output times needs an output directory")
         self.queue.append(job)
@@ -192,6 +211,30 @@ class Server:
                 j.next_step = j.steps + 1  # finished: retired without a result
                 return
         self.cancelled_ids.add(job_id)
+
+    def checkpoint(self, job_id, path: str) -> None:
+        """Write a running job's state: a `.cuco` snapshot at `path` (positions
+        after its last step, the velocities as they stand, its last forces)
+        and the job's schedule position in `path + ".json"`.  A job made by
+        Job.from_checkpoint continues the run where it stands; in the plain
+        form it ends bit-identical to the uninterrupted job, in the
+        fixed-point form the positions pass through float32 once (about
+        1e-7 of the box)."""
+        for k, j in enumerate(self.active):
+            if j.job_id == job_id and not j.finished:
+                if j.next_step == 0:
+                    raise RuntimeError(f"job {job_id} has not run a step yet")
+                self.ens.sync()
+                pos, vel, app, apm = self.ens.get_state(k)
+                write_snapshot(path, j, float(j.a[j.next_step - 1]), pos, vel, app, apm)
+                c = j.config
+                meta = {"job_id": j.job_id, "a_begin": j.a_begin, "steps": j.steps, "next_step": j.next_step,
+                        "outputs": list(j.outputs), "output_dir": j.output_dir,
+                        "config": {f: getattr(c, f) for f in c.__dataclass_fields__}}
+                with open(path + ".json", "w") as fh:
+                    json.dump(meta, fh)
+                return
+        raise KeyError(f"job {job_id} is not running")
 
     def _admit(self) -> list[Job]:
         new = []
@@ -244,6 +287,9 @@ class Server:
                     j.result_pos, j.result_vel = pos, vel
                 j.done = now
                 self.finished.append(j)
+                if self.log is not None:
+                    self.log.write("job_done", job=j.job_id, latency=j.done - j.arrival, steps=j.next_step,
+                                   cancelled=j.cancelled, particles=j.config.n)
 
     # ---------------------------------------------------------------- tick
     def tick(self) -> bool:
@@ -271,6 +317,10 @@ class Server:
                 j.next_step += 1
                 self.updates += j.config.n
         self.ticks += 1
+        if self.log is not None:
+            self.log.write("tick", tick=self.ticks, time=self.clock(),
+                           running=sum(not j.finished for j in self.active), queued=len(self.queue),
+                           updates=self.updates)
         return True
 
     def _outputs(self):

@@ -140,7 +140,10 @@ def test_faults_on_the_host_leave_the_other_jobs_unchanged():
     bad = jobs[2]
     bad.pos = bad.pos.copy()
     bad.pos[17, 1] = np.nan  # injected into the host-side copy of the state
-    srv = Server(1 << 40, clock=None)
+    import io
+    from cuco_gb300 import steplog
+    buf = io.StringIO()
+    srv = Server(1 << 40, clock=None, log=steplog.StepLog(buf))
     srv.clock = lambda: float(srv.ticks)
     tick = srv.tick
 
@@ -157,8 +160,55 @@ def test_faults_on_the_host_leave_the_other_jobs_unchanged():
     assert [j.job_id for j in srv.refused] == [2] and 2 not in done
     assert done[1].cancelled and done[1].result_pos is None
     assert 0 < ran["steps"] < jobs[1].steps  # it was running and stopped early
+    # the structured log: one record per tick, one per finished job
+    import json
+    recs = [json.loads(x) for x in buf.getvalue().splitlines()]
+    assert 0 < sum(r["kind"] == "tick" for r in recs) <= srv.ticks
+    finished = {r["job"]: r for r in recs if r["kind"] == "job_done"}
+    assert set(finished) == {0, 1, 3, 4} and finished[1]["cancelled"]
     for k in (0, 3, 4):
         alone, _, _ = serve([make_jobs()[k]])
         assert not done[k].cancelled
         assert np.array_equal(done[k].result_pos, alone[k].result_pos)
         assert np.array_equal(done[k].result_vel, alone[k].result_vel)
+
+
+def test_checkpoint_and_resume(tmp_path):
+    """A running job checkpointed (snapshot + schedule position), cancelled,
+    and resumed in another server ends bit-identical to the job run without
+    interruption (plain form: the state crosses the file exactly)."""
+    def plain_jobs():
+        out = []
+        for j in make_jobs()[:3]:
+            cfg = BoxConfig(**{**j.config.__dict__, "mode": 0})
+            out.append(Job(j.job_id, cfg, j.pos, j.vel, j.a_begin, j.steps, arrival=0.0))
+        return out
+
+    def run(server, jobs, hook=None):
+        server.clock = lambda: float(server.ticks)
+        if hook:
+            tick = server.tick
+
+            def hooked():
+                hook(server)
+                return tick()
+            server.tick = hooked
+        return {j.job_id: j for j in server.run(jobs)}
+
+    ref = run(Server(1 << 40, mode=0, clock=None), plain_jobs())
+    ck = str(tmp_path / "job1.cuco")
+
+    def stop_job1(server):
+        if server.ticks == 4:
+            server.checkpoint(1, ck)
+            server.cancel(1)
+
+    first = run(Server(1 << 40, mode=0, clock=None), plain_jobs(), stop_job1)
+    assert first[1].cancelled
+    resumed = Job.from_checkpoint(ck)
+    assert 0 < resumed.start_step < resumed.steps
+    second = run(Server(1 << 40, mode=0, clock=None), [resumed])
+    assert np.array_equal(second[1].result_pos, ref[1].result_pos)
+    assert np.array_equal(second[1].result_vel, ref[1].result_vel)
+    for k in (0, 2):  # the others were not disturbed
+        assert np.array_equal(first[k].result_pos, ref[k].result_pos)
