@@ -256,7 +256,8 @@ def run_serving(args, world, rank, local):
     for j in jobs:
         sizes_seen.setdefault((j.config.n, j.config.pm_grid), j.config)
     Ensemble(list(sizes_seen.values())).close()
-    srv = Server(int(args.hbm_budget_gb * 1e9), mode=mode, keep_results=False)
+    srv = Server(int(args.hbm_budget_gb * 1e9), max_active=args.max_active, mode=mode, keep_results=False,
+                 solo_threshold=args.solo_threshold or None)
     clocks = ClockSampler(local)
     clocks.start()
     t0 = time.perf_counter()
@@ -303,6 +304,8 @@ def run_serving(args, world, rank, local):
         "dtype": "u32+f32" if mode else "f32", "data": "synthetic",
         "config": {"workload": f"serving-{len(stream_all)}jobs-poisson20-N32to192-M2N-L50to500-50to200steps",
                    "jobs": len(stream_all), "arrival_rate_per_s": 20.0, "hbm_budget_gb": args.hbm_budget_gb,
+                   "max_active": args.max_active if args.max_active < (1 << 30) else None,
+                   "solo_threshold_particles": args.solo_threshold or None,
                    "sharding": f"jobs split by rank ({world} rank(s)), no exchange",
                    "n_side_min": min(sizes), "n_side_max": max(sizes),
                    "positions": "uint32 fixed point (L/2^32)" if mode else "float32",
@@ -777,6 +780,10 @@ def main():
     ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")
     ap.add_argument("--baseline-jobs", type=int, default=8, help="serving: jobs run alone on the plain path")
     ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
+    ap.add_argument("--solo-threshold", type=int, default=96 ** 3,
+                    help="serving: jobs of at least this many particles run on boxes of their own (0: none)")
+    ap.add_argument("--max-active", type=int, default=1 << 30,
+                    help="serving: most jobs running at once (besides the HBM budget)")
     ap.add_argument("--serving-mode", default="plain", choices=["plain", "fixed"],
                     help="serving: precision of the served ensemble")
     args = ap.parse_args()

@@ -44,7 +44,7 @@ import numpy as np
 
 from . import _native
 from ._native import check
-from .engine import MODE_FIXED, BoxConfig, cosmo_factors, fixed_step_schedule
+from .engine import MODE_FIXED, Box, BoxConfig, cosmo_factors, fixed_step_schedule
 from .ensemble import Ensemble
 from .ics import HEADER_DTYPE, PARTICLE_DTYPE
 
@@ -76,6 +76,7 @@ class Job:
     next_output: int = 0
     cancelled: bool = False
     start_step: int = 0          # a job resumed from a checkpoint starts here
+    box: object = field(default=None, repr=False)  # its own Box when it runs outside the ensemble
 
     @classmethod
     def from_checkpoint(cls, path: str, arrival: float = 0.0) -> "Job":
@@ -145,9 +146,17 @@ def footprint(configs: list[BoxConfig]) -> int:
 
 
 class Server:
+    """`solo_threshold`: jobs of at least this many particles run on boxes of
+    their own (the one-box path, each on its own stream, stepped every tick
+    beside the ensemble) instead of in the ensemble: a box that fills the GPU
+    by itself gains nothing from batching and runs faster alone.  None keeps
+    every job in the ensemble."""
+
     def __init__(self, hbm_budget: int, max_active: int = 1 << 30, mode: int = MODE_FIXED,
-                 clock=time.perf_counter, keep_results: bool = True, log=None):
+                 clock=time.perf_counter, keep_results: bool = True, log=None, solo_threshold: int | None = None):
         self.budget = hbm_budget
+        self.solo_threshold = solo_threshold
+        self.solo: list[Job] = []        # running on boxes of their own
         self.max_active = max_active
         self.mode = mode
         self.clock = clock
@@ -205,7 +214,7 @@ class Server:
                 j.done = self.clock()
                 self.finished.append(j)
                 return
-        for j in self.active:
+        for j in self.active + self.solo:
             if j.job_id == job_id and not j.finished:
                 j.cancelled = True
                 j.next_step = j.steps + 1  # finished: retired without a result
@@ -220,12 +229,15 @@ class Server:
         form it ends bit-identical to the uninterrupted job, in the
         fixed-point form the positions pass through float32 once (about
         1e-7 of the box)."""
-        for k, j in enumerate(self.active):
+        for k, j in list(enumerate(self.active)) + [(None, j) for j in self.solo]:
             if j.job_id == job_id and not j.finished:
                 if j.next_step == 0:
                     raise RuntimeError(f"job {job_id} has not run a step yet")
-                self.ens.sync()
-                pos, vel, app, apm = self.ens.get_state(k)
+                if k is None:
+                    pos, vel, app, apm = j.box.get_state()
+                else:
+                    self.ens.sync()
+                    pos, vel, app, apm = self.ens.get_state(k)
                 write_snapshot(path, j, float(j.a[j.next_step - 1]), pos, vel, app, apm)
                 c = j.config
                 meta = {"job_id": j.job_id, "a_begin": j.a_begin, "steps": j.steps, "next_step": j.next_step,
@@ -236,16 +248,27 @@ class Server:
                 return
         raise KeyError(f"job {job_id} is not running")
 
-    def _admit(self) -> list[Job]:
-        new = []
-        while self.queue and len(self.active) + len(new) < self.max_active:
-            cand = self.active + new + [self.queue[0]]
-            if footprint([j.config for j in cand]) > self.budget:
-                if not self.active and not new:
-                    raise RuntimeError(f"job {self.queue[0].job_id} alone exceeds the HBM budget")
+    def _is_solo(self, job: Job) -> bool:
+        return self.solo_threshold is not None and job.config.n >= self.solo_threshold
+
+    def _admit(self) -> tuple[list[Job], list[Job]]:
+        """(new ensemble jobs, new solo jobs) that fit beside the running ones."""
+        new, new_solo = [], []
+        solo_bytes = sum(footprint([j.config]) for j in self.solo if not j.finished)
+        running = len(self.active) + sum(not j.finished for j in self.solo)
+        while self.queue and running + len(new) + len(new_solo) < self.max_active:
+            job = self.queue[0]
+            solo = self._is_solo(job)
+            ens_jobs = self.active + new + ([] if solo else [job])
+            extra = footprint([job.config]) if solo else 0
+            need = (footprint([j.config for j in ens_jobs]) if ens_jobs else 0) + solo_bytes + extra
+            if need > self.budget:
+                if running == 0 and not new and not new_solo:
+                    raise RuntimeError(f"job {job.job_id} alone exceeds the HBM budget")
                 break
-            new.append(self.queue.pop(0))
-        return new
+            (new_solo if solo else new).append(self.queue.pop(0))
+            solo_bytes += extra
+        return new, new_solo
 
     # ------------------------------------------------------------- rebuild
     def _rebuild(self, keep: list[Job], new: list[Job]):
@@ -273,9 +296,18 @@ class Server:
 
     def _retire(self):
         """Collect finished jobs' results (their boxes stay in the ensemble,
-        frozen, until the next rebuild).  A job is done when the GPU has run
-        its last step: the ensemble's stream is waited for before the time is
-        taken, only on ticks where a job finishes."""
+        frozen, until the next rebuild; a solo job's box is released).  A job
+        is done when the GPU has run its last step: the stream is waited for
+        before the time is taken, only on ticks where a job finishes."""
+        for j in [j for j in self.solo if j.finished and j.done is None]:
+            j.box.sync()
+            if self.keep_results and not j.cancelled:
+                pos, vel, _, _ = j.box.get_state()
+                j.result_pos, j.result_vel = pos, vel
+            j.box.close()
+            j.box = None
+            self.solo.remove(j)
+            self._done(j, self.clock())
         if not any(j.finished and j.done is None for j in self.active):
             return
         self.ens.sync()
@@ -285,11 +317,14 @@ class Server:
                 if self.keep_results and not j.cancelled:
                     pos, vel, _, _ = self.ens.get_state(k)
                     j.result_pos, j.result_vel = pos, vel
-                j.done = now
-                self.finished.append(j)
-                if self.log is not None:
-                    self.log.write("job_done", job=j.job_id, latency=j.done - j.arrival, steps=j.next_step,
-                                   cancelled=j.cancelled, particles=j.config.n)
+                self._done(j, now)
+
+    def _done(self, j: Job, now: float):
+        j.done = now
+        self.finished.append(j)
+        if self.log is not None:
+            self.log.write("job_done", job=j.job_id, latency=j.done - j.arrival, steps=j.next_step,
+                           cancelled=j.cancelled, particles=j.config.n)
 
     # ---------------------------------------------------------------- tick
     def tick(self) -> bool:
@@ -300,26 +335,38 @@ class Server:
         # the ensemble is rebuilt (a rebuild carries positions and velocities)
         self._outputs()
         running = [j for j in self.active if not j.finished]
-        new = self._admit() if self.queue else []
+        new, new_solo = self._admit() if self.queue else ([], [])
         if new or len(running) != len(self.active):
             self._rebuild(running, new)
-        if not self.active:
+        for j in new_solo:
+            cfg = BoxConfig(**{**j.config.__dict__, "cell_grid": None})
+            j.box = Box(cfg)
+            j.box.set_state(j.pos, j.vel)
+            j.admitted = self.clock()
+            self.solo.append(j)
+        if new_solo:
+            self.peak_active = max(self.peak_active, len(self.active) + len(self.solo))
+        if not self.active and not self.solo:
             return bool(self.queue)
-        nb = len(self.active)
-        d = np.zeros(nb)
-        kp = np.zeros(nb)
-        for k, j in enumerate(self.active):
+        if self.active:
+            nb = len(self.active)
+            d = np.zeros(nb)
+            kp = np.zeros(nb)
+            for k, j in enumerate(self.active):
+                if not j.finished:
+                    d[k], kp[k] = j.drift[j.next_step], j.kick[j.next_step]
+            self.ens.step(d, kp, kp)
+        for j in self.solo:
             if not j.finished:
-                d[k], kp[k] = j.drift[j.next_step], j.kick[j.next_step]
-        self.ens.step(d, kp, kp)
-        for j in self.active:
+                j.box.step(j.drift[j.next_step], j.kick[j.next_step])
+        for j in self.active + self.solo:
             if not j.finished:
                 j.next_step += 1
                 self.updates += j.config.n
         self.ticks += 1
         if self.log is not None:
             self.log.write("tick", tick=self.ticks, time=self.clock(),
-                           running=sum(not j.finished for j in self.active), queued=len(self.queue),
+                           running=sum(not j.finished for j in self.active + self.solo), queued=len(self.queue),
                            updates=self.updates)
         return True
 
@@ -328,14 +375,14 @@ class Server:
         step s (s >= 1) drifts a[s-1] -> a[s]; an output a_out in (a[s-1],
         a[s]] is the state after step s-1 drifted to a_out (run.c:49-59).
         Output times at or before the start are skipped."""
-        for k, j in enumerate(self.active):
+        for k, j in list(enumerate(self.active)) + [(None, j) for j in self.solo]:
             s = j.next_step
             if j.finished or not j.outputs or s == 0:
                 continue
             while j.next_output < len(j.outputs) and j.outputs[j.next_output] <= j.a[s]:
                 a_out = j.outputs[j.next_output]
                 if a_out > j.a[0]:
-                    pos, vel, app, apm = self.ens.get_state(k)
+                    pos, vel, app, apm = self.ens.get_state(k) if k is not None else j.box.get_state()
                     drift = cosmo_factors(j.a[s - 1], a_out, j.omega0, j.omega_lambda)[0]
                     path = os.path.join(j.output_dir, f"job{j.job_id}_{j.next_output:03d}.cuco")
                     write_snapshot(path, j, a_out, output_positions(pos, vel, drift, j.config.boxsize), vel,
@@ -355,7 +402,7 @@ class Server:
         for j in pending:
             j.arrival += t0
         i = 0
-        while i < len(pending) or self.queue or any(not j.finished for j in self.active):
+        while i < len(pending) or self.queue or any(not j.finished for j in self.active + self.solo):
             now = self.clock()
             while i < len(pending) and pending[i].arrival <= now:
                 try:
@@ -381,3 +428,8 @@ class Server:
         if self.ens is not None:
             self.ens.close()
             self.ens = None
+        for j in self.solo:
+            if j.box is not None:
+                j.box.close()
+                j.box = None
+        self.solo = []

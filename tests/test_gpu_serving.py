@@ -212,3 +212,41 @@ def test_checkpoint_and_resume(tmp_path):
     assert np.array_equal(second[1].result_vel, ref[1].result_vel)
     for k in (0, 2):  # the others were not disturbed
         assert np.array_equal(first[k].result_pos, ref[k].result_pos)
+
+
+def test_large_jobs_on_boxes_of_their_own():
+    """With a solo threshold, the larger jobs run on boxes of their own (the
+    one-box path, stepped every tick beside the ensemble): each job's result
+    is the same alone and in the mix, and a solo job's result is the one-box
+    path's own."""
+    from cuco_gb300 import Box, fixed_step_schedule
+    threshold = 20 ** 3  # jobs 1 (20^3) and 3 (24^3) go solo
+
+    def run(jobs):
+        srv = Server(1 << 40, clock=None, solo_threshold=threshold)
+        srv.clock = lambda: float(srv.ticks)
+        peak = [0]
+        tick = srv.tick
+
+        def counting():
+            r = tick()
+            peak[0] = max(peak[0], len(srv.solo))
+            return r
+        srv.tick = counting
+        return {j.job_id: j for j in srv.run(jobs)}, peak[0]
+
+    mix, peak_solo = run(make_jobs())
+    assert len(mix) == len(JOBS) and peak_solo == 2
+    for job in make_jobs():
+        alone, _ = run([job])
+        assert np.array_equal(mix[job.job_id].result_pos, alone[job.job_id].result_pos)
+        assert np.array_equal(mix[job.job_id].result_vel, alone[job.job_id].result_vel)
+    j3 = make_jobs()[3]
+    _, drift, kick = fixed_step_schedule(j3.a_begin, 1.0, j3.steps)
+    box = Box(BoxConfig(**{**j3.config.__dict__, "cell_grid": None}))
+    box.set_state(j3.pos, j3.vel)
+    for s in range(j3.steps + 1):
+        box.step(drift[s], kick[s])
+    pos, vel, _, _ = box.get_state()
+    box.close()
+    assert np.array_equal(mix[3].result_pos, pos) and np.array_equal(mix[3].result_vel, vel)
