@@ -1222,12 +1222,27 @@ cuco_status_t pm_plan_create(PMPlan *plan, int M, float boxsize, float asmth, fl
     for (int t = 0; t < M; ++t) tw[t] = make_float2((float)cos(2 * M_PI * t / M), (float)-sin(2 * M_PI * t / M));
     CUCO_TRY_CUDA(cudaMemcpy(plan->green1d, g.data(), sizeof(float) * Mh, cudaMemcpyHostToDevice));
     CUCO_TRY_CUDA(cudaMemcpy(plan->twiddle, tw.data(), sizeof(float2) * M, cudaMemcpyHostToDevice));
+    // The shared-memory limit is an attribute of the kernel, not of a launch:
+    // it is set once to the most a CTA can have, so that boxes of different
+    // meshes in one process (a serving loop's) never lower it under each
+    // other's launches.
     const int P = fft_batch_z(M), B = fft_batch_axis(M);
-    size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
-    size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
-    CUCO_TRY_CUDA(cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
-    CUCO_TRY_CUDA(cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
-    CUCO_TRY_CUDA(cudaFuncSetAttribute(k_fft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
+    const size_t smz = sizeof(float2) * (2 * (size_t)M * (P + 1) + M);
+    const size_t sma = sizeof(float2) * (2 * (size_t)M * B + M);
+    constexpr int kMaxSmem = 227 * 1024;
+    if (smz > (size_t)kMaxSmem || sma > (size_t)kMaxSmem) {
+        set_error("PM: the transform of this mesh needs more shared memory than a CTA has");
+        return CUCO_ERR_UNSUPPORTED;
+    }
+    static const cudaError_t attr = [] {
+        cudaError_t e = cudaFuncSetAttribute(k_fft_z_r2c, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_fft_z_c2r, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_fft_axis, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmem);
+        return e;
+    }();
+    CUCO_TRY_CUDA(attr);
     return CUCO_OK;
 }
 
