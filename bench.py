@@ -780,7 +780,7 @@ def main():
     ap.add_argument("--jobs", type=int, default=120, help="serving: jobs in the stream")
     ap.add_argument("--baseline-jobs", type=int, default=8, help="serving: jobs run alone on the plain path")
     ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
-    ap.add_argument("--solo-threshold", type=int, default=96 ** 3,
+    ap.add_argument("--solo-threshold", type=int, default=0,
                     help="serving: jobs of at least this many particles run on boxes of their own (0: none)")
     ap.add_argument("--max-active", type=int, default=1 << 30,
                     help="serving: most jobs running at once (besides the HBM budget)")
