@@ -95,6 +95,8 @@ SIGNATURES = {
     "radixSortFloatKeys": (None, [_P, _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
     "radixSortFloatKeysOnly": (None, [_P, _P, _P, _P, _P, ctypes.c_size_t, _U, _U, ctypes.c_bool]),
     "cuco_radixsort_overflow": (None, [_U, _U]),
+    "cuco_box_selftest_timeout": (_I, [_P, _D]),
+    "cuco_debug_bounds_violations": (_I, [_P]),
     "read_ic": (None, [ctypes.c_char_p]),
     "savepositions": (None, [_I]),
     "cuco_box_load_snapshot": (_I, [_P, ctypes.c_char_p, _I, _P]),
@@ -173,11 +175,14 @@ SIGNATURES = {
 _lib = None
 
 
-def load(path: str = LIB_PATH):
-    """Load the native library (once).  Raises CucoError if it is not built."""
+def load(path: str | None = None):
+    """Load the native library (once).  Raises CucoError if it is not built.
+    $CUCO_LIBRARY selects another build of it (the debug build with bounds
+    checks, libcuco_gb300_debug.so)."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("CUCO_LIBRARY") or LIB_PATH
     if not os.path.isfile(path):
         raise CucoError(f"{path} is missing: build it with cuco_gb300.build.build() "
                         "(python -c 'import __graft_entry__ as g; g.build()')")

@@ -38,16 +38,24 @@ def _newer(target: str, deps: list[str]) -> bool:
     return all(os.path.getmtime(d) <= t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | None = None) -> str:
+DEBUG_LIB = os.path.join(OUT, "libcuco_gb300_debug.so")
+
+
+def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | None = None,
+          debug: bool = False) -> str:
+    """The release library; with debug=True the debug build with the kernels'
+    bounds checks (CUCO_BOUNDS_CHECK), libcuco_gb300_debug.so, beside it."""
     os.makedirs(OUT, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     cc = nvcc()
-    flags = FLAGS + (extra_flags or [])
+    flags = FLAGS + (extra_flags or []) + (["-DCUCO_BOUNDS_CHECK"] if debug else [])
+    lib_path = DEBUG_LIB if debug else LIB
+    suffix = ".debug.o" if debug else ".o"
 
     def compile_one(src: str) -> str:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT, src + ".o")
+        o = os.path.join(OUT, src + suffix)
         if not force and _newer(o, [s] + headers + [__file__]):
             return o
         cmd = [cc, *ARCH, *flags, "-c", s, "-o", o]
@@ -62,14 +70,14 @@ def build(verbose: bool = False, force: bool = False, extra_flags: list[str] | N
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    if force or not _newer(LIB, objs):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    if force or not _newer(lib_path, objs):
+        cmd = [cc, *ARCH, "-shared", "-o", lib_path, *objs, "-lcudart"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
-    return LIB
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -34,6 +34,39 @@ const char *last_error();
         if (_s != CUCO_OK) return _s;          \
     } while (0)
 
+// ---------------------------------------------------- debug bounds checks
+
+// Debug builds (compiled with -DCUCO_BOUNDS_CHECK) check the index of the
+// main global and shared memory accesses of the kernels against its bound.  A
+// failed check adds one to this translation unit's violation counter and the
+// access goes to the last in-bounds element instead, so the kernel keeps
+// running and the host reads the count afterwards
+// (cuco_debug_bounds_violations).  Release builds compile the checks away.
+#ifdef CUCO_BOUNDS_CHECK
+static __device__ unsigned int g_bounds_violations;
+__device__ __forceinline__ uint32_t bounds_checked(uint32_t i, uint32_t limit) {
+    if (i >= limit) {
+        atomicAdd(&g_bounds_violations, 1u);
+        return limit ? limit - 1u : 0u;
+    }
+    return i;
+}
+#define CUCO_IDX(i, limit) ::cuco::bounds_checked((uint32_t)(i), (uint32_t)(limit))
+// this translation unit's count, read and reset (host)
+static inline uint32_t bounds_violations_take() {
+    unsigned int v = 0, zero = 0;
+    cudaMemcpyFromSymbol(&v, g_bounds_violations, sizeof v);
+    cudaMemcpyToSymbol(g_bounds_violations, &zero, sizeof zero);
+    return v;
+}
+#else
+#define CUCO_IDX(i, limit) (i)
+static inline uint32_t bounds_violations_take() { return 0; }
+#endif
+uint32_t bounds_violations_sort();
+uint32_t bounds_violations_pm();
+uint32_t bounds_violations_shortrange();
+
 // -------------------------------------------------------------- sorting
 
 // Scratch a sort of n keys needs: alternate key/value buffers and the per-tile
@@ -147,6 +180,9 @@ constexpr int kSRCtlWords = 4;
 // Reads and clears the short range's timeout word (ctl[2]) after the work on
 // `stream` is done: CUCO_ERR_TIMEOUT when a staging wait gave up.
 cuco_status_t shortrange_check(uint32_t *ctl, cudaStream_t stream);
+// Runs the staging wait's timeout path with a barrier that never completes
+// and a limit of `limit_cycles`: returns what shortrange_check then reports.
+cuco_status_t shortrange_timeout_probe(uint32_t *ctl, long long limit_cycles, cudaStream_t stream);
 
 // pair_counter: when non-null, the launch adds its in-range pair count to it.
 cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,

@@ -758,6 +758,31 @@ cuco_status_t cuco_box_run(cuco_box_t *b, int nsteps, const double *drift, const
     return CUCO_OK;
 }
 
+cuco_status_t cuco_debug_bounds_violations(uint64_t *count) {
+#ifdef CUCO_BOUNDS_CHECK
+    CUCO_TRY_CUDA(cudaDeviceSynchronize());
+    const uint64_t v = (uint64_t)bounds_violations_sort() + bounds_violations_pm() + bounds_violations_shortrange();
+    if (count) *count = v;
+    return CUCO_OK;
+#else
+    (void)count;
+    set_error("cuco_debug_bounds_violations: this library is a release build (no bounds checks)");
+    return CUCO_ERR_UNSUPPORTED;
+#endif
+}
+
+cuco_status_t cuco_box_selftest_timeout(cuco_box_t *b, double seconds) {
+    if (!b || !(seconds > 0) || seconds > 1.0) {
+        set_error("cuco_box_selftest_timeout: null box or a limit outside (0, 1] s");
+        return CUCO_ERR_INVALID;
+    }
+    int dev = 0, khz = 0;
+    CUCO_TRY_CUDA(cudaGetDevice(&dev));
+    CUCO_TRY_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+    const long long cycles = (long long)(seconds * 1e3 * (khz > 0 ? khz : 2000000));
+    return shortrange_timeout_probe(b->work.ctl, cycles, b->stream);
+}
+
 cuco_status_t cuco_box_sync(cuco_box_t *b) {
     if (!b) return CUCO_ERR_INVALID;
     CUCO_TRY_CUDA(cudaStreamSynchronize(b->stream));

@@ -967,14 +967,15 @@ __device__ __forceinline__ void deposit_one(float4 p, unsigned long long *__rest
         for (int c = 0; c < 8; ++c) w[c] = sum[c];
     }
     if (lead) {
-        atomicAdd(&rho64[sx * Myz + sy * Mz + sz], w[0]);
-        atomicAdd(&rho64[sx * Myz + syy * Mz + sz], w[1]);
-        atomicAdd(&rho64[sx * Myz + sy * Mz + szz], w[2]);
-        atomicAdd(&rho64[sx * Myz + syy * Mz + szz], w[3]);
-        atomicAdd(&rho64[sxx * Myz + sy * Mz + sz], w[4]);
-        atomicAdd(&rho64[sxx * Myz + syy * Mz + sz], w[5]);
-        atomicAdd(&rho64[sxx * Myz + sy * Mz + szz], w[6]);
-        atomicAdd(&rho64[sxx * Myz + syy * Mz + szz], w[7]);
+        const uint32_t M3 = (uint32_t)(Myz * Mz);
+        atomicAdd(&rho64[CUCO_IDX(sx * Myz + sy * Mz + sz, M3)], w[0]);
+        atomicAdd(&rho64[CUCO_IDX(sx * Myz + syy * Mz + sz, M3)], w[1]);
+        atomicAdd(&rho64[CUCO_IDX(sx * Myz + sy * Mz + szz, M3)], w[2]);
+        atomicAdd(&rho64[CUCO_IDX(sx * Myz + syy * Mz + szz, M3)], w[3]);
+        atomicAdd(&rho64[CUCO_IDX(sxx * Myz + sy * Mz + sz, M3)], w[4]);
+        atomicAdd(&rho64[CUCO_IDX(sxx * Myz + syy * Mz + sz, M3)], w[5]);
+        atomicAdd(&rho64[CUCO_IDX(sxx * Myz + sy * Mz + szz, M3)], w[6]);
+        atomicAdd(&rho64[CUCO_IDX(sxx * Myz + syy * Mz + szz, M3)], w[7]);
     }
 }
 
@@ -1012,7 +1013,7 @@ __device__ __forceinline__ float4 interp_one(float4 p, const float *__restrict__
                 const int base = off[d1][2 + u] + off[d2][2 + v];
                 float f[6];
 #pragma unroll
-                for (int q = 0; q < 6; ++q) f[q] = __ldg(&phi[base + off[dim][q]]);
+                for (int q = 0; q < 6; ++q) f[q] = __ldg(&phi[CUCO_IDX(base + off[dim][q], (uint32_t)M * M * M)]);
                 // corner at s0 (f[2]) and at s0 + 1 (f[3])
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
@@ -1315,5 +1316,7 @@ cuco_status_t pm_forces(PMPlan &plan, const float4 *pos, uint32_t n, float4 *acc
     if (launches) *launches += 5 + (n ? 2 : 0);  // five transform passes, deposit and interpolation
     return CUCO_OK;
 }
+
+uint32_t bounds_violations_pm() { return bounds_violations_take(); }
 
 }  // namespace cuco

@@ -200,13 +200,27 @@ __device__ __forceinline__ bool bar_try_wait(uint64_t *bar, uint32_t parity) {
     return done != 0;
 }
 
-// Wait for the phase with parity `parity` to complete, at most kWaitCycles.
-__device__ __forceinline__ bool bar_wait_bounded(uint64_t *bar, uint32_t parity) {
+// Wait for the phase with parity `parity` to complete, at most `limit`
+// clock cycles.
+__device__ __forceinline__ bool bar_wait_bounded(uint64_t *bar, uint32_t parity, long long limit = kWaitCycles) {
     const long long t0 = clock64();
     for (;;) {
         if (bar_try_wait(bar, parity)) return true;
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     }
+}
+
+// The staging wait's timeout path on its own: one CTA arms the barrier for
+// 16 bytes of copies that are never issued, waits at most `limit` cycles (the
+// staging wait, with a shorter limit), and reports through the same timeout
+// word the short range uses.  No copy is in flight when it gives up.
+__global__ void k_staging_timeout_probe(uint32_t *__restrict__ err, long long limit) {
+    if (threadIdx.x == 0) bar_init(&g_stage_bar);
+    __syncthreads();
+    if (threadIdx.x == 0) bar_arrive_expect(&g_stage_bar, 16u);
+    __syncthreads();
+    const bool ok = bar_wait_bounded(&g_stage_bar, 0u, limit);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(err, 1u);
 }
 
 // bytes (a multiple of 16) from global src to shared dst, both 16-byte aligned
@@ -623,7 +637,7 @@ __device__ __forceinline__ bool shortrange_segment(
                 const uint32_t m0 = __reduce_or_sync(kFull, bit_at(ps - base));
                 const uint32_t k0 = base + lane;
                 const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
-                const float4 s0 = src[k0 < T ? k0 + d0 : (uint32_t)kMaxStage];
+                const float4 s0 = src[CUCO_IDX(k0 < T ? k0 + d0 : (uint32_t)kMaxStage, kMaxStage + 1)];
                 const bool xa = pair_fast(s0, ta.x, ta.y, ta.z, ax, ay, az);
                 const bool xb = pair_fast(s0, tb.x, tb.y, tb.z, bx, by, bz);
                 if (__any_sync(kFull, xa || xb)) {
@@ -752,9 +766,15 @@ __device__ __forceinline__ bool shortrange_segment(
             for (int rr = warp; rr < ncols * 2; rr += kWarps) {
                 const Run &r = runs[rr];
                 const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
-                if (r.cnt && hi > lo)
+                if (r.cnt && hi > lo) {
+#ifdef CUCO_BOUNDS_CHECK
+                    // the run lies inside the staging area (a skipped copy
+                    // also leaves the staging wait to time out)
+                    if (CUCO_IDX(hi - c0 - 1, kMaxStage) != hi - c0 - 1) continue;
+#endif
                     bulk_copy_g2s(src + (lo - c0), spos + r.gsrc + (lo - r.soff), (hi - lo) * (uint32_t)sizeof(float4),
                                   &g_stage_bar);
+                }
             }
         }
         bool ok = bar_wait_bounded(&g_stage_bar, phase);
@@ -1080,6 +1100,12 @@ void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const Colum
 
 uint32_t shortrange_heavy_cap(uint32_t n) { return 2u * (n / kTMax) + 16u; }
 
+cuco_status_t shortrange_timeout_probe(uint32_t *ctl, long long limit_cycles, cudaStream_t stream) {
+    k_staging_timeout_probe<<<1, kThreads, 0, stream>>>(ctl + 2, limit_cycles);
+    CUCO_TRY_CUDA(cudaGetLastError());
+    return shortrange_check(ctl, stream);
+}
+
 cuco_status_t shortrange_check(uint32_t *ctl, cudaStream_t stream) {
     uint32_t flag = 0;
     CUCO_TRY_CUDA(cudaMemcpyAsync(&flag, ctl + 2, sizeof flag, cudaMemcpyDeviceToHost, stream));
@@ -1226,5 +1252,7 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
 }
+
+uint32_t bounds_violations_shortrange() { return bounds_violations_take(); }
 
 }  // namespace cuco

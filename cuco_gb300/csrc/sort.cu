@@ -213,8 +213,8 @@ __global__ void __launch_bounds__(kSortThreads, 4)
         const uint32_t kk = skeys[j];
         const uint32_t d = (kk >> shift) & (RADIX - 1);
         const uint32_t o = gbase[d] + j - dstart[d];
-        kout[o] = kk;
-        if (WITH_VALS) vout[o] = svals[j];
+        kout[CUCO_IDX(o, n)] = kk;
+        if (WITH_VALS) vout[CUCO_IDX(o, n)] = svals[j];
     }
 }
 
@@ -377,8 +377,8 @@ __global__ void k_cell_subsort(const uint32_t *__restrict__ cell_off, const uint
         }
         const uint32_t at = __shfl_sync(0xffffffffu, base, s & (kZSub - 1)) + __popc(mine & lt);
         if (i < b) {
-            sorted_pos[a + at] = make_float4(p.x, p.y, p.z, (float)s);
-            perm_s[a + at] = o;
+            sorted_pos[CUCO_IDX(a + at, b)] = make_float4(p.x, p.y, p.z, (float)s);
+            perm_s[CUCO_IDX(a + at, b)] = o;
         }
         base += cnt;
     }
@@ -465,5 +465,7 @@ cuco_status_t launch_reorder_offsets(uint32_t *cell_off, float4 *sorted_pos,
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
 }
+
+uint32_t bounds_violations_sort() { return bounds_violations_take(); }
 
 }  // namespace cuco

@@ -279,6 +279,21 @@ cuco_status_t cuco_box_run(cuco_box_t *box, int nsteps, const double *drift,
                            const double *kick_pp, const double *kick_pm);
 
 cuco_status_t cuco_box_sync(cuco_box_t *box);
+/* No counterpart in the reference.  Exercises the short range's timeout
+ * path without a fault: one CTA waits, at most `seconds` (<= 1), on a staging
+ * barrier that is armed for copies never issued, gives up, and sets the
+ * box's timeout word; the call then returns CUCO_ERR_TIMEOUT as cuco_box_sync
+ * would after a real staging wait gave up, and clears the word.  The box
+ * stays usable. */
+cuco_status_t cuco_box_selftest_timeout(cuco_box_t *box, double seconds);
+/* No counterpart in the reference.  In a debug build of the library
+ * (libcuco_gb300_debug.so, compiled with CUCO_BOUNDS_CHECK) the kernels check
+ * the index of their main memory accesses (sort scatter, cell order, deposit,
+ * interpolation, short-range staging and source reads); a failed check is
+ * counted and the access clamped in bounds.  Waits for the device, returns
+ * the count since the last call in *count and resets it.  A release build
+ * returns CUCO_ERR_UNSUPPORTED. */
+cuco_status_t cuco_debug_bounds_violations(uint64_t *count);
 /* The box's CUDA stream (cudaStream_t).  Every pass is ordered on it: the
  * PM's second stream forks from it after the keys and joins it again before
  * the short range, so work enqueued on this stream before or after a pass is
