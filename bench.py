@@ -696,7 +696,9 @@ def run_gpu_arm(args, world, rank, local):
 
 def run_e2e(steps, ic, soft, device):
     """The reference's run loop (run.c:11-20) over the drop-in C ABI with a host
-    P[] array: every call copies P[] to the device and back."""
+    P[] array: every call reads P[] from the host and writes its results back
+    (in place over the host link where the device reads pageable host memory,
+    else through a device mirror), with the host time of each call."""
     from cuco_gb300 import _native, ics
     from cuco_gb300._native import All, Header, Particle
     lib = _native.load()
@@ -733,21 +735,35 @@ def run_e2e(steps, ic, soft, device):
     lib.linklist_init()
     lib.init_drift_table()
 
+    calls = {"sync_point": 0.0, "move_particles": 0.0, "compute_accelerations": 0.0,
+             "advance_and_find_timesteps": 0.0}
+
     def one_step():
         # find_next_sync_point_and_drift (run.c:28-69) with no output times; the
         # scan of P[].Ti_endstep (run.c:35-40) is the library's, which returns
-        # the minimum advance_and_find_timesteps computed on the device
+        # the minimum advance_and_find_timesteps computed on the device.  Each
+        # call returns with its work done (P[] updated), so host time per call
+        # is its cost.
+        t = [time.perf_counter()]
         min_glob = lib.cuco_dropin_min_ti_endstep()
         if min_glob >= al.PM_Ti_endstep:
             min_glob = al.PM_Ti_endstep
+        t.append(time.perf_counter())
         lib.move_particles(al.Ti_Current, min_glob)
         al.Ti_Current = min_glob
         al.Time = float(al.TimeBegin * math.exp(al.Ti_Current * al.Timebase_interval))
+        t.append(time.perf_counter())
         lib.compute_accelerations()
+        t.append(time.perf_counter())
         lib.advance_and_find_timesteps()
+        t.append(time.perf_counter())
+        for k, name in enumerate(calls):
+            calls[name] += t[k + 1] - t[k]
 
     one_step()  # opening force + half kick (untimed warm-up)
     one_step()
+    for name in calls:
+        calls[name] = 0.0
     t0 = time.perf_counter()
     for _ in range(steps):
         one_step()
@@ -762,7 +778,31 @@ def run_e2e(steps, ic, soft, device):
     return {"value": n * steps / dt, "unit": "particle-updates/s",
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": steps, "path": "drop-in run loop: move_particles + compute_accelerations + "
-                                    "advance_and_find_timesteps on host P[] (" + access + ")"}
+                                    "advance_and_find_timesteps on host P[] (" + access + ")",
+            "calls_ms_per_step": {k: round(v * 1e3 / steps, 4) for k, v in calls.items()},
+            "link": link_bandwidth(60 * n, device)}
+
+
+def link_bandwidth(nbytes, device, reps=5):
+    """GB/s of one plain cudaMemcpyAsync of `nbytes` from pinned host memory to
+    the device and back (CUDA events, best of `reps`): the host link's copy
+    rate that the drop-in's P[] traffic is measured against."""
+    import torch
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dev = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    out = {}
+    for name, (dst, src) in (("h2d_pinned_gbs", (dev, host)), ("d2h_pinned_gbs", (host, dev))):
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1) * 1e-3)
+        out[name] = round(nbytes / best / 1e9, 1)
+    out["bytes"] = nbytes
+    return out
 
 
 def main():

@@ -23,16 +23,17 @@
 //     periodic image shift applied once per run (in chunks of kMaxStage
 //     sources; every target runs against each chunk, its sums carried in
 //     shared memory);
-//   * one target per warp: lane k culls column k by the target's xy distance
-//     and narrows it to the z range sqrt(rcut^2 - d_xy^2) reaches, trimmed in
-//     the two end cells to the z slices it reaches (the cells' particles are
-//     ordered by slice, with per-cell slice counts); the column ranges,
-//     concatenated by a warp scan, are walked 64 candidates at a time, every
-//     lane on consecutive staged sources;
+//   * two consecutive targets per warp: lane k culls column k against the
+//     pair's bounding box in xy and narrows it to the z range
+//     sqrt(rcut^2 - d_xy^2) reaches, trimmed in the two end cells to the z
+//     slices it reaches (the cells' particles are ordered by slice, with
+//     per-cell slice counts); the column ranges, concatenated by a warp scan,
+//     are walked 32 candidates at a time, every lane on one staged source
+//     that it evaluates against both targets in packed FP32 (float2
+//     add/mul/fma, one instruction for the two targets);
 //   * the pair law runs without branches on the common path and flags the
 //     rest (bin-edge and cut-edge pairs decided in double, the spline), which
-//     runs under one warp-uniform branch; two candidates per lane per window
-//     into two accumulator sets;
+//     runs under one warp-uniform branch;
 //   * the warp adds its lanes' partial sums with xor shuffles (the precision
 //     form compensated by error-free splitting);
 //   * the warp's lanes scatter the forces to original particle order and, in
@@ -476,7 +477,7 @@ __device__ __forceinline__ bool shortrange_segment(
 
     // Kernel parameters used per candidate, held in registers.
 
-    // The pair law, in two parts.  pair_fast takes the common case - inside
+    // The pair law, in two parts.  pair_fast2 takes the common case - inside
     // the cut, away from a table-bin edge and from the cut, outside the
     // softening length - without a branch, and reports the rest (its
     // contribution there is zero): a candidate whose bin or cut decision is
@@ -491,24 +492,46 @@ __device__ __forceinline__ bool shortrange_segment(
     // table is padded to kTabPad entries with its last value, so a bin index
     // masked to the padding is the clamped one (fast pairs have bins below
     // kNTab; others read a padding value they do not use).
-    auto pair_fast = [&](float4 s, float tx, float ty, float tz, float &ax, float &ay, float &az) -> bool {
-        const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
-        const float r2 = dist2(dx, dy, dz);
+    // The two targets of a warp's pair are evaluated together in packed FP32
+    // (each float2 holds target A in .x and B in .y; Blackwell's paired
+    // add/mul/fma issue one instruction for both), with the targets' negated
+    // coordinates held in registers, so d = s + (-t) = s - t exactly.  Every
+    // element is rounded as the scalar law rounds it: the result is the
+    // scalar law's, bit for bit, for each target.
+    const float2 alo2 = make_float2(p.alo, p.alo), ahi2 = make_float2(p.ahi, p.ahi);
+    const float2 magic2 = make_float2(8388608.0f, 8388608.0f);
+    auto pair_fast2 = [&](float4 s, float2 ntx, float2 nty, float2 ntz, float2 &ax, float2 &ay, float2 &az,
+                          bool &slow_a, bool &slow_b) {
+        const float2 dx = __fadd2_rn(make_float2(s.x, s.x), ntx);
+        const float2 dy = __fadd2_rn(make_float2(s.y, s.y), nty);
+        const float2 dz = __fadd2_rn(make_float2(s.z, s.z), ntz);
+        // dist2's order: dz^2 + (dy^2 + dx^2)
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
         // r2 = 0 gives rinv = inf and r = NaN: not fast (r2 < hmin2), not flagged
-        const float rinv = rsqrt_ftz(r2);
-        const float r = r2 * rinv;
-        const float xl = __fmaf_rz(r, p.alo, 8388608.0f);
-        const bool edge = !FIXED && xl != __fmaf_rz(r, p.ahi, 8388608.0f);
-        const uint32_t ti = (uint32_t)(__float_as_int(xl) - 0x4B000000);
-        const bool fast = r2 <= p.rc2_lo && r2 >= p.hmin2 && !edge;
-        const float fac = fast ? rinv * rinv * rinv * tab[ti & (kTabPad - 1)] : 0.f;
-        ax = __fmaf_rn(dx, fac, ax);
-        ay = __fmaf_rn(dy, fac, ay);
-        az = __fmaf_rn(dz, fac, az);
-        if (COUNT) npairs += fast;
+        const float2 rinv = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+        const float2 r = __fmul2_rn(r2, rinv);
+        const float2 xl = __ffma2_rz(r, alo2, magic2);
+        bool edge_a = false, edge_b = false;
+        if (!FIXED) {
+            const float2 xh = __ffma2_rz(r, ahi2, magic2);
+            edge_a = xl.x != xh.x;
+            edge_b = xl.y != xh.y;
+        }
+        // the bin is the mantissa's low bits (2^23's own are zero)
+        const float2 t = make_float2(tab[__float_as_uint(xl.x) & (kTabPad - 1)],
+                                     tab[__float_as_uint(xl.y) & (kTabPad - 1)]);
+        const bool fast_a = r2.x <= p.rc2_lo && r2.x >= p.hmin2 && !edge_a;
+        const bool fast_b = r2.y <= p.rc2_lo && r2.y >= p.hmin2 && !edge_b;
+        const float2 f = __fmul2_rn(__fmul2_rn(__fmul2_rn(rinv, rinv), rinv), t);
+        const float2 fac = make_float2(fast_a ? f.x : 0.f, fast_b ? f.y : 0.f);
+        ax = __ffma2_rn(dx, fac, ax);
+        ay = __ffma2_rn(dy, fac, ay);
+        az = __ffma2_rn(dz, fac, az);
+        if (COUNT) npairs += fast_a + fast_b;
         // r2 == 0 (the self pair, or a coincident source) adds dx*fac = 0:
         // not flagged, so the rare-case branch is not taken once per target
-        return r2 <= p.rc2_hi && r2 != 0.f && !fast;
+        slow_a = r2.x <= p.rc2_hi && r2.x != 0.f && !fast_a;
+        slow_b = r2.y <= p.rc2_hi && r2.y != 0.f && !fast_b;
     };
     auto pair_slow = [&](float4 s, float tx, float ty, float tz, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
@@ -563,7 +586,10 @@ __device__ __forceinline__ bool shortrange_segment(
     auto pair_chunk = [&](float4 lo, float4 hi, float4 ta, float4 tb, uint32_t c0, uint32_t c1, float &ax,
                           float &ay, float &az, float &eax, float &eay, float &eaz, float &bx, float &by, float &bz,
                           float &ebx, float &eby, float &ebz) {
-        ax = ay = az = bx = by = bz = 0.f;
+        // the pair's sums (A in .x, B in .y) and negated coordinates
+        float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
+        const float2 ntx = make_float2(-ta.x, -tb.x), nty = make_float2(-ta.y, -tb.y),
+                     ntz = make_float2(-ta.z, -tb.z);
         for (int cb = 0; cb < ncols; cb += 32) {
             const int col = cb + lane;
             uint32_t b = 0, e = 0;
@@ -638,11 +664,11 @@ __device__ __forceinline__ bool shortrange_segment(
                 const uint32_t k0 = base + lane;
                 const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
                 const float4 s0 = src[CUCO_IDX(k0 < T ? k0 + d0 : (uint32_t)kMaxStage, kMaxStage + 1)];
-                const bool xa = pair_fast(s0, ta.x, ta.y, ta.z, ax, ay, az);
-                const bool xb = pair_fast(s0, tb.x, tb.y, tb.z, bx, by, bz);
+                bool xa, xb;
+                pair_fast2(s0, ntx, nty, ntz, sx, sy, sz, xa, xb);
                 if (__any_sync(kFull, xa || xb)) {
-                    if (xa) pair_slow(s0, ta.x, ta.y, ta.z, ax, ay, az);
-                    if (xb) pair_slow(s0, tb.x, tb.y, tb.z, bx, by, bz);
+                    if (xa) pair_slow(s0, ta.x, ta.y, ta.z, sx.x, sy.x, sz.x);
+                    if (xb) pair_slow(s0, tb.x, tb.y, tb.z, sx.y, sy.y, sz.y);
                 }
                 before += __popc(m0);
             }
@@ -690,6 +716,12 @@ __device__ __forceinline__ bool shortrange_segment(
                 two_sum(z, ez, z, ez);
             }
         };
+        ax = sx.x;
+        ay = sy.x;
+        az = sz.x;
+        bx = sx.y;
+        by = sy.y;
+        bz = sz.y;
         reduce(ax, ay, az, eax, eay, eaz);
         reduce(bx, by, bz, ebx, eby, ebz);
     };
