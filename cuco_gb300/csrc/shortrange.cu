@@ -500,8 +500,10 @@ __device__ __forceinline__ bool shortrange_segment(
     // scalar law's, bit for bit, for each target.
     const float2 alo2 = make_float2(p.alo, p.alo), ahi2 = make_float2(p.ahi, p.ahi);
     const float2 magic2 = make_float2(8388608.0f, 8388608.0f);
+    // acc = false: the flags alone (the revisit of a window with rare-case
+    // pairs), nothing added or counted.
     auto pair_fast2 = [&](float4 s, float2 ntx, float2 nty, float2 ntz, float2 &ax, float2 &ay, float2 &az,
-                          bool &slow_a, bool &slow_b) {
+                          bool &slow_a, bool &slow_b, bool acc) {
         const float2 dx = __fadd2_rn(make_float2(s.x, s.x), ntx);
         const float2 dy = __fadd2_rn(make_float2(s.y, s.y), nty);
         const float2 dz = __fadd2_rn(make_float2(s.z, s.z), ntz);
@@ -524,10 +526,12 @@ __device__ __forceinline__ bool shortrange_segment(
         const bool fast_b = r2.y <= p.rc2_lo && r2.y >= p.hmin2 && !edge_b;
         const float2 f = __fmul2_rn(__fmul2_rn(__fmul2_rn(rinv, rinv), rinv), t);
         const float2 fac = make_float2(fast_a ? f.x : 0.f, fast_b ? f.y : 0.f);
-        ax = __ffma2_rn(dx, fac, ax);
-        ay = __ffma2_rn(dy, fac, ay);
-        az = __ffma2_rn(dz, fac, az);
-        if (COUNT) npairs += fast_a + fast_b;
+        if (acc) {
+            ax = __ffma2_rn(dx, fac, ax);
+            ay = __ffma2_rn(dy, fac, ay);
+            az = __ffma2_rn(dz, fac, az);
+            if (COUNT) npairs += fast_a + fast_b;
+        }
         // r2 == 0 (the self pair, or a coincident source) adds dx*fac = 0:
         // not flagged, so the rare-case branch is not taken once per target
         slow_a = r2.x <= p.rc2_hi && r2.x != 0.f && !fast_a;
@@ -656,21 +660,39 @@ __device__ __forceinline__ bool shortrange_segment(
             // Each window of 32 candidates: one bit per column start, so a
             // lane's column is (columns started before the window) +
             // (starts at or below its position) - 1.  Positions at or past
-            // T read the sentinel.  The rare-case law runs under a
-            // warp-uniform branch.
-            uint32_t before = 0;
-            for (uint32_t base = 0; base < T; base += 32) {
-                const uint32_t m0 = __reduce_or_sync(kFull, bit_at(ps - base));
+            // T read the sentinel.
+            auto window_source = [&](uint32_t base, uint32_t before, uint32_t &m0) {
+                m0 = __reduce_or_sync(kFull, bit_at(ps - base));
                 const uint32_t k0 = base + lane;
                 const uint32_t d0 = wdelta[before + __popc(m0 & le_mask) - 1];
-                const float4 s0 = src[CUCO_IDX(k0 < T ? k0 + d0 : (uint32_t)kMaxStage, kMaxStage + 1)];
+                return src[CUCO_IDX(k0 < T ? k0 + d0 : (uint32_t)kMaxStage, kMaxStage + 1)];
+            };
+            // The windows with a rare-case pair are only marked here (at most
+            // 64: T <= kMaxStage) and revisited after the last one, so the
+            // loop carries none of the rare-case law's code.
+            uint64_t wslow = 0;
+            uint32_t before = 0, wi = 0;
+            for (uint32_t base = 0; base < T; base += 32, ++wi) {
+                uint32_t m0;
+                const float4 s0 = window_source(base, before, m0);
                 bool xa, xb;
-                pair_fast2(s0, ntx, nty, ntz, sx, sy, sz, xa, xb);
-                if (__any_sync(kFull, xa || xb)) {
-                    if (xa) pair_slow(s0, ta.x, ta.y, ta.z, sx.x, sy.x, sz.x);
-                    if (xb) pair_slow(s0, tb.x, tb.y, tb.z, sx.y, sy.y, sz.y);
-                }
+                pair_fast2(s0, ntx, nty, ntz, sx, sy, sz, xa, xb, true);
+                if (__any_sync(kFull, xa || xb)) wslow |= 1ull << wi;
                 before += __popc(m0);
+            }
+            // the rare-case pairs, window by window: the lane's candidate
+            // again, its flags, and the full law for the flagged targets
+            while (wslow) {
+                const uint32_t w = (uint32_t)__ffsll((long long)wslow) - 1u;
+                wslow &= wslow - 1;
+                const uint32_t base = 32u * w;
+                uint32_t m0;
+                const float4 s0 = window_source(base, __popc(__ballot_sync(kFull, ps < base)), m0);
+                bool xa, xb;
+                float2 unused = make_float2(0.f, 0.f);
+                pair_fast2(s0, ntx, nty, ntz, unused, unused, unused, xa, xb, false);
+                if (xa) pair_slow(s0, ta.x, ta.y, ta.z, sx.x, sy.x, sz.x);
+                if (xb) pair_slow(s0, tb.x, tb.y, tb.z, sx.y, sy.y, sz.y);
             }
             __syncwarp();
         }
