@@ -448,6 +448,9 @@ __device__ __forceinline__ bool shortrange_segment(
         total = s_total;
     }
     const bool single_chunk = total <= (uint32_t)kMaxStage;
+    // every column and z-cell of the stencil inside the box: no run carries a
+    // periodic image shift
+    const bool no_wrap = ix >= R && ix + R < G && iy >= R && iy + R < G && iz0 >= R && iz0 + S + R <= G;
 
     const uint32_t nt = t_end - t_begin;
     const float w = p.cellw;
@@ -738,15 +741,40 @@ __device__ __forceinline__ bool shortrange_segment(
                 two_sum(z, ez, z, ez);
             }
         };
-        ax = sx.x;
-        ay = sy.x;
-        az = sz.x;
-        bx = sx.y;
-        by = sy.y;
-        bz = sz.y;
-        reduce(ax, ay, az, eax, eay, eaz);
-        reduce(bx, by, bz, ebx, eby, ebz);
+        if (FIXED) {
+            ax = sx.x;
+            ay = sy.x;
+            az = sz.x;
+            bx = sx.y;
+            by = sy.y;
+            bz = sz.y;
+            reduce(ax, ay, az, eax, eay, eaz);
+            reduce(bx, by, bz, ebx, eby, ebz);
+        } else {
+            // The six sums (A.x A.y A.z B.x B.y B.z) over the warp in five
+            // exchanges, each halving the values a lane holds: afterwards
+            // lane 16 t + 4 c + j (j < 4) holds component c of target t in
+            // ax (c = 3: nothing).
+            const bool h16 = lane & 16;
+            float k0 = h16 ? sx.y : sx.x, k1 = h16 ? sy.y : sy.x, k2 = h16 ? sz.y : sz.x;
+            k0 = __fadd_rn(k0, __shfl_xor_sync(kFull, h16 ? sx.x : sx.y, 16));
+            k1 = __fadd_rn(k1, __shfl_xor_sync(kFull, h16 ? sy.x : sy.y, 16));
+            k2 = __fadd_rn(k2, __shfl_xor_sync(kFull, h16 ? sz.x : sz.y, 16));
+            const bool h8 = lane & 8;
+            float m0 = h8 ? k2 : k0, m1 = h8 ? 0.f : k1;
+            m0 = __fadd_rn(m0, __shfl_xor_sync(kFull, h8 ? k0 : k2, 8));
+            m1 = __fadd_rn(m1, __shfl_xor_sync(kFull, h8 ? k1 : 0.f, 8));
+            const bool h4 = lane & 4;
+            float v = __fadd_rn(h4 ? m1 : m0, __shfl_xor_sync(kFull, h4 ? m0 : m1, 4));
+            v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 2));
+            v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 1));
+            ax = v;
+        }
     };
+    // plain form: the lane that writes a reduced sum, its target (0: A, 1:
+    // B) and component
+    const int red_c = (lane >> 2) & 3, red_t = lane >> 4;
+    const bool red_w = (lane & 3) == 0 && red_c < 3;
 
     // a target's coordinates: absolute float (for the culling; fixed point
     // rounded to float, which the culling margin covers) and origin-relative
@@ -815,20 +843,18 @@ __device__ __forceinline__ bool shortrange_segment(
     auto stage = [&](uint32_t c0, uint32_t c1) -> bool {
         if (tid == 0) bar_arrive_expect(&g_stage_bar, (c1 - c0) * (uint32_t)sizeof(float4));
         __syncthreads();
-        if (lane == 0) {
-            fence_async_smem();
-            for (int rr = warp; rr < ncols * 2; rr += kWarps) {
-                const Run &r = runs[rr];
-                const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
-                if (r.cnt && hi > lo) {
+        for (int rr = tid; rr < ncols * 2; rr += kThreads) {
+            const Run &r = runs[rr];
+            const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
+            if (r.cnt && hi > lo) {
 #ifdef CUCO_BOUNDS_CHECK
-                    // the run lies inside the staging area (a skipped copy
-                    // also leaves the staging wait to time out)
-                    if (CUCO_IDX(hi - c0 - 1, kMaxStage) != hi - c0 - 1) continue;
+                // the run lies inside the staging area (a skipped copy also
+                // leaves the staging wait to time out)
+                if (CUCO_IDX(hi - c0 - 1, kMaxStage) != hi - c0 - 1) continue;
 #endif
-                    bulk_copy_g2s(src + (lo - c0), spos + r.gsrc + (lo - r.soff), (hi - lo) * (uint32_t)sizeof(float4),
-                                  &g_stage_bar);
-                }
+                fence_async_smem();
+                bulk_copy_g2s(src + (lo - c0), spos + r.gsrc + (lo - r.soff), (hi - lo) * (uint32_t)sizeof(float4),
+                              &g_stage_bar);
             }
         }
         bool ok = bar_wait_bounded(&g_stage_bar, phase);
@@ -838,14 +864,23 @@ __device__ __forceinline__ bool shortrange_segment(
             if (tid == 0) atomicOr(err, 1u);
             return false;
         }
-        for (int rr = warp; rr < ncols * 2; rr += kWarps) {
-            const Run r = runs[rr];
-            if (r.cnt == 0) continue;
-            const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
-            const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
-            for (uint32_t s0 = lo + lane; s0 < hi; s0 += 32) {
-                const float4 a = src[s0 - c0];
-                src[s0 - c0] = FIXED ? rel(a) : make_float4(a.x - cx, a.y - cy, a.z - cz, 0.f);
+        if (FIXED || no_wrap) {
+            // one shift for every staged source (fixed point: the int32
+            // offset is the periodic image whatever the run)
+            for (uint32_t i = tid; i < c1 - c0; i += kThreads) {
+                const float4 a = src[i];
+                src[i] = FIXED ? rel(a) : make_float4(a.x - ox, a.y - oy, a.z - oz, 0.f);
+            }
+        } else {
+            for (int rr = warp; rr < ncols * 2; rr += kWarps) {
+                const Run r = runs[rr];
+                if (r.cnt == 0) continue;
+                const float cx = ox - r.sx, cy = oy - r.sy, cz = oz - r.sz;
+                const uint32_t lo = max(r.soff, c0), hi = min(r.soff + r.cnt, c1);
+                for (uint32_t s0 = lo + lane; s0 < hi; s0 += 32) {
+                    const float4 a = src[s0 - c0];
+                    src[s0 - c0] = make_float4(a.x - cx, a.y - cy, a.z - cz, 0.f);
+                }
             }
         }
         return true;
@@ -873,7 +908,9 @@ __device__ __forceinline__ bool shortrange_segment(
                 by = __fadd_rn(by, eby);
                 bz = __fadd_rn(bz, ebz);
             }
-            if (lane == 0) {
+            if (!FIXED) {
+                if (red_w && (red_t == 0 || has_b)) s_acc[red_c][2 * q + red_t] = ax * mg;
+            } else if (lane == 0) {
                 s_acc[0][2 * q] = ax * mg;
                 s_acc[1][2 * q] = ay * mg;
                 s_acc[2][2 * q] = az * mg;
@@ -921,7 +958,9 @@ __device__ __forceinline__ bool shortrange_segment(
                 load_pair(q, lo, hi, ta, tb, has_b);
                 float ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz;
                 pair_chunk(lo, hi, ta, tb, c0, c1, ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz);
-                if (lane == 0) {
+                if (!FIXED) {
+                    if (red_w && (red_t == 0 || has_b)) s_acc[red_c][2 * q + red_t] += ax;
+                } else if (lane == 0) {
                     carry(2 * q, ax, ay, az, eax, eay, eaz);
                     if (has_b) carry(2 * q + 1, bx, by, bz, ebx, eby, ebz);
                 }
