@@ -699,80 +699,58 @@ __device__ __forceinline__ bool shortrange_segment(
             }
             __syncwarp();
         }
-        // the warp's sums, one target at a time
-        auto reduce = [&](float &x, float &y, float &z, float &ex, float &ey, float &ez) {
-            ex = ey = ez = 0.f;
-            if (FIXED) {
-                // Compensated by error-free splitting: with V a power of two
-                // above every lane's partial sum, each is split against the
-                // quantum q = V / 2^18 into a multiple of q (h = (v + C) - C,
-                // C = 1.5 * 2^23 q) and an exact remainder l = v - h
-                // (|l| <= q/2).  The 32 multiples of q add exactly in any
-                // order (|sum| <= 32 V = 2^23 q); the remainders add in float,
-                // their error far below q.  The result is the pair (sum of the
-                // h, sum of the l).
-                const float m = fmaxf(fmaxf(fabsf(x), fabsf(y)), fabsf(z));
+        // The six sums (A.x A.y A.z B.x B.y B.z) over the warp in five
+        // exchanges, each halving the values a lane holds: afterwards lane
+        // 16 t + 4 c + j (j < 4) holds component c of target t in ax (c = 3:
+        // nothing).  FIXED: compensated by error-free splitting.  With V a
+        // power of two above every lane's partial sum of a target, each
+        // partial is split against the quantum q = V / 2^18 into a multiple
+        // of q (h = (v + C) - C, C = 1.5 * 2^23 q) and an exact remainder
+        // l = v - h (|l| <= q/2).  The 32 multiples of q add exactly in any
+        // order (any partial sum is at most 32 V = 2^23 q); the remainders
+        // add in float, their error far below q.  The lane's result is then
+        // the normalised pair (ax, eax) = (sum of the h, sum of the l).
+        float h[6] = {sx.x, sy.x, sz.x, sx.y, sy.y, sz.y}, l[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (FIXED) {
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const float m = fmaxf(fmaxf(fabsf(h[3 * t]), fabsf(h[3 * t + 1])), fabsf(h[3 * t + 2]));
                 const uint32_t eb = __reduce_max_sync(kFull, __float_as_uint(m) >> 23);  // V = 2^(eb - 126)
                 const float C = __uint_as_float(((eb + 6u) << 23) | 0x400000u);       // 1.5 * 2^5 V
-                auto split = [&](float &v, float &l) {
-                    const float h = __fsub_rn(__fadd_rn(v, C), C);
-                    l = __fsub_rn(v, h);
-                    v = h;
-                };
-                split(x, ex);
-                split(y, ey);
-                split(z, ez);
-            }
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                x = __fadd_rn(x, __shfl_xor_sync(kFull, x, off));
-                y = __fadd_rn(y, __shfl_xor_sync(kFull, y, off));
-                z = __fadd_rn(z, __shfl_xor_sync(kFull, z, off));
-                if (FIXED) {
-                    ex = __fadd_rn(ex, __shfl_xor_sync(kFull, ex, off));
-                    ey = __fadd_rn(ey, __shfl_xor_sync(kFull, ey, off));
-                    ez = __fadd_rn(ez, __shfl_xor_sync(kFull, ez, off));
+                for (int c = 0; c < 3; ++c) {
+                    const float v = h[3 * t + c], hv = __fsub_rn(__fadd_rn(v, C), C);
+                    l[3 * t + c] = __fsub_rn(v, hv);
+                    h[3 * t + c] = hv;
                 }
             }
-            if (FIXED) {
-                // (sum, error) as a normalised pair for the callers
-                two_sum(x, ex, x, ex);
-                two_sum(y, ey, y, ey);
-                two_sum(z, ez, z, ez);
-            }
-        };
-        if (FIXED) {
-            ax = sx.x;
-            ay = sy.x;
-            az = sz.x;
-            bx = sx.y;
-            by = sy.y;
-            bz = sz.y;
-            reduce(ax, ay, az, eax, eay, eaz);
-            reduce(bx, by, bz, ebx, eby, ebz);
-        } else {
-            // The six sums (A.x A.y A.z B.x B.y B.z) over the warp in five
-            // exchanges, each halving the values a lane holds: afterwards
-            // lane 16 t + 4 c + j (j < 4) holds component c of target t in
-            // ax (c = 3: nothing).
-            const bool h16 = lane & 16;
-            float k0 = h16 ? sx.y : sx.x, k1 = h16 ? sy.y : sy.x, k2 = h16 ? sz.y : sz.x;
-            k0 = __fadd_rn(k0, __shfl_xor_sync(kFull, h16 ? sx.x : sx.y, 16));
-            k1 = __fadd_rn(k1, __shfl_xor_sync(kFull, h16 ? sy.x : sy.y, 16));
-            k2 = __fadd_rn(k2, __shfl_xor_sync(kFull, h16 ? sz.x : sz.y, 16));
-            const bool h8 = lane & 8;
-            float m0 = h8 ? k2 : k0, m1 = h8 ? 0.f : k1;
-            m0 = __fadd_rn(m0, __shfl_xor_sync(kFull, h8 ? k0 : k2, 8));
-            m1 = __fadd_rn(m1, __shfl_xor_sync(kFull, h8 ? k1 : 0.f, 8));
-            const bool h4 = lane & 4;
-            float v = __fadd_rn(h4 ? m1 : m0, __shfl_xor_sync(kFull, h4 ? m0 : m1, 4));
-            v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 2));
-            v = __fadd_rn(v, __shfl_xor_sync(kFull, v, 1));
-            ax = v;
         }
+        auto xchg = [&](float keep, float send, int off) {
+            return __fadd_rn(keep, __shfl_xor_sync(kFull, send, off));
+        };
+        const bool h16 = lane & 16, h8 = lane & 8, h4 = lane & 4;
+        float k[2][3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            k[0][c] = xchg(h16 ? h[3 + c] : h[c], h16 ? h[c] : h[3 + c], 16);
+            if (FIXED) k[1][c] = xchg(h16 ? l[3 + c] : l[c], h16 ? l[c] : l[3 + c], 16);
+        }
+        float v[2];
+#pragma unroll
+        for (int j = 0; j < (FIXED ? 2 : 1); ++j) {
+            const float m0 = xchg(h8 ? k[j][2] : k[j][0], h8 ? k[j][0] : k[j][2], 8);
+            const float m1 = xchg(h8 ? 0.f : k[j][1], h8 ? k[j][1] : 0.f, 8);
+            float u = xchg(h4 ? m1 : m0, h4 ? m0 : m1, 4);
+            u = xchg(u, u, 2);
+            v[j] = xchg(u, u, 1);
+        }
+        ax = v[0];
+        eax = 0.f;
+        if (FIXED) two_sum(v[0], v[1], ax, eax);
+        (void)ay, (void)az, (void)bx, (void)by, (void)bz, (void)eay, (void)eaz, (void)ebx, (void)eby, (void)ebz;
     };
-    // plain form: the lane that writes a reduced sum, its target (0: A, 1:
-    // B) and component
+    // the lane that writes a reduced sum, its target (0: A, 1: B) and
+    // component
     const int red_c = (lane >> 2) & 3, red_t = lane >> 4;
     const bool red_w = (lane & 3) == 0 && red_c < 3;
 
@@ -900,26 +878,8 @@ __device__ __forceinline__ bool shortrange_segment(
             load_pair(q, lo, hi, ta, tb, has_b);
             float ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz;
             pair_chunk(lo, hi, ta, tb, 0, total, ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz);
-            if (FIXED) {
-                ax = __fadd_rn(ax, eax);
-                ay = __fadd_rn(ay, eay);
-                az = __fadd_rn(az, eaz);
-                bx = __fadd_rn(bx, ebx);
-                by = __fadd_rn(by, eby);
-                bz = __fadd_rn(bz, ebz);
-            }
-            if (!FIXED) {
-                if (red_w && (red_t == 0 || has_b)) s_acc[red_c][2 * q + red_t] = ax * mg;
-            } else if (lane == 0) {
-                s_acc[0][2 * q] = ax * mg;
-                s_acc[1][2 * q] = ay * mg;
-                s_acc[2][2 * q] = az * mg;
-                if (has_b) {
-                    s_acc[0][2 * q + 1] = bx * mg;
-                    s_acc[1][2 * q + 1] = by * mg;
-                    s_acc[2][2 * q + 1] = bz * mg;
-                }
-            }
+            if (FIXED) ax = __fadd_rn(ax, eax);
+            if (red_w && (red_t == 0 || has_b)) s_acc[red_c][2 * q + red_t] = ax * mg;
         }
         // the warp's epilogues side by side: lane 2r + j takes target j of
         // its round r pair
@@ -929,20 +889,15 @@ __device__ __forceinline__ bool shortrange_segment(
     } else {
         for (uint32_t t = tid; t < nt; t += kThreads)
             for (int k = 0; k < 6; ++k) s_acc[k][t] = 0.f;
-        // target t's running sums (only the warp of t's pair touches them)
-        auto carry = [&](uint32_t t, float x, float y, float z, float ex, float ey, float ez) {
+        // component c of target t's running sum (only the warp of t's pair
+        // touches it)
+        auto carry = [&](uint32_t t, int c, float x, float ex) {
             if (FIXED) {
                 float e;
-                two_sum(s_acc[0][t], x, s_acc[0][t], e);
-                s_acc[3][t] = __fadd_rn(s_acc[3][t], __fadd_rn(ex, e));
-                two_sum(s_acc[1][t], y, s_acc[1][t], e);
-                s_acc[4][t] = __fadd_rn(s_acc[4][t], __fadd_rn(ey, e));
-                two_sum(s_acc[2][t], z, s_acc[2][t], e);
-                s_acc[5][t] = __fadd_rn(s_acc[5][t], __fadd_rn(ez, e));
+                two_sum(s_acc[c][t], x, s_acc[c][t], e);
+                s_acc[3 + c][t] = __fadd_rn(s_acc[3 + c][t], __fadd_rn(ex, e));
             } else {
-                s_acc[0][t] += x;
-                s_acc[1][t] += y;
-                s_acc[2][t] += z;
+                s_acc[c][t] += x;
             }
         };
         for (uint32_t c0 = 0; c0 < total; c0 += kMaxStage) {
@@ -958,12 +913,7 @@ __device__ __forceinline__ bool shortrange_segment(
                 load_pair(q, lo, hi, ta, tb, has_b);
                 float ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz;
                 pair_chunk(lo, hi, ta, tb, c0, c1, ax, ay, az, eax, eay, eaz, bx, by, bz, ebx, eby, ebz);
-                if (!FIXED) {
-                    if (red_w && (red_t == 0 || has_b)) s_acc[red_c][2 * q + red_t] += ax;
-                } else if (lane == 0) {
-                    carry(2 * q, ax, ay, az, eax, eay, eaz);
-                    if (has_b) carry(2 * q + 1, bx, by, bz, ebx, eby, ebz);
-                }
+                if (red_w && (red_t == 0 || has_b)) carry(2 * q + red_t, red_c, ax, eax);
             }
         }
         __syncthreads();
