@@ -326,8 +326,10 @@ def run_serving(args, world, rank, local):
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_shortrange launch at
 # z = 49 (ncu --set full, the first timed step of
-# `bench.py --steps 2 --warmup 3 --e2e-steps 0 --no-cpu`; 116.9 + 31.8 MB)
-SR_TRAFFIC = {"plain-128^3-L256-M256-G64-z49to0-200steps": 148.7e6}
+# `bench.py --steps 2 --warmup 3 --e2e-steps 0 --no-cpu`; 116.9 + 30.5 MB), and
+# of the precision form's launch (same command with --workload precision-128)
+SR_TRAFFIC = {"plain-128^3-L256-M256-G64-z49to0-200steps": 147.4e6,
+              "precision-128^3-L256-M256-G64-z49to0-200steps": 150.2e6}
 
 
 # softening (fraction of the mean spacing) of the small box: 0.03, the others 0.025
