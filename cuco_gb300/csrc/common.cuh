@@ -185,11 +185,17 @@ cuco_status_t shortrange_check(uint32_t *ctl, cudaStream_t stream);
 cuco_status_t shortrange_timeout_probe(uint32_t *ctl, long long limit_cycles, cudaStream_t stream);
 
 // pair_counter: when non-null, the launch adds its in-range pair count to it.
+// late_stream (with plan_done, an event of the caller's): the persistent grid
+// is split, one CTA per SM fewer on `stream` and the rest queued on
+// late_stream behind whatever that stream runs first (the PM); both parts
+// take units from the same counter, so work left when the late part starts
+// spreads over both.  The launch is complete when both streams have run it.
 cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_pos,
                                 const uint32_t *perm, const uint32_t *cell_a,
                                 const uint32_t *cell_b, CellFormat fmt, const float *table,
                                 float4 *acc_out, const KickArgs &kick, const SRWork &work, cudaStream_t stream,
-                                unsigned long long *pair_counter = nullptr);
+                                unsigned long long *pair_counter = nullptr, cudaStream_t late_stream = nullptr,
+                                cudaEvent_t plan_done = nullptr);
 
 // Many boxes in one launch (the batched form).  A box's descriptor holds its
 // parameters and neighbour-column set; shortrange_desc_fill writes one (in

@@ -116,6 +116,21 @@ __global__ void k_scatter4(const float4 *__restrict__ src_sorted, const uint32_t
     if (i < n) dst[perm[i]] = src_sorted[i];
 }
 
+// The PM half of the kick, after the short range's epilogue applied the PP
+// half: vel += GravPM * dt (timestep.c:58,88), rounded as the epilogue rounds
+// it when it applies both.
+__global__ void k_kick_pm(float4 *__restrict__ vel, const float4 *__restrict__ acc_pm, uint32_t n, float km) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float4 v = vel[i];
+        const float4 g = acc_pm[i];
+        v.x = __fmaf_rn(g.x, km, v.x);
+        v.y = __fmaf_rn(g.y, km, v.y);
+        v.z = __fmaf_rn(g.z, km, v.z);
+        vel[i] = v;
+    }
+}
+
 __global__ void k_pack3to4(const float *__restrict__ a, float4 *__restrict__ b, uint32_t n) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = make_float4(a[3 * i], a[3 * i + 1], a[3 * i + 2], 0.f);
@@ -296,7 +311,7 @@ struct cuco_box {
     // the PM runs on its own stream beside the sort and the cell order,
     // forked after the positions are final and joined before the short range
     cudaStream_t pm_stream = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, sr_plan = nullptr;
     float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr;
     float4 *spos = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr;
@@ -385,7 +400,6 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
                            b->timing ? &b->ev[b->ev_cur][4] : nullptr, b->timing ? &b->ev[b->ev_cur][5] : nullptr,
                            &b->launches));
         record(b, 6, b->pm_stream);
-        CUCO_TRY_CUDA(cudaEventRecord(b->join, b->pm_stream));
     } else {
         record(b, 4);
         record(b, 5);
@@ -409,18 +423,33 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
                                  nullptr, 1, b->cfg.mode == CUCO_MODE_FIXED, b->stream));
     b->launches += 2;
     record(b, 3);
-    if (pm) CUCO_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
     record(b, 8);
+    // The short range needs nothing from the PM: it starts when the cell
+    // order is ready, one CTA per SM short of a full persistent grid, so the
+    // PM's remaining kernels keep running beside it; its last CTAs are
+    // queued on the PM's stream behind the PM and take the units left then.
+    // The PM half of the kick follows once both are done.
+    const bool kick_on = kick && kick->vel;
     if (pp) {
         KickArgs k{};
         if (kick) k = *kick;
         k.acc_pm_s = nullptr;
         k.acc_pm_out = nullptr;
-        k.acc_pm_o = pm ? b->acc_pm : nullptr;
+        k.acc_pm_o = nullptr;
         CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, perm_s, b->cell_off,
                                    nullptr, kCellOffsets, b->table, b->acc_pp, k, b->work, b->stream,
-                                   b->count_pairs ? b->pair_counter : nullptr));
-        b->launches += 2;  // work plan + persistent short range
+                                   b->count_pairs ? b->pair_counter : nullptr, pm ? b->pm_stream : nullptr,
+                                   b->sr_plan));
+        b->launches += pm ? 3 : 2;  // work plan + persistent short range (in two parts beside the PM)
+    }
+    if (pm) {
+        CUCO_TRY_CUDA(cudaEventRecord(b->join, b->pm_stream));
+        CUCO_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
+        if (pp && kick_on && b->n) {
+            k_kick_pm<<<(b->n + 255) / 256, 256, 0, b->stream>>>(kick->vel, b->acc_pm, b->n, (float)kick->kick_pm);
+            CUCO_TRY_CUDA(cudaGetLastError());
+            b->launches += 1;
+        }
     }
     record(b, 7);
     return CUCO_OK;
@@ -516,7 +545,8 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
     }
     if (cudaStreamCreateWithPriority(&b->pm_stream, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->sr_plan, cudaEventDisableTiming) != cudaSuccess) {
         set_error("cudaStreamCreate failed");
         return fail(CUCO_ERR_CUDA);
     }
@@ -586,6 +616,7 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
             if (b->ev[k][i]) cudaEventDestroy(b->ev[k][i]);
     if (b->fork) cudaEventDestroy(b->fork);
     if (b->join) cudaEventDestroy(b->join);
+    if (b->sr_plan) cudaEventDestroy(b->sr_plan);
     if (b->pm_stream) cudaStreamDestroy(b->pm_stream);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;

@@ -1070,14 +1070,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
 }
 
 // CTAs a persistent launch of `kernel` keeps resident on this device.
+// The persistent grid of a kernel: SMs x its resident CTAs per SM.
+struct PersistentGrid {
+    unsigned sms, per;
+};
 template <typename K>
-unsigned persistent_grid(K kernel, size_t smem) {
+PersistentGrid persistent_grid(K kernel, size_t smem) {
     int dev = 0, sms = 0, per = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kThreads, smem) != cudaSuccess || per < 1)
         per = 1;
-    return (unsigned)(std::max(sms, 1) * per);
+    return {(unsigned)std::max(sms, 1), (unsigned)per};
 }
 
 // Neighbour columns (dx, dy) whose xy cell distance is within rcut (+margin).
@@ -1116,8 +1120,8 @@ bool build_columns(const ShortRangeParams &p, ColumnSet *cs) {
 }  // namespace
 
 template <CellFormat FMT, bool KICK, bool FIXED>
-void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const ColumnSet &cs, uint32_t nseg,
-                     const SRWork &work, const float4 *sorted_pos, const uint32_t *perm,
+void launch_fmt_kick(cudaStream_t stream, cudaStream_t late_stream, const ShortRangeParams &p, const ColumnSet &cs,
+                     uint32_t nseg, const SRWork &work, const float4 *sorted_pos, const uint32_t *perm,
                      const uint32_t *cell_a, const uint32_t *cell_b, const float *table,
                      float4 *acc_out, const KickArgs &kick, unsigned long long *counter) {
     const size_t sm = smem_bytes(cs.ncols, cs.S + 2 * cs.R, p.slices != nullptr);
@@ -1130,15 +1134,19 @@ void launch_fmt_kick(cudaStream_t stream, const ShortRangeParams &p, const Colum
         return true;
     }();
     (void)attr;
+    auto launch = [&](auto kernel) {
+        const PersistentGrid g = persistent_grid(kernel, sm);
+        const unsigned late = late_stream && g.per > 1 ? g.sms : 0u;
+        kernel<<<g.sms * g.per - late, kThreads, sm, stream>>>(p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b,
+                                                              table, acc_out, kick, counter);
+        if (late)
+            kernel<<<late, kThreads, sm, late_stream>>>(p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table,
+                                                        acc_out, kick, counter);
+    };
     if (counter)
-        k_shortrange<FMT, KICK, true, FIXED><<<persistent_grid(k_shortrange<FMT, KICK, true, FIXED>, sm), kThreads,
-                                               sm, stream>>>(p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b,
-                                                             table, acc_out, kick, counter);
+        launch(k_shortrange<FMT, KICK, true, FIXED>);
     else
-        k_shortrange<FMT, KICK, false, FIXED><<<persistent_grid(k_shortrange<FMT, KICK, false, FIXED>, sm),
-                                                kThreads, sm, stream>>>(p, cs, nseg, work, sorted_pos, perm,
-                                                                        cell_a, cell_b, table, acc_out, kick,
-                                                                        counter);
+        launch(k_shortrange<FMT, KICK, false, FIXED>);
 }
 
 uint32_t shortrange_heavy_cap(uint32_t n) { return 2u * (n / kTMax) + 16u; }
@@ -1183,7 +1191,7 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p_in, const float4 *sort
                                 const uint32_t *perm, const uint32_t *cell_a,
                                 const uint32_t *cell_b, CellFormat fmt, const float *table,
                                 float4 *acc_out, const KickArgs &kick, const SRWork &work, cudaStream_t stream,
-                                unsigned long long *pair_counter) {
+                                unsigned long long *pair_counter, cudaStream_t late_stream, cudaEvent_t plan_done) {
     ColumnSet cs;
     ShortRangeParams p = p_in;
     finish_pair_law(p);
@@ -1210,21 +1218,29 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p_in, const float4 *sort
         k_sr_plan<kCellOffsets><<<(nseg + 255) / 256, 256, 0, stream>>>(p, cs.S, nseg, cell_a, cell_b, work);
     else
         k_sr_plan<kCellStartEnd><<<(nseg + 255) / 256, 256, 0, stream>>>(p, cs.S, nseg, cell_a, cell_b, work);
+    if (late_stream) {
+        if (!plan_done) {
+            set_error("short range: a split launch needs the caller's plan event");
+            return CUCO_ERR_INVALID;
+        }
+        CUCO_TRY_CUDA(cudaEventRecord(plan_done, stream));
+        CUCO_TRY_CUDA(cudaStreamWaitEvent(late_stream, plan_done, 0));
+    }
     if (p.fixed) {
         if (kick_on)
-            launch_fmt_kick<kCellOffsets, true, true>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, true, true>(stream, late_stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellOffsets, false, true>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, false, true>(stream, late_stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     } else if (fmt == kCellOffsets) {
         if (kick_on)
-            launch_fmt_kick<kCellOffsets, true, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, true, false>(stream, late_stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellOffsets, false, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellOffsets, false, false>(stream, late_stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     } else {
         if (kick_on)
-            launch_fmt_kick<kCellStartEnd, true, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellStartEnd, true, false>(stream, late_stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
         else
-            launch_fmt_kick<kCellStartEnd, false, false>(stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
+            launch_fmt_kick<kCellStartEnd, false, false>(stream, late_stream, p, cs, nseg, work, sorted_pos, perm, cell_a, cell_b, table, acc_out, kick, pair_counter);
     }
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
@@ -1275,9 +1291,13 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
     const bool kick_on = kick.vel != nullptr;
     CUCO_TRY_CUDA(cudaMemsetAsync(work.ctl, 0, 2 * sizeof(uint32_t), stream));
     k_sr_plan_multi<<<(segments + 255) / 256, 256, 0, stream>>>(d, seg_base, nbox, segments, cell_off, work);
-#define CUCO_SR_MULTI(K, C, F)                                                                                   \
-    k_shortrange_multi<K, C, F><<<persistent_grid(k_shortrange_multi<K, C, F>, smem), kThreads, smem, stream>>>( \
-        d, kicks, seg_base, nbox, segments, work, sorted_pos, perm, cell_off, table, acc_out, kick, pair_counter)
+#define CUCO_SR_MULTI(K, C, F)                                                                      \
+    do {                                                                                            \
+        const PersistentGrid g = persistent_grid(k_shortrange_multi<K, C, F>, smem);                 \
+        k_shortrange_multi<K, C, F><<<g.sms * g.per, kThreads, smem, stream>>>(                      \
+            d, kicks, seg_base, nbox, segments, work, sorted_pos, perm, cell_off, table, acc_out, kick, \
+            pair_counter);                                                                          \
+    } while (0)
     if (fixed) {
         if (kick_on) {
             if (pair_counter) CUCO_SR_MULTI(true, true, true); else CUCO_SR_MULTI(true, false, true);
