@@ -576,6 +576,39 @@ def run_reference_arm(args, world, rank):
 
 # ----------------------------------------------------------------- GPU arm
 
+def measured_hbm_gbs():
+    """The HBM copy bandwidth measured on the GB300s (MEASURED_PEAKS.json
+    beside this file), else the fallback figure; and which."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def step_roofline(n, M, G, pairs_per_step, ms_per_step, fp32_tflops):
+    """Whole-step roofline: every phase at its bound (HBM for the sort, deposit,
+    transforms and interpolation; the FP32 pipe for the pair force), by the
+    fixed algorithmic conventions below, summed and divided by the measured
+    step time."""
+    hbm, kind = measured_hbm_gbs()
+    nbytes = {
+        "sort": 28 * n + 8 * G ** 3,                     # pos r + sorted pos w + permutation w; cell bounds
+        "deposit": 12 * n + 4 * M ** 3,                  # pos r; density grid w
+        "fft": 2 * 2 * 2 * 8 * M * M * (M // 2 + 1),    # fwd + inv, 2 passes each, read + write
+        "interpolation": 24 * n + 12 * M ** 3,           # pos r + accel w; three force grids r
+    }
+    ideal = {k: 1e3 * v / (hbm * 1e9) for k, v in nbytes.items()}
+    ideal["pair_force"] = 1e3 * 20.0 * pairs_per_step / (fp32_tflops * 1e12)
+    total = sum(ideal.values())
+    return {"ideal_ms_per_phase": {k: round(v, 5) for k, v in ideal.items()},
+            "algorithmic_bytes": nbytes, "ideal_ms": round(total, 5), "measured_ms": round(ms_per_step, 5),
+            "frac": total / ms_per_step, "hbm_peak_gbs": hbm, "hbm_peak_kind": kind,
+            "fp32_peak_tflops": fp32_tflops,
+            "convention": "bytes per phase as listed (the FD gradient is fused into the interpolation, "
+                          "its force grids counted there), 20 FP32 flops per in-range pair"}
+
+
 def run_gpu_arm(args, world, rank, local):
     from cuco_gb300 import Box, BoxConfig, ics, _native
     lib = _native.load()
@@ -664,6 +697,8 @@ def run_gpu_arm(args, world, rank, local):
                      "convention": "20 FP32 flops per in-range pair (pairs counted in-kernel in an untimed replay "
                                    "of the same steps), "
                                    "peak = measured FMA throughput"},
+        "step_roofline": step_roofline(ic.n, PM_GRID, CELL_GRID, pairs.value / K, 1e3 * t_total / K,
+                                       peak.value),
         "phase_ms_per_step": phases,
         "pairs_per_step": pairs.value / K,
         "late_window": late,

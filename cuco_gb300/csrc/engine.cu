@@ -298,7 +298,7 @@ void shortrange_table(float *t) {
 
 using namespace cuco;
 
-constexpr int kPhaseEvents = 9;
+constexpr int kPhaseEvents = 10;
 
 struct cuco_box {
     cuco_config_t cfg;
@@ -445,6 +445,9 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
     if (pm) {
         CUCO_TRY_CUDA(cudaEventRecord(b->join, b->pm_stream));
         CUCO_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
+    }
+    record(b, 9);  // both parts of the short range done
+    if (pm) {
         if (pp && kick_on && b->n) {
             k_kick_pm<<<(b->n + 255) / 256, 256, 0, b->stream>>>(kick->vel, b->acc_pm, b->n, (float)kick->kick_pm);
             CUCO_TRY_CUDA(cudaGetLastError());
@@ -462,9 +465,10 @@ cuco_status_t read_pending(cuco_box *b) {
     cudaEvent_t *e = b->ev[b->ev_cur ^ 1];
     CUCO_TRY_CUDA(cudaEventSynchronize(e[7]));
     // drift+keys, sort, cell order; the PM's three phases from the fork (they
-    // overlap the sort and the cell order); the short range from the join;
+    // overlap the sort, the cell order and the start of the short range); the
+    // short range from the cell order to the end of both parts of its launch;
     // the whole pass
-    static const int from[8] = {0, 1, 2, 1, 4, 5, 8, 0}, to[8] = {1, 2, 3, 4, 5, 6, 7, 7};
+    static const int from[8] = {0, 1, 2, 1, 4, 5, 8, 0}, to[8] = {1, 2, 3, 4, 5, 6, 9, 7};
     for (int i = 0; i < 8; ++i) {
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e[from[i]], e[to[i]]);

@@ -295,18 +295,20 @@ cuco_status_t cuco_box_selftest_timeout(cuco_box_t *box, double seconds);
  * returns CUCO_ERR_UNSUPPORTED. */
 cuco_status_t cuco_debug_bounds_violations(uint64_t *count);
 /* The box's CUDA stream (cudaStream_t).  Every pass is ordered on it: the
- * PM's second stream forks from it after the keys and joins it again before
- * the short range, so work enqueued on this stream before or after a pass is
- * ordered with all of the pass. */
+ * PM's second stream forks from it after the keys and joins it again after
+ * the short range (whose last CTAs it runs behind the PM), so work enqueued
+ * on this stream before or after a pass is ordered with all of the pass. */
 cuco_status_t cuco_box_stream(cuco_box_t *box, void **stream);
 
 /* Device time (ms) of each phase of the last cuco_box_forces/cuco_box_step:
  * [0] drift+keys, [1] sort, [2] reorder (cell bounds and z-slice order),
  * [3] PM deposit, [4] PM FFT+Green, [5] PM gradient+interpolation,
- * [6] short range (+kick), [7] total.  The PM runs on a second stream beside
- * the sort and the reorder (from the end of [0] to the start of [6]), so
- * [0] + max([1] + [2], [3] + [4] + [5]) + [6] is about [7].
- * Only filled when phase timing is enabled. */
+ * [6] short range (with the PP half of the kick), [7] total.  The PM runs on
+ * a second stream from the end of [0], beside the sort, the reorder and the
+ * start of the short range, whose last CTAs it runs after itself; [6] spans
+ * the short range's whole launch, from the end of [2] until both of its
+ * parts are done.  [0] + [1] + [2] + [6] + the PM half of the kick (after
+ * [6]) is [7].  Only filled when phase timing is enabled. */
 cuco_status_t cuco_box_enable_timing(cuco_box_t *box, int enable);
 cuco_status_t cuco_box_timings(cuco_box_t *box, float *ms /* 8 */);
 /* Sums of the phase times since timing was enabled (or the last reset).  A
