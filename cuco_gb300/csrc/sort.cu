@@ -284,103 +284,147 @@ __global__ void k_reorder_offsets(uint32_t *__restrict__ cell_off, float4 *__res
     if (i < n && sorted_pos) sorted_pos[i] = pos[perm[i]];
 }
 
-// One warp per cell: a stable counting sort of the cell's particles by z
-// slice.  A lane's slice is spelled out by four ballots (three slice bits and
-// "no particle"), so the lanes of each slice, their counts and each lane's
-// rank among equal slices are popcounts; lane k < kZSub keeps slice k's
-// running offset.  The order is fixed by the input order alone.
-__global__ void k_cell_subsort(const uint32_t *__restrict__ cell_off, const uint32_t *__restrict__ perm,
-                               const float4 *__restrict__ pos, float4 *__restrict__ sorted_pos,
-                               uint32_t *__restrict__ perm_s, uint4 *__restrict__ slices, uint32_t ncells,
-                               const __grid_constant__ CellBox one, const CellBox *__restrict__ boxes, int nbox,
-                               int fixed) {
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t lane = threadIdx.x & 31;
-    if (c >= ncells) return;  // warp-uniform
-    const uint32_t a = cell_off[c], b = cell_off[c + 1];
-    // lanes 0..kZSub-1 write the cell's inclusive slice counts as u16
-    uint16_t *sl = reinterpret_cast<uint16_t *>(slices + c);
+// A stable counting sort of each cell's particles by z slice.  A lane's
+// slice is spelled out by four ballots (three slice bits and "no particle"),
+// so the lanes of each slice, their counts and each lane's rank among equal
+// slices are popcounts of the ballots masked to the cell's lanes, and one
+// lane per slice keeps the slice's running offset.  The order is fixed by the
+// input order alone.  A warp takes four consecutive cells: eight lanes per
+// cell, eight particles at a time, which keeps four cells' dependent loads
+// (bounds, permutation, position) in flight where cells hold a few particles
+// (one warp per cell left most lanes idle waiting on them); where one of the
+// four holds more than 32, the warp sorts them one after the other with all
+// 32 lanes, so a dense cell does not leave three groups of lanes idle.
+constexpr uint32_t kSubLanes = 8;  // lanes per cell in the four-cell mode
+static_assert(kZSub == (int)kSubLanes, "one lane per slice within a cell's lanes");
+
+// The cell box of cell c: `one`, or the box of a many-box launch holding c.
+__device__ __forceinline__ CellBox cell_box(uint32_t c, const CellBox &one, const CellBox *__restrict__ boxes,
+                                            int nbox) {
+    if (!boxes) return one;
+    int lo = 0, hi = nbox;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&boxes[mid].cell_base) <= c)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return boxes[lo];
+}
+
+// slice of z within cell cz: plain, of the key rule's product G/L * z (in
+// [cz, cz + 1) but for the clamped top face); fixed point, the three bits
+// below the cell index of z * G / 2^32
+__device__ __forceinline__ uint32_t z_slice(float4 p, const CellBox &d, uint32_t cz, int fixed) {
+    if (fixed) return (uint32_t)(((uint64_t)__float_as_uint(p.z) * d.G) >> (32 - kZSubBits)) & (kZSub - 1);
+    const float t = __fmul_rn(p.z, d.gridfac);
+    const int s = __float2int_rd(__fmul_rn(__fsub_rn(t, (float)cz), (float)kZSub));
+    return (uint32_t)min(max(s, 0), kZSub - 1);
+}
+
+// One cell [a, b) sorted by the lanes of gmask (W = 8 or 32 consecutive
+// lanes; gl = lane within them); every lane of the warp calls it together.
+// `valid`: whether this lane's group has a cell (c < ncells).
+template <uint32_t W>
+__device__ __forceinline__ void subsort_cell(bool valid, uint32_t c, uint32_t a, uint32_t b, const CellBox &d,
+                                             uint32_t gmask, uint32_t gl, const uint32_t *__restrict__ perm,
+                                             const float4 *__restrict__ pos, float4 *__restrict__ sorted_pos,
+                                             uint32_t *__restrict__ perm_s, uint4 *__restrict__ slices,
+                                             int fixed) {
+    const uint32_t lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+    const uint32_t n_cell = b - a;
+    const uint32_t cz = valid ? (c - d.cell_base) % d.G : 0u;
+    // lanes gl < kZSub write the cell's inclusive slice counts as u16
+    uint16_t *sl = reinterpret_cast<uint16_t *>(slices + (valid ? c : 0u));
     auto put_counts = [&](uint32_t incl) {
-        if (lane < kZSub) sl[lane] = b - a >= 0xffffu ? (uint16_t)0xffffu : (uint16_t)incl;
+        if (valid && gl < kZSub) sl[gl] = n_cell >= 0xffffu ? (uint16_t)0xffffu : (uint16_t)incl;
     };
-    if (a >= b) {
-        put_counts(0);
-        return;
-    }
-    CellBox d = one;
-    if (boxes) {
-        int lo = 0, hi = nbox;
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(&boxes[mid].cell_base) <= c)
-                lo = mid;
-            else
-                hi = mid;
-        }
-        d = boxes[lo];
-    }
-    const uint32_t cz = (c - d.cell_base) % d.G;
-    const uint32_t lt = (1u << lane) - 1u;
-    // slice of z within cell cz: plain, of the key rule's product G/L * z
-    // (in [cz, cz + 1) but for the clamped top face); fixed point, the three
-    // bits below the cell index of z * G / 2^32
-    auto slice = [&](float4 p) -> uint32_t {
-        if (fixed) return (uint32_t)(((uint64_t)__float_as_uint(p.z) * d.G) >> (32 - kZSubBits)) & (kZSub - 1);
-        const float t = __fmul_rn(p.z, d.gridfac);
-        const int s = __float2int_rd(__fmul_rn(__fsub_rn(t, (float)cz), (float)kZSub));
-        return (uint32_t)min(max(s, 0), kZSub - 1);
-    };
-    // lanes holding slice k (k = kZSub: no particle)
+    // the lanes of gmask holding slice k (k = kZSub: no particle)
     auto lanes_of = [&](uint32_t k, uint32_t b0, uint32_t b1, uint32_t b2, uint32_t none) {
-        return ((k & 1) ? b0 : ~b0) & ((k & 2) ? b1 : ~b1) & ((k & 4) ? b2 : ~b2) & ~none;
+        return ((k & 1) ? b0 : ~b0) & ((k & 2) ? b1 : ~b1) & ((k & 4) ? b2 : ~b2) & ~none & gmask;
     };
-    uint32_t base = 0;  // lane k < kZSub: slice k's next offset
-    if (b - a > 32) {
-        for (uint32_t i0 = a; i0 < b; i0 += 32) {
-            const uint32_t i = i0 + lane;
-            const uint32_t s = i < b ? slice(pos[perm[i]]) : (uint32_t)kZSub;
+    // inclusive scan over the group's first kZSub lanes
+    auto scan = [&](uint32_t v) {
+#pragma unroll
+        for (uint32_t off = 1; off < (uint32_t)kZSub; off <<= 1) {
+            const uint32_t u = __shfl_up_sync(0xffffffffu, v, off, W);
+            if (gl >= off) v += u;
+        }
+        return v;
+    };
+    const uint32_t chunks = (n_cell + W - 1) / W;
+    const uint32_t chunks_max = __reduce_max_sync(0xffffffffu, chunks);
+    const bool multi = chunks > 1;
+    if (n_cell == 0) put_counts(0);
+    const uint32_t gbase = lane - gl;  // the group's first lane
+    uint32_t base = 0;                  // lane gl < kZSub: slice gl's next offset in the cell
+    if (__any_sync(0xffffffffu, multi)) {
+        // cells of more than one chunk count their slices first
+        for (uint32_t j = 0; j < chunks_max; ++j) {
+            const uint32_t i = a + j * W + gl;
+            const uint32_t s = multi && i < b ? z_slice(pos[perm[i]], d, cz, fixed) : (uint32_t)kZSub;
             const uint32_t b0 = __ballot_sync(0xffffffffu, s & 1), b1 = __ballot_sync(0xffffffffu, s & 2),
                            b2 = __ballot_sync(0xffffffffu, s & 4), none = __ballot_sync(0xffffffffu, s == kZSub);
-            if (lane < kZSub) base += __popc(lanes_of(lane, b0, b1, b2, none));
+            if (gl < kZSub) base += __popc(lanes_of(gl, b0, b1, b2, none));
         }
-        // exclusive scan of the slice counts over lanes 0..kZSub-1
-        uint32_t incl = base;
-        for (int off = 1; off < kZSub; off <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
-            if (lane >= (uint32_t)off) incl += v;
-        }
-        put_counts(incl);
+        const uint32_t incl = scan(base);
+        if (multi) put_counts(incl);
         base = incl - base;
     }
-    for (uint32_t i0 = a; i0 < b; i0 += 32) {
-        const uint32_t i = i0 + lane;
+    for (uint32_t j = 0; j < chunks_max; ++j) {
+        const uint32_t i = a + j * W + gl;
         uint32_t o = 0, s = kZSub;
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
         if (i < b) {
             o = perm[i];
             p = pos[o];
-            s = slice(p);
+            s = z_slice(p, d, cz, fixed);
         }
         const uint32_t b0 = __ballot_sync(0xffffffffu, s & 1), b1 = __ballot_sync(0xffffffffu, s & 2),
                        b2 = __ballot_sync(0xffffffffu, s & 4), none = __ballot_sync(0xffffffffu, s == kZSub);
         const uint32_t mine = lanes_of(s, b0, b1, b2, none);
-        const uint32_t cnt = lane < kZSub ? __popc(lanes_of(lane, b0, b1, b2, none)) : 0u;
-        if (b - a <= 32) {
-            // one chunk: the offsets are the exclusive scan of this chunk's counts
-            uint32_t incl = cnt;
-            for (int off = 1; off < kZSub; off <<= 1) {
-                const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
-                if (lane >= (uint32_t)off) incl += v;
-            }
-            put_counts(incl);
+        const uint32_t cnt = gl < kZSub ? __popc(lanes_of(gl, b0, b1, b2, none)) : 0u;
+        const uint32_t incl = scan(cnt);
+        if (!multi && j == 0) {
+            // one chunk: the offsets are the exclusive scan of its counts
+            if (n_cell) put_counts(incl);
             base = incl - cnt;
         }
-        const uint32_t at = __shfl_sync(0xffffffffu, base, s & (kZSub - 1)) + __popc(mine & lt);
+        const uint32_t at = __shfl_sync(0xffffffffu, base, gbase + (s & (kZSub - 1))) + __popc(mine & lt);
         if (i < b) {
             sorted_pos[CUCO_IDX(a + at, b)] = make_float4(p.x, p.y, p.z, (float)s);
             perm_s[CUCO_IDX(a + at, b)] = o;
         }
         base += cnt;
+    }
+}
+
+__global__ void k_cell_subsort(const uint32_t *__restrict__ cell_off, const uint32_t *__restrict__ perm,
+                               const float4 *__restrict__ pos, float4 *__restrict__ sorted_pos,
+                               uint32_t *__restrict__ perm_s, uint4 *__restrict__ slices, uint32_t ncells,
+                               const __grid_constant__ CellBox one, const CellBox *__restrict__ boxes, int nbox,
+                               int fixed) {
+    constexpr uint32_t kCells = 32 / kSubLanes;
+    const uint32_t lane = threadIdx.x & 31, grp = lane / kSubLanes;
+    const uint32_t c0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * kCells;
+    if (c0 >= ncells) return;  // warp-uniform
+    const uint32_t c = c0 + grp;
+    const bool valid = c < ncells;
+    const uint32_t a = valid ? cell_off[c] : 0u, b = valid ? cell_off[c + 1] : 0u;
+    if (__any_sync(0xffffffffu, b - a > 32u)) {
+        // the four cells one after the other, all 32 lanes on each
+        for (uint32_t g = 0; g < kCells; ++g) {
+            const uint32_t cg = c0 + g;
+            if (cg >= ncells) break;  // warp-uniform
+            const uint32_t ag = __shfl_sync(0xffffffffu, a, g * kSubLanes), bg = __shfl_sync(0xffffffffu, b, g * kSubLanes);
+            subsort_cell<32>(true, cg, ag, bg, cell_box(cg, one, boxes, nbox), 0xffffffffu, lane, perm, pos,
+                             sorted_pos, perm_s, slices, fixed);
+        }
+    } else {
+        const CellBox d = valid ? cell_box(c, one, boxes, nbox) : one;
+        subsort_cell<kSubLanes>(valid, c, a, b, d, 0xffu << (grp * kSubLanes), lane % kSubLanes, perm, pos,
+                                sorted_pos, perm_s, slices, fixed);
     }
 }
 
@@ -391,7 +435,7 @@ cuco_status_t launch_cell_subsort(const uint32_t *cell_off, const uint32_t *perm
                                   const CellBox &one, const CellBox *boxes, int nbox, bool fixed,
                                   cudaStream_t stream) {
     if (ncells == 0) return CUCO_OK;
-    const uint64_t threads = 32ull * ncells;
+    const uint64_t threads = 32ull * ((ncells + 32 / kSubLanes - 1) / (32 / kSubLanes));
     k_cell_subsort<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(
         cell_off, perm, pos, sorted_pos, perm_s, slices, ncells, one, boxes, nbox, fixed ? 1 : 0);
     CUCO_TRY_CUDA(cudaGetLastError());
