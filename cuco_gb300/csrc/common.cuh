@@ -77,10 +77,14 @@ size_t sort_hist_entries(uint32_t n, int key_bits, int max_radix_bits);
 // be null: the values are then the input positions 0..n-1.  The sorted data
 // ends in (keys, vals) when `result_in_alt` comes back false, else in
 // (keys_alt, vals_alt).  max_radix_bits bounds the digit width (4..8).
+// hist2: a second histogram of the same size, or null.  With it each pass's
+// scatter also counts the next pass's digits of the keys it places (into the
+// other histogram, cleared by the pass's scan), so only the first pass runs a
+// histogram kernel; the result is the same.
 cuco_status_t sort_pairs(uint32_t *keys, uint32_t *vals, const uint32_t *vals_in,
                          uint32_t *keys_alt, uint32_t *vals_alt, uint32_t *hist, uint32_t n,
                          int key_bits, int max_radix_bits, cudaStream_t stream,
-                         bool *result_in_alt, int *launches);
+                         bool *result_in_alt, int *launches, uint32_t *hist2 = nullptr);
 
 // Cell keys of float4 positions (calcHashD rule); idx gets 0..n-1 when non-null.
 cuco_status_t launch_cell_keys(const float4 *pos, uint32_t *keys, uint32_t *idx, uint32_t n,

@@ -315,7 +315,7 @@ struct cuco_box {
     float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr;
     float4 *spos = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr;
-    uint32_t *hist = nullptr, *cell_off = nullptr;
+    uint32_t *hist = nullptr, *hist2 = nullptr, *cell_off = nullptr;
     uint4 *cell_sl = nullptr;  // per cell: z-slice counts
     uint32_t *sorted_keys = nullptr, *sorted_perm = nullptr;  // where the last sort ended
     uint32_t *perm_s = nullptr;  // the z-slice order's map to original indices (the sort's spare buffer)
@@ -387,6 +387,17 @@ void record(cuco_box *b, int i, cudaStream_t s = nullptr) {
     if (b->timing) cudaEventRecord(b->ev[b->ev_cur][i], s ? s : b->stream);
 }
 
+// Particle count from which the short range runs beside the PM (a split
+// launch) rather than after it.
+constexpr uint32_t kSplitMinParticles = 1u << 20;
+
+// The box's stream waits for everything enqueued on the PM's stream so far.
+cuco_status_t join_pm(cuco_box *b) {
+    CUCO_TRY_CUDA(cudaEventRecord(b->join, b->pm_stream));
+    CUCO_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
+    return CUCO_OK;
+}
+
 // keys must already be in b->keys; runs sort, reorder, PM, short range (+kick)
 cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kick) {
     // The PM reads the positions in original order and writes its
@@ -407,7 +418,7 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
     }
     bool in_alt = false;
     CUCO_TRY(sort_pairs(b->keys, b->perm, nullptr, b->keys_alt, b->perm_alt, b->hist, b->n,
-                        b->key_bits, 8, b->stream, &in_alt, &b->launches));
+                        b->key_bits, 8, b->stream, &in_alt, &b->launches, b->hist2));
     b->sorted_keys = in_alt ? b->keys_alt : b->keys;
     b->sorted_perm = in_alt ? b->perm_alt : b->perm;
     record(b, 2);
@@ -423,37 +434,37 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
                                  nullptr, 1, b->cfg.mode == CUCO_MODE_FIXED, b->stream));
     b->launches += 2;
     record(b, 3);
+    // The short range needs nothing from the PM: in a large box it starts
+    // when the cell order is ready, one CTA per SM short of a full persistent
+    // grid, so the PM's remaining kernels keep running beside it; its last
+    // CTAs are queued on the PM's stream behind the PM and take the units
+    // left then, and the PM half of the kick follows once both are done.  A
+    // small box's step is launch-bound: its short range waits for the PM and
+    // applies both halves of the kick in its epilogue (fewer launches).
+    const bool split = pm && b->n >= kSplitMinParticles;
+    if (pm && !split) CUCO_TRY(join_pm(b));
     record(b, 8);
-    // The short range needs nothing from the PM: it starts when the cell
-    // order is ready, one CTA per SM short of a full persistent grid, so the
-    // PM's remaining kernels keep running beside it; its last CTAs are
-    // queued on the PM's stream behind the PM and take the units left then.
-    // The PM half of the kick follows once both are done.
     const bool kick_on = kick && kick->vel;
     if (pp) {
         KickArgs k{};
         if (kick) k = *kick;
         k.acc_pm_s = nullptr;
         k.acc_pm_out = nullptr;
-        k.acc_pm_o = nullptr;
+        k.acc_pm_o = pm && !split ? b->acc_pm : nullptr;
         CUCO_TRY(launch_shortrange(make_sr_params(b), b->spos, perm_s, b->cell_off,
                                    nullptr, kCellOffsets, b->table, b->acc_pp, k, b->work, b->stream,
-                                   b->count_pairs ? b->pair_counter : nullptr, pm ? b->pm_stream : nullptr,
+                                   b->count_pairs ? b->pair_counter : nullptr, split ? b->pm_stream : nullptr,
                                    b->sr_plan));
-        b->launches += pm ? 3 : 2;  // work plan + persistent short range (in two parts beside the PM)
+        b->launches += split ? 3 : 2;  // work plan + persistent short range (in two parts beside the PM)
     }
-    if (pm) {
-        CUCO_TRY_CUDA(cudaEventRecord(b->join, b->pm_stream));
-        CUCO_TRY_CUDA(cudaStreamWaitEvent(b->stream, b->join, 0));
+    if (split) CUCO_TRY(join_pm(b));
+    record(b, 9);  // the short range done (both parts)
+    if (split && pp && kick_on && b->n) {
+        k_kick_pm<<<(b->n + 255) / 256, 256, 0, b->stream>>>(kick->vel, b->acc_pm, b->n, (float)kick->kick_pm);
+        CUCO_TRY_CUDA(cudaGetLastError());
+        b->launches += 1;
     }
-    record(b, 9);  // both parts of the short range done
-    if (pm) {
-        if (pp && kick_on && b->n) {
-            k_kick_pm<<<(b->n + 255) / 256, 256, 0, b->stream>>>(kick->vel, b->acc_pm, b->n, (float)kick->kick_pm);
-            CUCO_TRY_CUDA(cudaGetLastError());
-            b->launches += 1;
-        }
-    }
+    if (pm && !pp) CUCO_TRY(join_pm(b));
     record(b, 7);
     return CUCO_OK;
 }
@@ -560,6 +571,7 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
         (s = alloc(&b->keys, n)) || (s = alloc(&b->perm, n)) || (s = alloc(&b->keys_alt, n)) ||
         (s = alloc(&b->perm_alt, n)) ||
         (s = alloc(&b->hist, sort_hist_entries(b->n, b->key_bits, 8))) ||
+        (s = alloc(&b->hist2, sort_hist_entries(b->n, b->key_bits, 8))) ||
         (s = alloc(&b->cell_off, (size_t)b->ncells + 1)) || (s = alloc(&b->cell_sl, (size_t)b->ncells)) ||
         (s = alloc(&b->table, kNTab)) ||
         (s = alloc(&b->stage3, 3 * n)) || (s = alloc(&b->pair_counter, 1)) ||
@@ -604,6 +616,7 @@ cuco_status_t cuco_box_destroy(cuco_box_t *b) {
     cudaFree(b->keys_alt);
     cudaFree(b->perm_alt);
     cudaFree(b->hist);
+    cudaFree(b->hist2);
     cudaFree(b->cell_off);
     cudaFree(b->cell_sl);
     cudaFree(b->table);

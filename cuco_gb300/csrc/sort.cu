@@ -74,10 +74,15 @@ __global__ void __launch_bounds__(kSortThreads)
 // those counts over the tiles, one CTA per digit.  A digit's total is then its
 // last entry, and the scatter derives every run's global offset from these
 // (no second pass over the table, no scratch beyond it).
-__global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__restrict__ hist, uint32_t tiles) {
+// zero_next (or null): the next pass's histogram, whose row of this digit is
+// cleared here for the scatter to count into.
+__global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__restrict__ hist, uint32_t tiles,
+                                                            uint32_t *__restrict__ zero_next) {
     __shared__ uint32_t wsum[kSortWarps];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *h = hist + (size_t)blockIdx.x * tiles;
+    if (zero_next)
+        for (uint32_t t = threadIdx.x; t < tiles; t += kSortThreads) zero_next[(size_t)blockIdx.x * tiles + t] = 0u;
     uint32_t carry = 0;
     for (uint32_t t0 = 0; t0 < tiles; t0 += kSortThreads) {
         const uint32_t t = t0 + threadIdx.x;
@@ -103,11 +108,15 @@ __global__ void __launch_bounds__(kSortThreads) k_sort_scan(uint32_t *__restrict
     }
 }
 
-template <int RB, bool WITH_VALS, bool SINGLE_TILE>
+// NEXT: also count the next pass's digit (at next_shift) of every key placed,
+// per destination tile, into next_hist (cleared by this pass's scan): the
+// histogram the next pass would build from this pass's output.
+template <int RB, bool WITH_VALS, bool SINGLE_TILE, bool NEXT>
 __global__ void __launch_bounds__(kSortThreads, 4)
     k_sort_scatter(const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin,
                    uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint32_t n,
-                   int shift, const uint32_t *__restrict__ hist, uint32_t tiles) {
+                   int shift, const uint32_t *__restrict__ hist, uint32_t tiles,
+                   uint32_t *__restrict__ next_hist, int next_shift) {
     constexpr int RADIX = 1 << RB;
     __shared__ uint32_t wcnt[kSortWarps][RADIX];
     __shared__ uint32_t dstart[RADIX];
@@ -209,38 +218,68 @@ __global__ void __launch_bounds__(kSortThreads, 4)
     }
     __syncthreads();
     const uint32_t tile_n = min((uint32_t)kSortTile, n - base);
-    for (uint32_t j = threadIdx.x; j < tile_n; j += kSortThreads) {
-        const uint32_t kk = skeys[j];
-        const uint32_t d = (kk >> shift) & (RADIX - 1);
-        const uint32_t o = gbase[d] + j - dstart[d];
-        kout[CUCO_IDX(o, n)] = kk;
-        if (WITH_VALS) vout[CUCO_IDX(o, n)] = svals[j];
+    // (the loop's trip count is the same for every lane of a warp: tile_n
+    // only cuts the last warp's lanes, which still vote)
+    for (uint32_t j0 = 0; j0 < (uint32_t)kSortTile; j0 += kSortThreads) {
+        const uint32_t j = j0 + threadIdx.x;
+        const bool in = j < tile_n;
+        uint32_t kk = 0, o = 0;
+        if (in) {
+            kk = skeys[j];
+            const uint32_t d = (kk >> shift) & (RADIX - 1);
+            o = gbase[d] + j - dstart[d];
+            kout[CUCO_IDX(o, n)] = kk;
+            if (WITH_VALS) vout[CUCO_IDX(o, n)] = svals[j];
+        }
+        if (NEXT) {
+            // one atomic per (digit, destination tile) group of the warp
+            const uint32_t slot = in ? ((kk >> next_shift) & (RADIX - 1)) * tiles + o / kSortTile : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(kFull, slot);
+            if (in && (threadIdx.x & 31) == __ffs(peers) - 1)
+                atomicAdd(&next_hist[CUCO_IDX(slot, (uint32_t)RADIX * tiles)], (uint32_t)__popc(peers));
+        }
     }
 }
 
+// One pass.  hist_ready: `hist` already holds this pass's histogram (counted
+// by the previous pass's scatter); next_hist (or null): count the next pass's
+// digits at next_shift into it.
 template <int RB>
 cuco_status_t sort_pass(const uint32_t *kin, const uint32_t *vin, uint32_t *kout, uint32_t *vout,
                         bool with_vals, uint32_t *hist, uint32_t n, int shift,
-                        cudaStream_t stream, int *launches) {
+                        cudaStream_t stream, int *launches, bool hist_ready = false,
+                        uint32_t *next_hist = nullptr, int next_shift = 0) {
     const uint32_t tiles = (n + kSortTile - 1) / kSortTile;
     if (tiles == 1) {
         if (with_vals)
-            k_sort_scatter<RB, true, true><<<1, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n,
-                                                                          shift, hist, tiles);
+            k_sort_scatter<RB, true, true, false><<<1, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n, shift,
+                                                                                 hist, tiles, nullptr, 0);
         else
-            k_sort_scatter<RB, false, true><<<1, kSortThreads, 0, stream>>>(kin, vin, kout, vout,
-                                                                           n, shift, hist, tiles);
+            k_sort_scatter<RB, false, true, false><<<1, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n, shift,
+                                                                                  hist, tiles, nullptr, 0);
         *launches += 1;
     } else {
-        k_sort_hist<RB><<<tiles, kSortThreads, 0, stream>>>(kin, n, shift, hist, tiles);
-        k_sort_scan<<<1u << RB, kSortThreads, 0, stream>>>(hist, tiles);
-        if (with_vals)
-            k_sort_scatter<RB, true, false><<<tiles, kSortThreads, 0, stream>>>(
-                kin, vin, kout, vout, n, shift, hist, tiles);
-        else
-            k_sort_scatter<RB, false, false><<<tiles, kSortThreads, 0, stream>>>(
-                kin, vin, kout, vout, n, shift, hist, tiles);
-        *launches += 3;
+        if (!hist_ready) {
+            k_sort_hist<RB><<<tiles, kSortThreads, 0, stream>>>(kin, n, shift, hist, tiles);
+            *launches += 1;
+        }
+        k_sort_scan<<<1u << RB, kSortThreads, 0, stream>>>(hist, tiles, next_hist);
+        if (next_hist) {
+            if (with_vals)
+                k_sort_scatter<RB, true, false, true><<<tiles, kSortThreads, 0, stream>>>(
+                    kin, vin, kout, vout, n, shift, hist, tiles, next_hist, next_shift);
+            else
+                k_sort_scatter<RB, false, false, true><<<tiles, kSortThreads, 0, stream>>>(
+                    kin, vin, kout, vout, n, shift, hist, tiles, next_hist, next_shift);
+        } else {
+            if (with_vals)
+                k_sort_scatter<RB, true, false, false><<<tiles, kSortThreads, 0, stream>>>(
+                    kin, vin, kout, vout, n, shift, hist, tiles, nullptr, 0);
+            else
+                k_sort_scatter<RB, false, false, false><<<tiles, kSortThreads, 0, stream>>>(
+                    kin, vin, kout, vout, n, shift, hist, tiles, nullptr, 0);
+        }
+        *launches += 2;
     }
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
@@ -452,7 +491,7 @@ size_t sort_hist_entries(uint32_t n, int key_bits, int max_radix_bits) {
 cuco_status_t sort_pairs(uint32_t *keys, uint32_t *vals, const uint32_t *vals_in,
                          uint32_t *keys_alt, uint32_t *vals_alt, uint32_t *hist, uint32_t n,
                          int key_bits, int max_radix_bits, cudaStream_t stream,
-                         bool *result_in_alt, int *launches) {
+                         bool *result_in_alt, int *launches, uint32_t *hist2) {
     int passes, rb;
     split_bits(key_bits, max_radix_bits, &passes, &rb);
     bool with_vals = vals != nullptr;
@@ -460,17 +499,28 @@ cuco_status_t sort_pairs(uint32_t *keys, uint32_t *vals, const uint32_t *vals_in
     if (n == 0) return CUCO_OK;
     uint32_t *kbuf[2] = {keys, keys_alt};
     uint32_t *vbuf[2] = {vals, vals_alt};
+    uint32_t *hbuf[2] = {hist, hist2 ? hist2 : hist};
     int cur = 0;
     for (int p = 0; p < passes; ++p) {
         const uint32_t *vin = (p == 0) ? vals_in : vbuf[cur];
-        int shift = p * rb;
+        const int shift = p * rb;
+        // with two histograms, pass p uses hbuf[p & 1] and counts pass p+1's
+        // digits into the other
+        const bool fused = hist2 != nullptr;
+        uint32_t *h = hbuf[fused ? (p & 1) : 0];
+        uint32_t *hn = fused && p + 1 < passes ? hbuf[(p + 1) & 1] : nullptr;
+        const bool ready = fused && p > 0;
         cuco_status_t s;
         switch (rb) {
-            case 4: s = sort_pass<4>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
-            case 5: s = sort_pass<5>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
-            case 6: s = sort_pass<6>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
-            case 7: s = sort_pass<7>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
-            default: s = sort_pass<8>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, hist, n, shift, stream, launches); break;
+#define CUCO_SORT_PASS(R)                                                                                    \
+    s = sort_pass<R>(kbuf[cur], vin, kbuf[cur ^ 1], vbuf[cur ^ 1], with_vals, h, n, shift, stream, launches, \
+                     ready, hn, shift + rb)
+            case 4: CUCO_SORT_PASS(4); break;
+            case 5: CUCO_SORT_PASS(5); break;
+            case 6: CUCO_SORT_PASS(6); break;
+            case 7: CUCO_SORT_PASS(7); break;
+            default: CUCO_SORT_PASS(8); break;
+#undef CUCO_SORT_PASS
         }
         if (s != CUCO_OK) return s;
         cur ^= 1;
