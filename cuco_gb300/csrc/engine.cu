@@ -309,7 +309,8 @@ struct cuco_box {
     float gridfac = 0.f;
     cudaStream_t stream = nullptr;
     // the PM runs on its own stream beside the sort and the cell order,
-    // forked after the positions are final and joined before the short range
+    // forked after the positions are final; joined before the short range in
+    // a small box, after it in a large one (whose short range it runs beside)
     cudaStream_t pm_stream = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, sr_plan = nullptr;
     float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr;

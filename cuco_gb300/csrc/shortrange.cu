@@ -32,10 +32,11 @@
 //     that it evaluates against both targets in packed FP32 (float2
 //     add/mul/fma, one instruction for the two targets);
 //   * the pair law runs without branches on the common path and flags the
-//     rest (bin-edge and cut-edge pairs decided in double, the spline), which
-//     runs under one warp-uniform branch;
-//   * the warp adds its lanes' partial sums with xor shuffles (the precision
-//     form compensated by error-free splitting);
+//     rest (bin-edge and cut-edge pairs decided in double, the spline); the
+//     windows holding a flagged pair are revisited after the last window;
+//   * the warp reduces its lanes' six partial sums (3 components x 2
+//     targets) with a transpose-reduce of xor shuffles (the precision form
+//     compensated by error-free splitting);
 //   * the warp's lanes scatter the forces to original particle order and, in
 //     the engine's step, kick the velocities (timestep.c:56-59,86-91).
 //
