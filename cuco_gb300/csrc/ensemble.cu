@@ -288,6 +288,7 @@ struct cuco_ensemble {
     float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr, *spos = nullptr,
            *acc_pm_s = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr, *hist = nullptr,
+             *hist2 = nullptr,
              *cell_off = nullptr, *sorted_perm = nullptr;
     uint4 *cell_sl = nullptr;  // per cell: z-slice counts
     float *stage3 = nullptr;
@@ -327,7 +328,7 @@ struct cuco_ensemble {
     cudaStream_t pm_stream = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     // capacities (elements) of the grow-only arrays
-    size_t cap_n = 0, cap_hist = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
+    size_t cap_n = 0, cap_hist = 0, cap_hist2 = 0, cap_cells = 0, cap_stage3 = 0, cap_mesh = 0, cap_mesh64 = 0, cap_spec = 0,
            cap_green = 0, cap_tw = 0, cap_table = 0, cap_pbeg = 0, cap_segbase = 0, cap_drift = 0, cap_pm = 0,
            cap_kicks = 0, cap_factors = 0, cap_counter = 0, cap_sr = 0, cap_hfactors[2] = {0, 0},
            cap_hkicks[2] = {0, 0},
@@ -357,7 +358,7 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
     CUCO_TRY_CUDA(cudaEventRecord(e->join, e->pm_stream));
     bool in_alt = false;
     CUCO_TRY(sort_pairs(e->keys, e->perm, nullptr, e->keys_alt, e->perm_alt, e->hist, e->n, e->key_bits, 8,
-                        e->stream, &in_alt, &e->launches));
+                        e->stream, &in_alt, &e->launches, e->hist2));
     const uint32_t *skeys = in_alt ? e->keys_alt : e->keys;
     e->sorted_perm = in_alt ? e->perm_alt : e->perm;
     CUCO_TRY(launch_reorder_offsets(e->cell_off, nullptr, skeys, e->sorted_perm, e->pos, e->n, (uint32_t)e->ncells,
@@ -569,6 +570,7 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
     }
     const size_t nbc = (size_t)nbox + 1;
     if ((s = grow(e->hist, e->cap_hist, sort_hist_entries((uint32_t)n, kbits, 8), st)) ||
+        (s = grow(e->hist2, e->cap_hist2, sort_hist_entries((uint32_t)n, kbits, 8), st)) ||
         (s = grow(e->cell_off, e->cap_cells, ncells + 1, st)) || (s = grow(e->cell_sl, e->cap_cellsl, ncells, st)) || (s = grow(e->stage3, e->cap_stage3, 3 * maxn, st)) ||
         (s = grow(e->rho, e->cap_mesh, mbase[nbox], st)) ||
         (s = grow(e->rho64, e->cap_mesh64, mbase[nbox], st)) || (s = grow(e->spec, e->cap_spec, sbase[nbox], st)) ||
@@ -731,7 +733,7 @@ cuco_status_t cuco_ensemble_destroy(cuco_ensemble_t *e) {
     drop_graph(e);
     for (void *p : {(void *)e->pos, (void *)e->vel, (void *)e->acc_pp, (void *)e->acc_pm, (void *)e->spos,
                     (void *)e->acc_pm_s, (void *)e->keys, (void *)e->perm, (void *)e->keys_alt, (void *)e->perm_alt,
-                    (void *)e->hist, (void *)e->cell_off, (void *)e->cell_sl, (void *)e->stage3, (void *)e->rho, (void *)e->rho64,
+                    (void *)e->hist, (void *)e->hist2, (void *)e->cell_off, (void *)e->cell_sl, (void *)e->stage3, (void *)e->rho, (void *)e->rho64,
                     (void *)e->spec,
                     (void *)e->green, (void *)e->tw, (void *)e->table, (void *)e->d_pbeg, (void *)e->d_segbase,
                     (void *)e->d_drift, (void *)e->d_pm, (void *)e->d_mapz, (void *)e->d_mapa, (void *)e->d_sr,
@@ -914,9 +916,10 @@ cuco_status_t cuco_ensemble_footprint(const cuco_config_t *boxes, int nbox, uint
         set_error("cuco_ensemble_footprint: invalid argument");
         return CUCO_ERR_INVALID;
     }
-    uint64_t b = 0, maxn = 0;
+    uint64_t b = 0, maxn = 0, ntot = 0;
     for (int k = 0; k < nbox; ++k) {
         const uint64_t n = (uint64_t)boxes[k].n, M = (uint64_t)boxes[k].pm_grid;
+        ntot += n;
         const uint64_t G = boxes[k].cell_grid > 0 ? (uint64_t)boxes[k].cell_grid : M / 2;  // the largest tuned grid
         b += n * (6 * sizeof(float4) + 4 * sizeof(uint32_t));    // state, sorted copies, keys
         b += 4 * (G * G * G + 1) + 16 * G * G * G;               // cell offsets, z-slice counts
@@ -925,6 +928,7 @@ cuco_status_t cuco_ensemble_footprint(const cuco_config_t *boxes, int nbox, uint
         maxn = std::max(maxn, n);
     }
     b += 12 * maxn + 4 * (uint64_t)kNTab;
+    b += 2 * 4 * 256 * (ntot / 4096 + 1);  // the sort's two digit histograms (digits of at most 8 bits)
     *bytes = b;
     return CUCO_OK;
 }
