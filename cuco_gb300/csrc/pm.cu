@@ -239,7 +239,7 @@ __device__ __forceinline__ void dft_reg(float2 (&v)[N]) {
 template <int M1, int M2>
 struct RegFFT {
     static constexpr int M = M1 * M2, N1 = M1, N2 = M2;
-    static constexpr int T = M1 > M2 ? M1 : M2;  // threads per column
+    // a column takes max(M1, M2) threads
     __device__ static int slot(int k) { return M2 * (k & (M1 - 1)) + k / M1; }
     // twiddle exp(S 2 pi i j / M) from the table of exp(-2 pi i j / M)
     template <int S>
@@ -967,7 +967,7 @@ __device__ __forceinline__ void deposit_one(float4 p, unsigned long long *__rest
         for (int c = 0; c < 8; ++c) w[c] = sum[c];
     }
     if (lead) {
-        const uint32_t M3 = (uint32_t)(Myz * Mz);
+        [[maybe_unused]] const uint32_t M3 = (uint32_t)(Myz * Mz);  // the bounds checks' grid size
         atomicAdd(&rho64[CUCO_IDX(sx * Myz + sy * Mz + sz, M3)], w[0]);
         atomicAdd(&rho64[CUCO_IDX(sx * Myz + syy * Mz + sz, M3)], w[1]);
         atomicAdd(&rho64[CUCO_IDX(sx * Myz + sy * Mz + szz, M3)], w[2]);
