@@ -674,14 +674,16 @@ __device__ __forceinline__ bool shortrange_segment(
             // The windows with a rare-case pair are only marked here (at most
             // 64: T <= kMaxStage) and revisited after the last one, so the
             // loop carries none of the rare-case law's code.
-            uint64_t wslow = 0;
-            uint32_t before = 0, wi = 0;
-            for (uint32_t base = 0; base < T; base += 32, ++wi) {
+            // (two windows per iteration: their loads and laws interleave)
+            uint64_t wslow = 0, wbit = 1;
+            uint32_t before = 0;
+#pragma unroll 2
+            for (uint32_t base = 0; base < T; base += 32, wbit <<= 1) {
                 uint32_t m0;
                 const float4 s0 = window_source(base, before, m0);
                 bool xa, xb;
                 pair_fast2(s0, ntx, nty, ntz, sx, sy, sz, xa, xb, true);
-                if (__any_sync(kFull, xa || xb)) wslow |= 1ull << wi;
+                if (__any_sync(kFull, xa || xb)) wslow |= wbit;
                 before += __popc(m0);
             }
             // the rare-case pairs, window by window: the lane's candidate
