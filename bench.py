@@ -324,12 +324,13 @@ def run_serving(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_shortrange launch at
-# z = 49 (ncu --set full, the first timed step of
-# `bench.py --steps 2 --warmup 3 --e2e-steps 0 --no-cpu`; 116.9 + 30.5 MB), and
-# of the precision form's launch (same command with --workload precision-128)
-SR_TRAFFIC = {"plain-128^3-L256-M256-G64-z49to0-200steps": 147.4e6,
-              "precision-128^3-L256-M256-G64-z49to0-200steps": 150.2e6}
+# dram__bytes_read.sum + dram__bytes_write.sum of the short range at z = 49:
+# ncu --set full of the first part of the split launch in the first timed step
+# of `bench.py --steps 2 --warmup 3 --e2e-steps 0 --no-cpu` (-s 6 -c 1), which
+# runs alone under ncu and takes every unit (83.0 + 20.9 MB), and of the
+# precision form's (same command with --workload precision-128; 83.3 + 23.1 MB)
+SR_TRAFFIC = {"plain-128^3-L256-M256-G64-z49to0-200steps": 103.9e6,
+              "precision-128^3-L256-M256-G64-z49to0-200steps": 106.4e6}
 
 
 # softening (fraction of the mean spacing) of the small box: 0.03, the others 0.025
@@ -692,8 +693,9 @@ def run_gpu_arm(args, world, rank, local):
         "roofline": {"bound": "fp32", "kernel": "k_shortrange", "achieved": achieved,
                      "peak": peak.value, "unit": "TFLOP/s", "frac": achieved / peak.value,
                      "traffic": SR_TRAFFIC.get(WORKLOAD),
-                     "traffic_note": "DRAM bytes read + written by one short-range launch at z = 49, from an ncu "
-                                     "capture of this workload (not measured by this run)",
+                     "traffic_note": "DRAM bytes read + written by the short range at z = 49, from an ncu capture "
+                                     "of this workload (its split launch's first part, alone under ncu, takes "
+                                     "every unit; not measured by this run)",
                      "convention": "20 FP32 flops per in-range pair (pairs counted in-kernel in an untimed replay "
                                    "of the same steps), "
                                    "peak = measured FMA throughput"},
