@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -313,6 +314,7 @@ struct cuco_box {
     // a small box, after it in a large one (whose short range it runs beside)
     cudaStream_t pm_stream = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, sr_plan = nullptr;
+    uint32_t split_min = 0;  // particles from which the short range runs beside the PM
     float4 *pos = nullptr, *vel = nullptr, *acc_pp = nullptr, *acc_pm = nullptr;
     float4 *spos = nullptr;
     uint32_t *keys = nullptr, *perm = nullptr, *keys_alt = nullptr, *perm_alt = nullptr;
@@ -389,8 +391,18 @@ void record(cuco_box *b, int i, cudaStream_t s = nullptr) {
 }
 
 // Particle count from which the short range runs beside the PM (a split
-// launch) rather than after it.
+// launch) rather than after it; CUCO_SPLIT_MIN_PARTICLES, read when a box is
+// created, overrides it (the two schedules give the same results: the tests
+// compare them).
 constexpr uint32_t kSplitMinParticles = 1u << 20;
+
+uint32_t split_min_particles() {
+    const char *env = getenv("CUCO_SPLIT_MIN_PARTICLES");
+    if (!env || !*env) return kSplitMinParticles;
+    char *end = nullptr;
+    const unsigned long long v = strtoull(env, &end, 10);
+    return end && *end == '\0' && v <= 0xffffffffull ? (uint32_t)v : kSplitMinParticles;
+}
 
 // The box's stream waits for everything enqueued on the PM's stream so far.
 cuco_status_t join_pm(cuco_box *b) {
@@ -442,7 +454,7 @@ cuco_status_t forces_after_keys(cuco_box *b, int pm, int pp, const KickArgs *kic
     // left then, and the PM half of the kick follows once both are done.  A
     // small box's step is launch-bound: its short range waits for the PM and
     // applies both halves of the kick in its epilogue (fewer launches).
-    const bool split = pm && b->n >= kSplitMinParticles;
+    const bool split = pm && b->n >= b->split_min;
     if (pm && !split) CUCO_TRY(join_pm(b));
     record(b, 8);
     const bool kick_on = kick && kick->vel;
@@ -543,6 +555,7 @@ cuco_status_t cuco_box_create(const cuco_config_t *cfg, cuco_box_t **out) {
     b->ncells = (uint32_t)b->G * b->G * b->G;
     b->key_bits = bits_for(b->ncells);
     b->gridfac = (float)b->G / cfg->boxsize;  // float division as gravlist.cpp:61
+    b->split_min = split_min_particles();
     cuco_status_t s = CUCO_OK;
     auto fail = [&](cuco_status_t st) {
         cuco_box_destroy(b);
