@@ -207,11 +207,16 @@ cuco_status_t launch_shortrange(const ShortRangeParams &p, const float4 *sorted_
 // count and shared memory.  kicks[b] = (kick_pp, kick_pm) of box b.
 size_t shortrange_desc_bytes();
 cuco_status_t shortrange_desc_fill(const ShortRangeParams &p, void *desc, uint32_t *segments, size_t *smem);
+// uniform_law_desc (host memory, or null): a descriptor whose pair law every
+// box shares (shortrange_descs_uniform_law said so); the launch then reads
+// the law from its parameters instead of each box's descriptor.
+bool shortrange_descs_uniform_law(const void *host_descs, int nbox);
 cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, const uint32_t *seg_base,
                                       int nbox, uint32_t segments, size_t smem, bool fixed,
                                       const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
                                       const float *table, float4 *acc_out, const KickArgs &kick,
-                                      const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter);
+                                      const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter,
+                                      const void *uniform_law_desc = nullptr);
 
 // ------------------------------------------------------------------- PM
 

@@ -316,6 +316,9 @@ struct cuco_ensemble {
     PMMulti pm{};
     uint32_t segments = 0;
     size_t sr_smem = 0;
+    // box 0's short-range descriptor (host copy) when every box has its pair
+    // law, so the launch reads the law from its parameters
+    std::vector<char> sr_law;
     unsigned long long *pair_counter = nullptr;
     bool count_pairs = false;
     bool has_state = false;
@@ -376,7 +379,8 @@ cuco_status_t ensemble_pass(cuco_ensemble *e, int do_drift, bool kick) {
     SRWork w{e->sr_heavy, (uint32_t)e->cap_heavy, e->sr_segnt, (uint32_t)e->cap_segnt, e->sr_ctl};
     CUCO_TRY(launch_shortrange_multi(e->d_sr, e->d_kicks, e->d_segbase, e->nbox, e->segments, e->sr_smem, e->fixed,
                                      e->spos, perm_s, e->cell_off, e->table, e->acc_pp, k, w, e->stream,
-                                     e->count_pairs ? e->pair_counter : nullptr));
+                                     e->count_pairs ? e->pair_counter : nullptr,
+                                     e->sr_law.empty() ? nullptr : e->sr_law.data()));
     e->launches += 2;  // work plan + persistent short range
     return CUCO_OK;
 }
@@ -652,6 +656,9 @@ cuco_status_t ensemble_layout(cuco_ensemble *e, const cuco_config_t *boxes, int 
     e->key_bits = kbits;
     e->segments = segbase[nbox];
     e->sr_smem = sr_smem;
+    e->sr_law.clear();
+    if (shortrange_descs_uniform_law(srd.data(), nbox))
+        e->sr_law.assign(srd.begin(), srd.begin() + shortrange_desc_bytes());
     e->pm = PMMulti{nbox, e->fixed, e->d_pm, e->d_pbeg, e->d_mapz, e->d_mapa, (uint32_t)mapz.size(),
                     (uint32_t)mapa.size(), smz, sma, e->rho64, (size_t)mbase[nbox]};
     for (int b = 0; b < nbox; ++b) e->pm.big = e->pm.big || pm_big_fft(cfg[b].pm_grid, P[b], B[b]);

@@ -243,9 +243,13 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 // are that box's kick factors.  A unit has at most kTMax targets.
 // Returns false when a staging wait gave up (the error word is set; the CTA
 // must stop).  `phase` is the parity of the CTA's staging barrier.
+// `law`: the pair law's constants (rc2_lo, rc2_hi, hmin2, alo, ahi, rcut2_d,
+// asmthfac_d, h, hinv, h3inv): the box's own (p), or the launch's when every
+// box of a many-box launch has the same (read from the kernel's parameters).
 template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
 __device__ __forceinline__ bool shortrange_segment(
-    const ShortRangeParams &p, const ColumnSet &cs, const int seg, const uint32_t slice_lo,
+    const ShortRangeParams &p, const ShortRangeParams &law, const ColumnSet &cs, const int seg,
+    const uint32_t slice_lo,
     const uint32_t slice_hi, const double kick_pp, const double kick_pm, const float4 *__restrict__ spos,
     const uint32_t *__restrict__ perm, const uint32_t *__restrict__ ca, const uint32_t *__restrict__ cb,
     const float *__restrict__ table_g, float4 *__restrict__ acc_out, const KickArgs &kick,
@@ -488,7 +492,8 @@ __device__ __forceinline__ bool shortrange_segment(
     // made in double and the spline inside h (the self pair, r = 0, adds
     // nothing and is skipped).  pair_slow applies the full law to those.  Both add into the same
     // accumulators in the same order as a single law would.
-    // The bounds (p.rc2_lo, ...) are the launch's constants, read where used.
+    // The bounds (law.rc2_lo, ...) are kernel parameters where the law is the
+    // launch's, read where used.
     // bin = floor(asmthfac * r): a round-toward-zero fma onto 2^23 leaves the
     // floor in the mantissa, with no conversion instruction.  Plain: the bins
     // of r * asmthfac * (1 -/+ kEdge) differ when r lies within kEdge
@@ -502,7 +507,7 @@ __device__ __forceinline__ bool shortrange_segment(
     // coordinates held in registers, so d = s + (-t) = s - t exactly.  Every
     // element is rounded as the scalar law rounds it: the result is the
     // scalar law's, bit for bit, for each target.
-    const float2 alo2 = make_float2(p.alo, p.alo), ahi2 = make_float2(p.ahi, p.ahi);
+    const float2 alo2 = make_float2(law.alo, law.alo), ahi2 = make_float2(law.ahi, law.ahi);
     const float2 magic2 = make_float2(8388608.0f, 8388608.0f);
     // acc = false: the flags alone (the revisit of a window with rare-case
     // pairs), nothing added or counted.
@@ -526,8 +531,8 @@ __device__ __forceinline__ bool shortrange_segment(
         // the bin is the mantissa's low bits (2^23's own are zero)
         const float2 t = make_float2(tab[__float_as_uint(xl.x) & (kTabPad - 1)],
                                      tab[__float_as_uint(xl.y) & (kTabPad - 1)]);
-        const bool fast_a = r2.x <= p.rc2_lo && r2.x >= p.hmin2 && !edge_a;
-        const bool fast_b = r2.y <= p.rc2_lo && r2.y >= p.hmin2 && !edge_b;
+        const bool fast_a = r2.x <= law.rc2_lo && r2.x >= law.hmin2 && !edge_a;
+        const bool fast_b = r2.y <= law.rc2_lo && r2.y >= law.hmin2 && !edge_b;
         const float2 f = __fmul2_rn(__fmul2_rn(__fmul2_rn(rinv, rinv), rinv), t);
         const float2 fac = make_float2(fast_a ? f.x : 0.f, fast_b ? f.y : 0.f);
         if (acc) {
@@ -538,27 +543,27 @@ __device__ __forceinline__ bool shortrange_segment(
         }
         // r2 == 0 (the self pair, or a coincident source) adds dx*fac = 0:
         // not flagged, so the rare-case branch is not taken once per target
-        slow_a = r2.x <= p.rc2_hi && r2.x != 0.f && !fast_a;
-        slow_b = r2.y <= p.rc2_hi && r2.y != 0.f && !fast_b;
+        slow_a = r2.x <= law.rc2_hi && r2.x != 0.f && !fast_a;
+        slow_b = r2.y <= law.rc2_hi && r2.y != 0.f && !fast_b;
     };
     auto pair_slow = [&](float4 s, float tx, float ty, float tz, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
         const float r2 = dist2(dx, dy, dz);
-        bool ok = r2 <= p.rc2_hi && r2 != 0.f;
+        bool ok = r2 <= law.rc2_hi && r2 != 0.f;
         const float rinv = rsqrtf(ok ? r2 : 1.f);
         const float r = r2 * rinv;
-        const float xl = __fmaf_rz(r, p.alo, 8388608.0f);
+        const float xl = __fmaf_rz(r, law.alo, 8388608.0f);
         int ti = __float_as_int(xl) - 0x4B000000;
         float fac = rinv * rinv * rinv;
-        if (!FIXED && (xl != __fmaf_rz(r, p.ahi, 8388608.0f) || r2 > p.rc2_lo)) {
+        if (!FIXED && (xl != __fmaf_rz(r, law.ahi, 8388608.0f) || r2 > law.rc2_lo)) {
             // decided in double as the reference's CPU path computes it
             const double dd = (double)dx * dx + (double)dy * dy + (double)dz * dz;
-            ok = ok && dd <= p.rcut2_d;
-            ti = (int)(p.asmthfac_d * sqrt(dd));
+            ok = ok && dd <= law.rcut2_d;
+            ti = (int)(law.asmthfac_d * sqrt(dd));
         }
-        if (r < p.h) {
-            const float u = r * p.hinv;
-            const float h3inv = p.h3inv;
+        if (r < law.h) {
+            const float u = r * law.hinv;
+            const float h3inv = law.h3inv;
             if (u < 0.5f)
                 fac = __fmul_rn(h3inv, __fmaf_rn(__fmul_rn(u, u), __fmaf_rn(32.0f, u, -38.4f), 10.66667f));
             else
@@ -1028,7 +1033,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
     load_table(table_g);
     while (next_unit(w, nseg, &seg, &lo, &skip)) {
         if (skip) continue;
-        if (!shortrange_segment<FMT, KICK, COUNT, FIXED>(p, cs, (int)seg, lo, lo + kTMax, kick.kick_pp,
+        if (!shortrange_segment<FMT, KICK, COUNT, FIXED>(p, p, cs, (int)seg, lo, lo + kTMax, kick.kick_pp,
                                                          kick.kick_pm, spos, perm, ca, cb, table_g, acc_out, kick,
                                                          pair_counter, phase, w.ctl + 2))
             return;
@@ -1048,14 +1053,17 @@ __global__ void k_sr_plan_multi(const SRBoxDesc *__restrict__ boxes, const uint3
     plan_segment<kCellOffsets>(d.p, d.cs.S, gseg - seg_base[b], gseg, cell_off, nullptr, w);
 }
 
-template <bool KICK, bool COUNT, bool FIXED>
+// UNIFORM: every box has the pair law of `law` (a kernel parameter, read as
+// constant-bank operands); else each box's own from its descriptor.
+template <bool KICK, bool COUNT, bool FIXED, bool UNIFORM>
 __global__ void __launch_bounds__(kThreads, kMinBlocks)
     k_shortrange_multi(const SRBoxDesc *__restrict__ boxes, const double2 *__restrict__ kicks,
                        const uint32_t *__restrict__ seg_base, int nbox, uint32_t nseg,
                        const __grid_constant__ SRWork w, const float4 *__restrict__ spos,
                        const uint32_t *__restrict__ perm, const uint32_t *__restrict__ cell_off,
                        const float *__restrict__ table_g, float4 *__restrict__ acc_out,
-                       const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter) {
+                       const __grid_constant__ KickArgs kick, unsigned long long *__restrict__ pair_counter,
+                       const __grid_constant__ ShortRangeParams law) {
     uint32_t seg, lo, phase = 0;
     bool skip;
     load_table(table_g);
@@ -1064,10 +1072,10 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const int b = find_box(seg_base, nbox, seg);
         const SRBoxDesc &d = boxes[b];
         const double2 k = KICK ? kicks[b] : make_double2(0.0, 0.0);
-        if (!shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, d.cs, (int)(seg - seg_base[b]), lo,
-                                                                  lo + kTMax, k.x, k.y, spos, perm, cell_off, nullptr,
-                                                                  table_g, acc_out, kick, pair_counter, phase,
-                                                                  w.ctl + 2))
+        if (!shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, UNIFORM ? law : d.p, d.cs,
+                                                                  (int)(seg - seg_base[b]), lo, lo + kTMax, k.x, k.y,
+                                                                  spos, perm, cell_off, nullptr, table_g, acc_out,
+                                                                  kick, pair_counter, phase, w.ctl + 2))
             return;
     }
 }
@@ -1267,21 +1275,45 @@ cuco_status_t shortrange_desc_fill(const ShortRangeParams &p, void *desc, uint32
     return CUCO_OK;
 }
 
+bool shortrange_descs_uniform_law(const void *host_descs, int nbox) {
+    const SRBoxDesc *d = static_cast<const SRBoxDesc *>(host_descs);
+    for (int b = 1; b < nbox; ++b) {
+        const ShortRangeParams &x = d[0].p, &y = d[b].p;
+        if (x.rc2_lo != y.rc2_lo || x.rc2_hi != y.rc2_hi || x.hmin2 != y.hmin2 || x.alo != y.alo ||
+            x.ahi != y.ahi || x.rcut2_d != y.rcut2_d || x.asmthfac_d != y.asmthfac_d || x.h != y.h ||
+            x.hinv != y.hinv || x.h3inv != y.h3inv)
+            return false;
+    }
+    return nbox > 0;
+}
+
 cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, const uint32_t *seg_base,
                                       int nbox, uint32_t segments, size_t smem, bool fixed,
                                       const float4 *sorted_pos, const uint32_t *perm, const uint32_t *cell_off,
                                       const float *table, float4 *acc_out, const KickArgs &kick,
-                                      const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter) {
+                                      const SRWork &work, cudaStream_t stream, unsigned long long *pair_counter,
+                                      const void *uniform_law_desc) {
     static const size_t sm_max = smem_base_bytes(kMaxCols, kMaxSeg + 2 * kMaxR) + kMaxSliceTable;
     static bool attr = [] {
-        cudaFuncSetAttribute(k_shortrange_multi<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-        cudaFuncSetAttribute(k_shortrange_multi<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
+#define CUCO_SR_MULTI_ATTR(K, C, F, U) \
+    cudaFuncSetAttribute(k_shortrange_multi<K, C, F, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max)
+        CUCO_SR_MULTI_ATTR(true, true, true, false);
+        CUCO_SR_MULTI_ATTR(true, false, true, false);
+        CUCO_SR_MULTI_ATTR(false, true, true, false);
+        CUCO_SR_MULTI_ATTR(false, false, true, false);
+        CUCO_SR_MULTI_ATTR(true, true, false, false);
+        CUCO_SR_MULTI_ATTR(true, false, false, false);
+        CUCO_SR_MULTI_ATTR(false, true, false, false);
+        CUCO_SR_MULTI_ATTR(false, false, false, false);
+        CUCO_SR_MULTI_ATTR(true, true, true, true);
+        CUCO_SR_MULTI_ATTR(true, false, true, true);
+        CUCO_SR_MULTI_ATTR(false, true, true, true);
+        CUCO_SR_MULTI_ATTR(false, false, true, true);
+        CUCO_SR_MULTI_ATTR(true, true, false, true);
+        CUCO_SR_MULTI_ATTR(true, false, false, true);
+        CUCO_SR_MULTI_ATTR(false, true, false, true);
+        CUCO_SR_MULTI_ATTR(false, false, false, true);
+#undef CUCO_SR_MULTI_ATTR
         return true;
     }();
     (void)attr;
@@ -1294,12 +1326,23 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
     const bool kick_on = kick.vel != nullptr;
     CUCO_TRY_CUDA(cudaMemsetAsync(work.ctl, 0, 2 * sizeof(uint32_t), stream));
     k_sr_plan_multi<<<(segments + 255) / 256, 256, 0, stream>>>(d, seg_base, nbox, segments, cell_off, work);
-#define CUCO_SR_MULTI(K, C, F)                                                                      \
-    do {                                                                                            \
-        const PersistentGrid g = persistent_grid(k_shortrange_multi<K, C, F>, smem);                 \
-        k_shortrange_multi<K, C, F><<<g.sms * g.per, kThreads, smem, stream>>>(                      \
-            d, kicks, seg_base, nbox, segments, work, sorted_pos, perm, cell_off, table, acc_out, kick, \
-            pair_counter);                                                                          \
+    // the shared law (any box's, all being equal) or, unused, box 0's shape
+    ShortRangeParams law{};
+    const bool uniform = uniform_law_desc != nullptr;
+    if (uniform) law = static_cast<const SRBoxDesc *>(uniform_law_desc)->p;
+#define CUCO_SR_MULTI_U(K, C, F, U)                                                                     \
+    do {                                                                                                \
+        const PersistentGrid g = persistent_grid(k_shortrange_multi<K, C, F, U>, smem);                  \
+        k_shortrange_multi<K, C, F, U><<<g.sms * g.per, kThreads, smem, stream>>>(                       \
+            d, kicks, seg_base, nbox, segments, work, sorted_pos, perm, cell_off, table, acc_out, kick,     \
+            pair_counter, law);                                                                         \
+    } while (0)
+#define CUCO_SR_MULTI(K, C, F)                 \
+    do {                                       \
+        if (uniform)                           \
+            CUCO_SR_MULTI_U(K, C, F, true);    \
+        else                                   \
+            CUCO_SR_MULTI_U(K, C, F, false);   \
     } while (0)
     if (fixed) {
         if (kick_on) {
@@ -1315,6 +1358,7 @@ cuco_status_t launch_shortrange_multi(const void *descs, const double2 *kicks, c
         }
     }
 #undef CUCO_SR_MULTI
+#undef CUCO_SR_MULTI_U
     CUCO_TRY_CUDA(cudaGetLastError());
     return CUCO_OK;
 }
