@@ -246,7 +246,10 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 // `law`: the pair law's constants (rc2_lo, rc2_hi, hmin2, alo, ahi, rcut2_d,
 // asmthfac_d, h, hinv, h3inv): the box's own (p), or the launch's when every
 // box of a many-box launch has the same (read from the kernel's parameters).
-template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED>
+// PIN_LAW: the law lives in global memory (a many-box launch's descriptor):
+// its three range bounds are held in registers for a pair's windows, where the
+// compiler would otherwise reload them in every window.
+template <CellFormat FMT, bool KICK, bool COUNT, bool FIXED, bool PIN_LAW = false>
 __device__ __forceinline__ bool shortrange_segment(
     const ShortRangeParams &p, const ShortRangeParams &law, const ColumnSet &cs, const int seg,
     const uint32_t slice_lo,
@@ -512,7 +515,7 @@ __device__ __forceinline__ bool shortrange_segment(
     // acc = false: the flags alone (the revisit of a window with rare-case
     // pairs), nothing added or counted.
     auto pair_fast2 = [&](float4 s, float2 ntx, float2 nty, float2 ntz, float2 &ax, float2 &ay, float2 &az,
-                          bool &slow_a, bool &slow_b, bool acc) {
+                          bool &slow_a, bool &slow_b, bool acc, float rc2_lo, float hmin2, float rc2_hi) {
         const float2 dx = __fadd2_rn(make_float2(s.x, s.x), ntx);
         const float2 dy = __fadd2_rn(make_float2(s.y, s.y), nty);
         const float2 dz = __fadd2_rn(make_float2(s.z, s.z), ntz);
@@ -531,8 +534,8 @@ __device__ __forceinline__ bool shortrange_segment(
         // the bin is the mantissa's low bits (2^23's own are zero)
         const float2 t = make_float2(tab[__float_as_uint(xl.x) & (kTabPad - 1)],
                                      tab[__float_as_uint(xl.y) & (kTabPad - 1)]);
-        const bool fast_a = r2.x <= law.rc2_lo && r2.x >= law.hmin2 && !edge_a;
-        const bool fast_b = r2.y <= law.rc2_lo && r2.y >= law.hmin2 && !edge_b;
+        const bool fast_a = r2.x <= rc2_lo && r2.x >= hmin2 && !edge_a;
+        const bool fast_b = r2.y <= rc2_lo && r2.y >= hmin2 && !edge_b;
         const float2 f = __fmul2_rn(__fmul2_rn(__fmul2_rn(rinv, rinv), rinv), t);
         const float2 fac = make_float2(fast_a ? f.x : 0.f, fast_b ? f.y : 0.f);
         if (acc) {
@@ -543,8 +546,8 @@ __device__ __forceinline__ bool shortrange_segment(
         }
         // r2 == 0 (the self pair, or a coincident source) adds dx*fac = 0:
         // not flagged, so the rare-case branch is not taken once per target
-        slow_a = r2.x <= law.rc2_hi && r2.x != 0.f && !fast_a;
-        slow_b = r2.y <= law.rc2_hi && r2.y != 0.f && !fast_b;
+        slow_a = r2.x <= rc2_hi && r2.x != 0.f && !fast_a;
+        slow_b = r2.y <= rc2_hi && r2.y != 0.f && !fast_b;
     };
     auto pair_slow = [&](float4 s, float tx, float ty, float tz, float &ax, float &ay, float &az) {
         const float dx = s.x - tx, dy = s.y - ty, dz = s.z - tz;
@@ -601,6 +604,8 @@ __device__ __forceinline__ bool shortrange_segment(
                           float &ebx, float &eby, float &ebz) {
         // the pair's sums (A in .x, B in .y) and negated coordinates
         float2 sx = make_float2(0.f, 0.f), sy = sx, sz = sx;
+        float b_lo = law.rc2_lo, b_h = law.hmin2, b_hi = law.rc2_hi;
+        if (PIN_LAW) asm volatile("" : "+f"(b_lo), "+f"(b_h), "+f"(b_hi));
         const float2 ntx = make_float2(-ta.x, -tb.x), nty = make_float2(-ta.y, -tb.y),
                      ntz = make_float2(-ta.z, -tb.z);
         for (int cb = 0; cb < ncols; cb += 32) {
@@ -687,7 +692,7 @@ __device__ __forceinline__ bool shortrange_segment(
                 uint32_t m0;
                 const float4 s0 = window_source(base, before, m0);
                 bool xa, xb;
-                pair_fast2(s0, ntx, nty, ntz, sx, sy, sz, xa, xb, true);
+                pair_fast2(s0, ntx, nty, ntz, sx, sy, sz, xa, xb, true, b_lo, b_h, b_hi);
                 if (__any_sync(kFull, xa || xb)) wslow |= wbit;
                 before += __popc(m0);
             }
@@ -701,7 +706,7 @@ __device__ __forceinline__ bool shortrange_segment(
                 const float4 s0 = window_source(base, __popc(__ballot_sync(kFull, ps < base)), m0);
                 bool xa, xb;
                 float2 unused = make_float2(0.f, 0.f);
-                pair_fast2(s0, ntx, nty, ntz, unused, unused, unused, xa, xb, false);
+                pair_fast2(s0, ntx, nty, ntz, unused, unused, unused, xa, xb, false, b_lo, b_h, b_hi);
                 if (xa) pair_slow(s0, ta.x, ta.y, ta.z, sx.x, sy.x, sz.x);
                 if (xb) pair_slow(s0, tb.x, tb.y, tb.z, sx.y, sy.y, sz.y);
             }
@@ -1072,7 +1077,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks)
         const int b = find_box(seg_base, nbox, seg);
         const SRBoxDesc &d = boxes[b];
         const double2 k = KICK ? kicks[b] : make_double2(0.0, 0.0);
-        if (!shortrange_segment<kCellOffsets, KICK, COUNT, FIXED>(d.p, UNIFORM ? law : d.p, d.cs,
+        if (!shortrange_segment<kCellOffsets, KICK, COUNT, FIXED, !UNIFORM>(d.p, UNIFORM ? law : d.p, d.cs,
                                                                   (int)(seg - seg_base[b]), lo, lo + kTMax, k.x, k.y,
                                                                   spos, perm, cell_off, nullptr, table_g, acc_out,
                                                                   kick, pair_counter, phase, w.ctl + 2))
