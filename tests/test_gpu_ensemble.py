@@ -14,7 +14,7 @@ import pytest
 
 import oracle
 from cuco_gb300 import Box, BoxConfig, fixed_step_schedule, ics
-from cuco_gb300.engine import MODE_FIXED
+from cuco_gb300.engine import MODE_FIXED, MODE_PLAIN
 from cuco_gb300.ensemble import Ensemble
 from conftest import rms_rel
 
@@ -138,6 +138,47 @@ def test_ensemble_graph_steps_track_single_boxes():
         box = Box(BoxConfig(**{**c.__dict__, "cell_grid": ens.plan(b)[0]}))
         box.set_state(ic.pos, ic.canonical_velocity())
         for s in range(5):
+            box.step(drift[s], kick[s])
+        pos1, vel1, _, _ = box.get_state()
+        box.close()
+        assert np.array_equal(pos, pos1) and np.array_equal(vel, vel1), f"box {b} differs from the box alone"
+    ens.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_FIXED])
+def test_ensemble_shared_pair_law_tracks_single_boxes(mode):
+    """Boxes of one configuration (seeds apart) share one pair law, which the
+    short range then takes as a kernel parameter instead of from each box's
+    descriptor; forces and graph-replayed steps still equal each box alone,
+    bit for bit."""
+    ics_, cfgs = make([(16, 32, 60.0, s) for s in (21, 22, 23)], mode)
+    ens = Ensemble(cfgs)
+    for b, ic in enumerate(ics_):
+        ens.set_state(b, ic.pos)
+    ens.forces()
+    for b, (ic, c) in enumerate(zip(ics_, cfgs)):
+        _, _, app, apm = ens.get_state(b)
+        box = Box(BoxConfig(**{**c.__dict__, "cell_grid": ens.plan(b)[0]}))
+        box.set_state(ic.pos)
+        box.forces()
+        _, _, app1, apm1 = box.get_state()
+        box.close()
+        assert np.array_equal(app, app1), f"box {b}: short range differs from the box alone"
+        assert np.array_equal(apm, apm1), f"box {b}: PM differs from the box alone"
+    ens.close()
+
+    ens = Ensemble(cfgs)
+    for b, ic in enumerate(ics_):
+        ens.set_state(b, ic.pos, ic.canonical_velocity())
+    a, drift, kick = fixed_step_schedule(ics_[0].a, 0.05, 3)
+    for s in range(4):  # the first call captures the graph, the rest replay it
+        ens.step(drift[s], kick[s])
+    ens.sync()
+    for b, (ic, c) in enumerate(zip(ics_, cfgs)):
+        pos, vel, _, _ = ens.get_state(b)
+        box = Box(BoxConfig(**{**c.__dict__, "cell_grid": ens.plan(b)[0]}))
+        box.set_state(ic.pos, ic.canonical_velocity())
+        for s in range(4):
             box.step(drift[s], kick[s])
         pos1, vel1, _, _ = box.get_state()
         box.close()
