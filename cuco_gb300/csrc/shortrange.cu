@@ -18,11 +18,12 @@
 //     segment in xy, over z-cells iz0-R .. iz0+S-1+R.  A column's cells are
 //     consecutive keys, so it is at most two contiguous runs of the cell order
 //     (two when the z range wraps); the unit's threads find every cell's
-//     staged offset with one block scan, and warps copy the runs into shared
-//     memory relative to an integer origin at the segment corner, with the
-//     periodic image shift applied once per run (in chunks of kMaxStage
-//     sources; every target runs against each chunk, its sums carried in
-//     shared memory);
+//     staged offset with one block scan, each thread issues one run as a
+//     bulk copy (cp.async.bulk, completing on one mbarrier) into shared
+//     memory, and the staged sources are then moved relative to an integer
+//     origin at the segment corner, with the periodic image shift applied
+//     once per run (in chunks of kMaxStage sources; every target runs
+//     against each chunk, its sums carried in shared memory);
 //   * two consecutive targets per warp: lane k culls column k against the
 //     pair's bounding box in xy and narrows it to the z range
 //     sqrt(rcut^2 - d_xy^2) reaches, trimmed in the two end cells to the z
@@ -827,10 +828,12 @@ __device__ __forceinline__ bool shortrange_segment(
     };
 
     // stage [c0, c1): each run's part is one bulk copy into shared memory,
-    // issued by lane 0 of the warp that owns the run; after the barrier's
-    // phase completes, the warp shifts its runs in place to the origin (the
-    // periodic image shift once per run; fixed point: the int32 offsets from
-    // the corner).  Entered by all threads after a CTA barrier.
+    // issued by one thread (run rr by thread rr mod kThreads); after the
+    // barrier's phase completes, the staged sources are shifted in place to
+    // the origin: all with one shift where no run is a periodic image (and in
+    // fixed point, where the int32 offsets from the corner are the image),
+    // else run by run, one warp per run.  Entered by all threads after a CTA
+    // barrier.
     auto stage = [&](uint32_t c0, uint32_t c1) -> bool {
         if (tid == 0) bar_arrive_expect(&g_stage_bar, (c1 - c0) * (uint32_t)sizeof(float4));
         __syncthreads();
