@@ -487,8 +487,6 @@ __device__ __forceinline__ bool shortrange_segment(
     uint32_t *wdelta = s_wdelta[warp];
     const uint32_t lt_mask = (1u << lane) - 1u, le_mask = lt_mask | (1u << lane);
 
-    // Kernel parameters used per candidate, held in registers.
-
     // The pair law, in two parts.  pair_fast2 takes the common case - inside
     // the cut, away from a table-bin edge and from the cut, outside the
     // softening length - without a branch, and reports the rest (its
@@ -496,8 +494,10 @@ __device__ __forceinline__ bool shortrange_segment(
     // made in double and the spline inside h (the self pair, r = 0, adds
     // nothing and is skipped).  pair_slow applies the full law to those.  Both add into the same
     // accumulators in the same order as a single law would.
-    // The bounds (law.rc2_lo, ...) are kernel parameters where the law is the
-    // launch's, read where used.
+    // The bounds (law.rc2_lo, law.hmin2, law.rc2_hi) are read into registers
+    // once per chunk; where they come from a box's descriptor in global memory
+    // (PIN_LAW), an empty asm statement keeps them there instead of a reload
+    // in every window.
     // bin = floor(asmthfac * r): a round-toward-zero fma onto 2^23 leaves the
     // floor in the mantissa, with no conversion instruction.  Plain: the bins
     // of r * asmthfac * (1 -/+ kEdge) differ when r lies within kEdge
