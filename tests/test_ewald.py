@@ -66,3 +66,16 @@ def test_softened_pair_uses_the_reference_spline(port):
         expect = fs * d - (4 * np.pi / 3) * d / L ** 3
         out.append(np.abs(acc - expect).max() / np.linalg.norm(expect))
     assert max(out) < 1e-7  # the O((d/L)^5) lattice remainder, as for the close pair
+
+
+def test_error_metric():
+    """rms relative error over all components, and the median and 99th
+    percentile of the per-particle relative error (zero reference forces left
+    out)."""
+    from conftest import err_stats
+    ref = np.array([[3.0, 0, 0], [0, 4.0, 0], [0, 0, 0], [1.0, 0, 0]])
+    a = ref + np.array([[0.3, 0, 0], [0, 0, 0.4], [0.5, 0, 0], [0, 0.2, 0]])
+    s = err_stats(a, ref)
+    assert s["rms"] == pytest.approx(np.sqrt((0.09 + 0.16 + 0.25 + 0.04) / 26.0))
+    assert s["median"] == pytest.approx(0.1)  # per particle: 0.1, 0.1, 0.2
+    assert s["p99"] == pytest.approx(np.percentile([0.1, 0.1, 0.2], 99))
