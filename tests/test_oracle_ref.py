@@ -4,6 +4,8 @@ The reference's CPU force path (gravlist.cpp, pm_periodic.c, driftfac.c) is
 compiled from its sources by oracle/Makefile into oracle/_ref/.  These tests
 need the reference sources and are skipped where they are absent.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -23,8 +25,12 @@ def setup_ref(pmgrid, n_side, box_mpc, seed, frac=0.03):
     return ic, ref
 
 
-@pytest.mark.parametrize("pmgrid,n_side,box", [(32, 16, 50.0), (64, 32, 100.0), (128, 32, 100.0)])
+@pytest.mark.parametrize("pmgrid,n_side,box", [(32, 16, 50.0), (64, 32, 100.0), (128, 32, 100.0),
+                                                (512, 32, 100.0)])
 def test_port_forces_bit_exact(port, pmgrid, n_side, box):
+    """Short range and PM of the restatement equal the reference's own, bit for
+    bit, from the smallest mesh to the 512 mesh (the reference built with
+    that PMGRID; its PM takes ~40 s there on one core)."""
     ic, ref = setup_ref(pmgrid, n_side, box, seed=pmgrid)
     pos = ref.get()[0]
     app = ref.pp(1)
@@ -33,6 +39,14 @@ def test_port_forces_bit_exact(port, pmgrid, n_side, box):
     assert p.asmth == np.float32(ref.asmth) and p.rcut == np.float32(ref.rcut)
     assert np.array_equal(port.pp(pos, p, pmgrid, 4), app)
     assert np.array_equal(port.pm(pos, p, pmgrid, 4), apm)
+
+
+@pytest.mark.skipif(os.environ.get("CUCO_ORACLE_LARGE_MESH") != "1",
+                    reason="~7 minutes and ~30 GB of host memory; set CUCO_ORACLE_LARGE_MESH=1")
+def test_port_forces_bit_exact_mesh_1024(port):
+    """The 1024 mesh (the 512^3 workload's): the restatement's PM and short
+    range equal the reference built with PMGRID 1024, bit for bit."""
+    test_port_forces_bit_exact(port, 1024, 32, 100.0)
 
 
 def test_port_pp_threads_and_targets(port):
