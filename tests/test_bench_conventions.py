@@ -3,7 +3,8 @@ algorithmic bytes per phase (sort 28 B/particle + 8 B per cell, deposit 12
 B/particle + 4 B per mesh point, two transforms of two passes each reading and
 writing the half spectrum, interpolation 24 B/particle + three force grids),
 20 FP32 flops per in-range pair, and the HBM peak taken from the measured
-peaks file when present."""
+peaks file when present; and the reference arm's JSON line, which runs on
+the CPU."""
 import json
 import os
 
@@ -36,3 +37,24 @@ def test_hbm_peak_source():
             assert kind == "measured" and hbm == float(json.load(f)["hbm_gbs"])
     else:
         assert kind == "fallback" and hbm == 6800.0
+
+
+def test_reference_arm_line():
+    """`bench.py --impl reference` (the CPU force path, no GPU) prints one JSON
+    line with the GPU arm's metric and unit, `impl`, a cpu_baseline describing
+    the run and an e2e of zero copied bytes; warm-up is held at 3 or more."""
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(bench.__file__))
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"],
+                       cwd=here, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "particle-updates/s" and d["unit"] == "particle-updates/s"
+    assert d["steps"] == 1 and d["warmup"] >= 3 and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["cpu_baseline"]["value"] == d["value"]
+    assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"]
