@@ -3,8 +3,8 @@ algorithmic bytes per phase (sort 28 B/particle + 8 B per cell, deposit 12
 B/particle + 4 B per mesh point, two transforms of two passes each reading and
 writing the half spectrum, interpolation 24 B/particle + three force grids),
 20 FP32 flops per in-range pair, and the HBM peak taken from the measured
-peaks file when present; and the reference arm's JSON line, which runs on
-the CPU."""
+peaks file when present; the clocks record summarised from nvidia-smi
+samples; and the reference arm's JSON line, which runs on the CPU."""
 import json
 import os
 
@@ -58,3 +58,19 @@ def test_reference_arm_line():
     assert d["cpu_baseline"]["kind"] in ("port", "reference") and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"]
+
+
+def test_clock_summary():
+    """The clocks record of the bench line from nvidia-smi samples: the median
+    SM clock under load, the maximum, and every throttle reason seen active
+    (unparseable readings skipped)."""
+    cs = bench.ClockSampler()
+    na, act = "Not Active", "Active"
+    cs.samples = [["2070", "2070", "901.2", na, na, na, na],
+                  ["1980", "2070", "1398.0", na, na, na, act],
+                  ["[N/A]", "2070", "1400.0", na, na, na, act],
+                  ["2055", "[N/A]", "1200.0", na, act, na, na]]
+    s = cs.stop()
+    assert s["sm_mhz"] == 2055.0 and s["sm_max_mhz"] == 2070.0 and s["samples"] == 4
+    assert s["reasons"] == ["hw_thermal_slowdown", "sw_power_cap"]
+    assert bench.ClockSampler().stop()["reasons"] == ["unsampled"]
