@@ -5,6 +5,8 @@ PARTICLE[NumPart] (60 bytes each) raw (read_ic.c:9-45, io.c:9-40):
   file read into the globals and written back as snapshot <num> is the same
   bytes, apart from the redshift that io.c:28 recomputes from All.Time in
   float;
+* a serving job's output snapshot (host code): the same format, read back by
+  read_ic; its drift to the output time as predict.c computes it;
 * cuco_box_load_snapshot / cuco_box_save_snapshot (GPU): a file loaded into a
   box and saved again keeps Pos, Vel and Mass bit for bit and carries the
   box's last forces in GravAccel/GravPM."""
@@ -53,6 +55,65 @@ def test_read_ic_and_savepositions_round_trip(tmp_path):
     same = [0, 1, 2, 4, 5, 6, 7]  # all but the redshift (index 3)
     assert np.array_equal(h_in[same], h_out[same])
     assert h_out[3] == np.float32(np.float32(1) / np.float32(hdr.Time) - np.float32(1))
+
+
+def test_serving_output_snapshot_is_the_reference_format(tmp_path):
+    """A serving job's output snapshot (host code, no GPU): the reference's
+    HEADER + PARTICLE[] with the drifted positions, the velocities and both
+    forces; the drop-in's read_ic reads it as the reference would."""
+    from cuco_gb300.serve import Job, output_positions, write_snapshot
+    ic = _ic()
+    cfg = BoxConfig(n=ic.n, pm_grid=16, boxsize=ic.boxsize, mass=ic.mass, G=ics.G_INTERNAL, softening=1.0)
+    vel = ic.canonical_velocity()
+    job = Job(7, cfg, ic.pos, vel, ic.a, 10, omega0=0.25, omega_lambda=0.75, hubble_param=0.68)
+    rng = np.random.default_rng(5)
+    acc_pp = rng.normal(size=(ic.n, 3)).astype(np.float32)
+    acc_pm = rng.normal(size=(ic.n, 3)).astype(np.float32)
+    # a drift large enough that some particles cross the box edge
+    pos = output_positions(ic.pos, vel, 0.02 * ic.boxsize / float(np.abs(vel).max()), ic.boxsize)
+    assert pos.dtype == np.float32 and pos.min() >= 0 and pos.max() < np.float32(ic.boxsize)
+    path = tmp_path / "job7_out0.cuco"
+    write_snapshot(str(path), job, 0.25, pos, vel, acc_pp, acc_pm)
+    hdr, parts = read_cuco(str(path))
+    assert hdr["NumPart"] == ic.n and hdr["Time"] == np.float32(0.25) and hdr["Redshift"] == np.float32(3.0)
+    assert hdr["BoxSize"] == np.float32(ic.boxsize) and hdr["Mass"] == np.float32(ic.mass)
+    assert (hdr["Omega0"], hdr["OmegaLambda"], hdr["HubbleParam"]) == (np.float32(0.25), np.float32(0.75),
+                                                                        np.float32(0.68))
+    for name, want in (("Pos", pos), ("Vel", vel), ("GravAccel", acc_pp), ("GravPM", acc_pm)):
+        assert np.array_equal(parts[name], want), name
+    assert np.all(parts["Mass"] == np.float32(ic.mass))
+    lib = _native.load()
+    lib.read_ic(str(path).encode())
+    n = ctypes.c_uint.in_dll(lib, "NumPart").value
+    assert n == ic.n
+    p = ctypes.c_void_p.in_dll(lib, "P").value
+    recs = np.frombuffer((ctypes.c_uint8 * (60 * n)).from_address(p), dtype=np.uint8).copy()
+    assert np.array_equal(recs, np.fromfile(path, dtype=np.uint8)[32:])
+
+
+def test_output_positions_follow_predict_c():
+    """The drift to an output time and the box wrapping, element by element
+    as predict.c:19,34-38 computes them (a float position plus a float
+    velocity times a double drift, in double, stored as float; then L added
+    or subtracted in double while outside [0, L))."""
+    from cuco_gb300.serve import output_positions
+    rng = np.random.default_rng(8)
+    L = 20000.0
+    pos = rng.uniform(0, L, (500, 3)).astype(np.float32)
+    pos[:5] = [[0.0, L * (1 - 2 ** -20), 1.0]] * 5
+    vel = rng.normal(0, 300, (500, 3)).astype(np.float32)
+    drift = 3.7
+    got = output_positions(pos, vel, drift, L)
+    want = np.empty_like(pos)
+    for i in range(pos.shape[0]):
+        for j in range(3):
+            x = np.float32(float(pos[i, j]) + float(vel[i, j]) * drift)
+            while x < 0:
+                x = np.float32(float(x) + L)
+            while x >= L:
+                x = np.float32(float(x) - L)
+            want[i, j] = x
+    assert np.array_equal(got, want)
 
 
 @pytest.mark.gpu
