@@ -123,3 +123,43 @@ def test_host_only_entry_points(lib):
     assert lib.cuco_cosmo_factors(-1.0, 1.0, 0.3, 0.7, 0.1, ctypes.byref(d), ctypes.byref(k)) == 1
     assert b"positive" in lib.cuco_last_error()
     assert lib.cuco_version().startswith(b"cuco_gb300")
+
+
+def test_reference_style_hosts_link(lib, tmp_path):
+    """Hosts that keep the reference's calls link against the headers and the
+    library alone: the C++ host with gravlist.cpp's `RadixSort` use
+    (tests/gravlist_host.cpp, run on the GPU by test_gpu_radixsort_host.py),
+    and a C host that defines its own globals as allvars.c does and calls the
+    reference-named drop-in functions in begrun's and run.c's order.  Nothing
+    is run here."""
+    lib_dir = os.path.dirname(_native.LIB_PATH)
+    inc = os.path.join(ROOT, "include")
+    link = ["-L", lib_dir, "-lcuco_gb300", "-Wl,-rpath," + lib_dir]
+    r = subprocess.run(["g++", "-O1", "-std=c++11", "-Wall", "-Werror", "-I", inc,
+                        os.path.join(ROOT, "tests", "gravlist_host.cpp"), *link,
+                        "-o", str(tmp_path / "gravlist_host")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    src = tmp_path / "run_loop.c"
+    src.write_text(r'''
+#include "cuco_gb300.h"
+/* the host's own globals, as allvars.c:7-10 defines them */
+unsigned int NumPart;
+PARTICLE *P;
+HEADER header;
+ALL All;
+int main(int argc, char **argv) {
+    if (argc < 2) return 0;           /* linked, not run */
+    read_ic(argv[1]);
+    init_drift_table();
+    long_range_init();
+    linklist_init();
+    compute_accelerations();
+    move_particles(All.Ti_Current, All.Ti_Current + 1);
+    advance_and_find_timesteps();
+    savepositions(0);
+    return 0;
+}
+''')
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I", inc, str(src), *link,
+                        "-o", str(tmp_path / "run_loop")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
