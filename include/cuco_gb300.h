@@ -198,7 +198,7 @@ typedef enum {
     CUCO_ERR_CUDA = 3,        /* a CUDA call failed; see cuco_last_error() */
     CUCO_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
     CUCO_ERR_STATE = 5,       /* call out of order (e.g. no state uploaded) */
-    CUCO_ERR_UNSUPPORTED = 6  /* configuration this build does not handle */
+    CUCO_ERR_UNSUPPORTED = 6  /* configuration the library does not handle */
 } cuco_status_t;
 
 typedef enum {
