@@ -578,8 +578,9 @@ def run_reference_arm(args, world, rank):
 # ----------------------------------------------------------------- GPU arm
 
 def measured_hbm_gbs():
-    """The HBM copy bandwidth measured on the GB300s (MEASURED_PEAKS.json
-    beside this file), else the fallback figure; and which."""
+    """The HBM copy bandwidth measured on the GB300s the bench runs on
+    (MEASURED_PEAKS.json beside this file), else the fallback figure; and
+    which."""
     try:
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
             return float(json.load(f)["hbm_gbs"]), "measured"
