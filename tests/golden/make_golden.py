@@ -12,12 +12,15 @@ Zel'dovich box (L = 50 Mpc/h, z = 49, PMGRID = 32) and stores:
                   short range (run.c:11-20, accel.c, timestep.c)
   asmth, rcut, G, softening, mass, boxsize, timebase_interval: the constants
 and, in ref_n16_pm32_mixed.npz, eight passes of the run loop on a box whose
-particles take different individual timesteps (see mixed() below).
+particles take different individual timesteps (see mixed() below); and, in
+ref_n32_pm64.npz, the forces of the small workload's box (32^3 particles,
+L = 100 Mpc/h, PMGRID = 64, softening 0.03 of the mean spacing) on a seeded
+subsample of 4096 targets (see small_workload() below).
 The keys/permutation fixture uses the oracle's restatement of calcHashD plus
 a stable sort (the reference computes keys only on the GPU, which does not
 build on CUDA 13); it is pinned by tests/test_oracle_ref.py.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [n16] [n32]   (default: both)
 """
 import os
 import sys
@@ -98,5 +101,30 @@ def mixed():
     print("wrote", path, "Ti:", ti, "steps:", dict(zip(steps.tolist(), counts.tolist())))
 
 
+SMALL_N_SIDE, SMALL_BOX_MPC, SMALL_SEED, SMALL_PMGRID, SMALL_TARGETS = 32, 100.0, 1, 64, 4096
+
+
+def small_workload():
+    """The small workload's box at z = 49: all positions, and the reference's
+    short-range and PM forces on a seeded subsample of targets."""
+    ic = ics.zeldovich(SMALL_N_SIDE, SMALL_BOX_MPC, Z, SMALL_SEED)
+    eps = float(np.float32(0.03 * ic.boxsize / SMALL_N_SIDE))
+    ref = oracle.Reference(SMALL_PMGRID)
+    ref.begrun(ic, soft_comoving=eps)
+    pos = ref.get()[0]
+    acc_pp = ref.pp(8)
+    acc_pm = ref.pm()
+    sub = np.sort(np.random.default_rng(SMALL_TARGETS).choice(ic.n, SMALL_TARGETS, replace=False))
+    out = dict(pos=pos, targets=sub, acc_pp=acc_pp[sub], acc_pm=acc_pm[sub], asmth=ref.asmth, rcut=ref.rcut,
+               G=ref.G, softening=ref.softening, mass=ic.mass, boxsize=ic.boxsize, pmgrid=SMALL_PMGRID, eps=eps)
+    path = os.path.join(HERE, "ref_n32_pm64.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+
+
 if __name__ == "__main__":
-    main()
+    which = sys.argv[1:] or ["n16", "n32"]
+    if "n16" in which:
+        main()
+    if "n32" in which:
+        small_workload()

@@ -48,3 +48,13 @@ def test_golden_keys_and_permutation(port, gold):
     sk, perm = port.stable_sort(keys, G ** 3)
     assert np.array_equal(perm, gold["perm"])
     assert np.array_equal(sk, gold["sorted_keys"])
+
+
+def test_golden_small_workload_bit_exact(port):
+    """The small workload's box (32^3, PMGRID 64): the restatement's short range
+    and PM on the fixture's targets equal the reference's, bit for bit."""
+    g = dict(np.load(os.path.join(HERE, "golden", "ref_n32_pm64.npz")))
+    p = params(g)
+    M, tg = int(g["pmgrid"]), g["targets"]
+    assert np.array_equal(port.pp_targets(g["pos"], tg, p, M, 4), g["acc_pp"])
+    assert np.array_equal(port.pm(g["pos"], p, M, 4)[tg], g["acc_pm"])

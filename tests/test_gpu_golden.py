@@ -1,6 +1,7 @@
 """The GPU path against fixtures produced by the reference's own CPU code
-(tests/golden/make_golden.py): forces at the IC, and three passes of the
-reference's run loop driven through the drop-in C ABI."""
+(tests/golden/make_golden.py): forces at the IC (16^3 with PMGRID 32, and the
+small workload's 32^3 box with PMGRID 64 on a subsample of targets), and
+passes of the reference's run loop driven through the drop-in C ABI."""
 import os
 
 import numpy as np
@@ -34,6 +35,24 @@ def test_forces_vs_reference_fixture(gold, cell_grid):
     print(f"G={cell_grid}: pp {e_pp:.2e} pm {e_pm:.2e}")
     assert e_pp < 1e-4 and e_pm < 1e-4
     box.close()
+
+
+@pytest.mark.parametrize("cell_grid", [64, 16])
+def test_small_workload_forces_vs_reference_fixture(cell_grid):
+    """The small workload's box (32^3, L = 100 Mpc/h, M = 64) against the
+    reference's own forces on the fixture's 4096 targets."""
+    g = dict(np.load(os.path.join(os.path.dirname(FIX), "ref_n32_pm64.npz")))
+    M, tg = int(g["pmgrid"]), g["targets"]
+    box = Box(BoxConfig(n=g["pos"].shape[0], pm_grid=M, cell_grid=cell_grid, boxsize=float(g["boxsize"]),
+                        mass=float(g["mass"]), G=float(g["G"]), softening=float(g["softening"]),
+                        asmth=float(g["asmth"]), rcut=float(g["rcut"])))
+    box.set_state(g["pos"])
+    box.forces()
+    _, _, app, apm = box.get_state()
+    box.close()
+    e_pp, e_pm = rms_rel(app[tg], g["acc_pp"]), rms_rel(apm[tg], g["acc_pm"])
+    print(f"32^3 M=64 G={cell_grid}: pp {e_pp:.2e} pm {e_pm:.2e}")
+    assert e_pp < 1e-4 and e_pm < 1e-4
 
 
 @pytest.mark.parametrize("mirror", ["0", "1"])
