@@ -21,6 +21,24 @@ def gold():
     return dict(np.load(FIX))
 
 
+def test_restatement_on_this_host_vs_fixtures(port, gold):
+    """The oracle's restatement - the checker of the other GPU tests - on the
+    host these tests run on, where the reference's sources are absent: its
+    short range and PM equal the reference-made fixtures bit for bit (this
+    test itself uses no GPU)."""
+    import oracle
+    for g, tg in ((gold, None), (dict(np.load(os.path.join(os.path.dirname(FIX), "ref_n32_pm64.npz"))), "targets")):
+        p = oracle.OpParams(float(g["boxsize"]), float(np.float32(g["mass"])), float(g["G"]),
+                            float(g["asmth"]), float(g["rcut"]), float(g["softening"]))
+        M = int(g["pmgrid"])
+        if tg is None:
+            assert np.array_equal(port.pp(g["pos"], p, M, 4), g["acc_pp"])
+            assert np.array_equal(port.pm(g["pos"], p, M, 4), g["acc_pm"])
+        else:
+            assert np.array_equal(port.pp_targets(g["pos"], g[tg], p, M, 4), g["acc_pp"])
+            assert np.array_equal(port.pm(g["pos"], p, M, 4)[g[tg]], g["acc_pm"])
+
+
 @pytest.mark.parametrize("cell_grid", [32, 16, 8])
 def test_forces_vs_reference_fixture(gold, cell_grid):
     M = int(gold["pmgrid"])
